@@ -1,0 +1,394 @@
+#!/usr/bin/env python
+"""Throughput of qLogNEI value + gradient at the headline point.
+
+Workload: SingleTaskGP (Matern-5/2 ARD, d=20, n=4096 training points,
+y = sum of Branin over 10 coordinate pairs + noise, lengthscales U[0.2, 1])
+and qLogNoisyExpectedImprovement with 512 Sobol samples, evaluated with its
+gradient on b=4096 t-batches of q=8 candidates per step (synthetic, seeded).
+One step = one value+gradient call over the b t-batches with inputs resident
+on the device; L2 is flushed (a 256 MB write) before every timed step.
+
+Reports (one JSON line on rank 0):
+  value      evaluations (t-batches) per second of the mixed-precision path
+  e2e        the same through the public API with host buffers (H2D of X,
+             D2H of value and gradient inside the timed region)
+  roofline   the cross-covariance GEMMs (the dominant kernels), timed live
+  cpu_baseline  the float64 CPU restatement of the reference path (oracle)
+  plus the plain float64 GPU path's throughput and the mixed path's error
+  against the float64 oracle.
+
+``--impl reference`` times the reference's CPU float64 path (its restatement
+under oracle/, since the reference's gpytorch/linear_operator dependencies
+are not installed) on the host cores, on bounded samples of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import torch  # noqa: E402
+
+METRIC = "qLogNEI value+grad evals/sec at n=4096,d=20,q=8 vs plain FP64 GPU @≤1e-5 rel err"
+N_TRAIN, DIM, Q, S, B = 4096, 20, 8, 512, 4096
+WORKLOAD = f"qlognei_branin_d{DIM}_n{N_TRAIN}_q{Q}_S{S}_b{B}"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--b", type=int, default=B)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int) -> None:
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        rows = []
+        if self.path.exists():
+            for line in self.path.read_text().splitlines():
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- workload
+def make_model(device, w):
+    from botorch_gb300 import (ConstantMean, GaussianLikelihood, MaternKernel, ScaleKernel,
+                               SingleTaskGP)
+
+    covar = ScaleKernel(MaternKernel(nu=2.5, ard_num_dims=w.train_X.shape[-1], lengthscale=w.lengthscale),
+                        outputscale=w.outputscale)
+    return SingleTaskGP(w.train_X, w.train_Y, likelihood=GaussianLikelihood(w.noise), covar_module=covar,
+                        mean_module=ConstantMean(w.mean_constant), device=device)
+
+
+def make_acqf(model, w, precision):
+    from botorch_gb300 import SobolQMCNormalSampler, qLogNoisyExpectedImprovement
+
+    torch.manual_seed(0)
+    return qLogNoisyExpectedImprovement(model, w.train_X, sampler=SobolQMCNormalSampler(
+        torch.Size([w.n_samples]), seed=w.seed), precision=precision)
+
+
+def gemm_flops(rows: int, n: int, r: int) -> float:
+    """Algorithmic flops of the two triangular cross-covariance GEMMs of one call.
+
+    Forward V = K(X,Xt) L^-T: rows * n(n+1)/2 multiply-adds, plus the alpha
+    column (rows * n) and P = V Vb^T (rows * n * r); adjoint D = H L^-1: rows *
+    n(n+1)/2. Two flops per multiply-add.
+    """
+    tri = rows * n * (n + 1) / 2
+    return 2.0 * (2 * tri + rows * n + rows * n * r)
+
+
+def traffic_from_profiles() -> float | None:
+    f = ROOT / "profiles" / "crosscov_gemm_traffic.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["dram_bytes_per_launch"])
+        except (ValueError, KeyError):
+            return None
+    return None
+
+
+def measured_peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        return json.loads(f.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def time_steps(fn, steps: int, device, flush) -> list[float]:
+    """Per-step device time (ms) with CUDA events on the launching stream; L2 flushed before each."""
+    stream = torch.cuda.current_stream(device)
+    times = []
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        times.append((e0, e1))
+    torch.cuda.synchronize(device)
+    return [a.elapsed_time(b) for a, b in times]
+
+
+def cpu_baseline(w, model_kw, n_batches: int = 32) -> dict:
+    """The float64 oracle (restatement of the reference path) on the host cores."""
+    from oracle.acquisition import QLogNoisyExpectedImprovement as OQLogNEI
+    from oracle.gp import ExactGP
+
+    om = ExactGP(w.train_X, w.train_Y, w.lengthscale, w.outputscale, w.noise, w.mean_constant, w.kernel)
+    torch.manual_seed(0)
+    oa = OQLogNEI(om, w.train_X, w.n_samples, w.seed)
+    Xs = w.X[:n_batches]
+    oa.value_and_grad(Xs[:2])  # warm-up
+    t0 = time.perf_counter()
+    v, g = oa.value_and_grad(Xs)
+    dt = time.perf_counter() - t0
+    return {"value": n_batches / dt, "unit": "evals/s", "cores": torch.get_num_threads(), "kind": "port",
+            "sample": f"{n_batches} t-batches of the headline workload, value+grad, float64, after init"}, (v, g)
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args) -> None:
+    from botorch_gb300 import _native as nat
+    from botorch_gb300 import testing as T
+
+    world, rank, local = dist_info()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    b = args.b
+    w = T.qlognei_branin(n=N_TRAIN, b=b, q=Q, d=DIM, seed=0)
+    if rank > 0:  # weak scaling: every rank evaluates its own candidates
+        g = torch.Generator().manual_seed(1000 + rank)
+        w.X = torch.rand(b, Q, DIM, generator=g, dtype=torch.float64)
+    model = make_model(device, w)
+    acqf = make_acqf(model, w, "mixed")
+    acqf.check_status = False
+    Xd = w.X.to(device).contiguous()
+    out = (torch.empty(b, dtype=torch.float64, device=device),
+           torch.empty(b, Q, DIM, dtype=torch.float64, device=device),
+           torch.empty(b, dtype=torch.int32, device=device))
+    step = lambda: acqf.value_and_grad_raw(Xd, True, check=False, out=out)  # noqa: E731
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(device)
+    lib = nat.lib()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(device)
+    launches0 = lib.bgb_launch_count()
+    with ClockSampler(local) as clk:
+        t_wall0 = time.perf_counter()
+        step_ms = time_steps(step, args.steps, device, flush)
+        t_wall = time.perf_counter() - t_wall0
+    launches = lib.bgb_launch_count() - launches0
+    torch.cuda.synchronize(device)
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        total_ms = float(t.item())
+    status_ok = int(out[2].max().item()) == 0
+    value = world * b * args.steps / (total_ms / 1e3)
+
+    # roofline of the cross-covariance GEMMs, timed live per stage
+    import ctypes
+    stage = (ctypes.c_float * 7)()
+    acq = acqf._acq_struct(Q)
+    wp, wb = acqf._ws.get(lib.bgb_acq_workspace_bytes(ctypes.byref(acq), b))
+    stage_runs = []
+    for _ in range(3):
+        flush.zero_()
+        rc = lib.bgb_acq_forward_backward_timed(ctypes.byref(acq), Xd.data_ptr(), b, out[0].data_ptr(),
+                                                out[1].data_ptr(), out[2].data_ptr(), wp, wb, stage,
+                                                nat.stream_handle(device))
+        nat.check(rc, "timed call")
+        stage_runs.append(list(stage))
+    st = [statistics.median(s[i] for s in stage_runs) for i in range(7)]
+    names = ["kernel_build", "crosscov_gemm_fwd", "sigma_reduce", "batch_step", "mix_rows",
+             "crosscov_gemm_adj", "adjoint"]
+    peaks = measured_peaks()
+    gemm_ms = st[1] + st[5]
+    flops = gemm_flops(b * Q, N_TRAIN, acqf.r)
+    achieved = flops / (gemm_ms / 1e3) / 1e12 / 2  # per launch: two launches per call
+    per_launch_ms = gemm_ms / 2
+    ach_tflops = (flops / 2) / (per_launch_ms / 1e3) / 1e12
+    traffic = traffic_from_profiles()
+    roofline = {"bound": "tensor", "kernel": "crosscov GEMM (triangular, fwd + adjoint)",
+                "achieved": round(ach_tflops, 3), "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                "frac": round(ach_tflops / peaks.get("bf16_tflops", 1900.0), 5),
+                "traffic": traffic, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
+                "algorithmic_tflop_per_launch": round(flops / 2 / 1e12, 4),
+                "avg_launch_ms": round(per_launch_ms, 4)}
+    del achieved
+
+    # end to end through the public API: pinned host X -> value + grad back on the host
+    Xh = w.X.clone().pin_memory()
+    for _ in range(2):
+        X = Xh.to(device, non_blocking=True).requires_grad_(True)
+        v = acqf(X)
+        (gx,) = torch.autograd.grad(v.sum(), X)
+        v.detach().cpu(), gx.cpu()
+    torch.cuda.synchronize(device)
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        X = Xh.to(device, non_blocking=True).requires_grad_(True)
+        v = acqf(X)
+        (gx,) = torch.autograd.grad(v.sum(), X)
+        vh, gh = v.detach().cpu(), gx.cpu()
+    torch.cuda.synchronize(device)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": round(world * b / e2e_s, 1), "unit": "evals/s", "h2d_bytes_per_step": int(Xh.numel() * 8),
+           "d2h_bytes_per_step": int(vh.numel() * 8 + gh.numel() * 8)}
+    if world > 1:
+        torch.distributed.barrier()
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+
+    # plain float64 GPU path (the denominator of the headline target), smaller b
+    acq64 = make_acqf(model, w, "fp64")
+    acq64.check_status = False
+    b64 = 256
+    X64 = Xd[:b64].contiguous()
+    o64 = (torch.empty(b64, dtype=torch.float64, device=device),
+           torch.empty(b64, Q, DIM, dtype=torch.float64, device=device),
+           torch.empty(b64, dtype=torch.int32, device=device))
+    step64 = lambda: acq64.value_and_grad_raw(X64, True, check=False, out=o64)  # noqa: E731
+    step64()
+    ms64 = statistics.median(time_steps(step64, 3, device, flush))
+    fp64_evals = b64 / (ms64 / 1e3)
+
+    # accuracy of the mixed path against the float64 oracle (and of the fp64 path)
+    cpu = None
+    err = {}
+    if not args.no_cpu_baseline:
+        cpu, (ov, og) = cpu_baseline(w, None, n_batches=32)
+        nb = ov.shape[0]
+        vm, gm_ = out[0][:nb].cpu(), out[1][:nb].cpu()
+        err = {"value_rel_err_mixed": float((vm - ov).norm() / ov.norm()),
+               "grad_rel_err_mixed": float((gm_ - og).norm() / og.norm()),
+               "value_rel_err_fp64": float((o64[0][:nb].cpu() - ov).norm() / ov.norm()),
+               "grad_rel_err_fp64": float((o64[1][:nb].cpu() - og).norm() / og.norm()),
+               "error_sample": f"first {nb} t-batches vs float64 oracle, norm-wise"}
+
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "evals/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded Branin-sum GP workload)",
+        "config": {"workload": WORKLOAD, "n": N_TRAIN, "d": DIM, "q": Q, "mc_samples": S,
+                   "batch_per_call": b, "baseline_points_r": acqf.r, "kernel": "matern52",
+                   "precision": "mixed: f32 kernel build + cross-covariance GEMMs, f64 Cholesky/"
+                                "sample step/log-mean-exp", "l2": "flushed before each step (256 MB write)",
+                   "parallelism": f"replicas, weak scaling over t-batches x{world}"},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "stage_ms": {k: round(v, 4) for k, v in zip(names, st)},
+        "fp64_gpu_evals_per_s": round(fp64_evals, 1),
+        "speedup_vs_fp64_gpu": round(value / world / fp64_evals, 2),
+        "status_ok": status_ok, "wall_s_timed": round(t_wall, 3), **err,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(args) -> None:
+    world, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from botorch_gb300 import testing as T
+    from oracle.acquisition import QLogNoisyExpectedImprovement as OQLogNEI
+    from oracle.gp import ExactGP
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    w = T.qlognei_branin(n=N_TRAIN, b=args.b, q=Q, d=DIM, seed=0)
+    om = ExactGP(w.train_X, w.train_Y, w.lengthscale, w.outputscale, w.noise, w.mean_constant, w.kernel)
+    torch.manual_seed(0)
+    oa = OQLogNEI(om, w.train_X, w.n_samples, w.seed)
+    per_step = 8
+    for i in range(max(args.warmup, 1)):
+        oa.value_and_grad(w.X[i * per_step:(i + 1) * per_step])
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        j = (i * per_step) % (args.b - per_step)
+        oa.value_and_grad(w.X[j:j + per_step])
+    dt = time.perf_counter() - t0
+    value = per_step * args.steps / dt
+    cores = torch.get_num_threads()
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Branin-sum GP workload)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "n": N_TRAIN, "d": DIM, "q": Q, "mc_samples": S,
+                       "batch_per_call": args.b, "parallelism": "host CPU, rank 0"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "evals/s", "cores": cores, "kind": "port",
+                             "sample": f"{per_step} t-batches per step, value+grad, float64"},
+            "e2e": {"value": round(value, 3), "unit": "evals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference CPU float64 path via its restatement in oracle/ (gpytorch and "
+                    "linear_operator, which hold the reference's arithmetic, are not installable offline)"}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,327 @@
+"""qExpectedImprovement and qLogNoisyExpectedImprovement on the CUDA library.
+
+The classes keep the reference's constructor arguments and ``forward``
+contract (``batch_shape x q x d`` -> ``batch_shape``) so they drop into
+``optimize_acqf`` / ``gen_candidates_scipy`` (botorch/generation/gen.py:423-487).
+``forward`` is differentiable in X: when X requires grad, one fused call
+computes the value and the hand-written adjoint gradient, and the gradient is
+handed to autograd by ``_FusedValueGrad``.
+
+References: botorch/acquisition/monte_carlo.py:268-305 and :374-437 (qEI),
+botorch/acquisition/logei.py:246-565 (qLogNEI with cached root),
+botorch/acquisition/cached_cholesky.py:126-192, botorch/utils/low_rank.py:84-172,
+botorch/acquisition/utils.py:97-141 and :347-437 (best_f and pruning).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+import torch
+from torch import Tensor
+
+from botorch_gb300 import _native as nat
+from botorch_gb300.exceptions import NanError, NotPSDError, UnsupportedError
+from botorch_gb300.gp_regression import SingleTaskGP
+from botorch_gb300.sampling import SobolQMCNormalSampler, draw_sobol_normal_samples
+
+TAU_RELU = 1e-6
+TAU_MAX = 1e-2
+
+
+class _FusedValueGrad(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, X: Tensor, acqf: "_MCAcquisition") -> Tensor:
+        need_grad = ctx.needs_input_grad[0]
+        value, grad = acqf._run(X, need_grad)
+        if need_grad:
+            ctx.save_for_backward(grad)
+        return value
+
+    @staticmethod
+    def backward(ctx, g: Tensor):
+        (grad,) = ctx.saved_tensors
+        return g.reshape(*g.shape, 1, 1) * grad, None
+
+
+class _MCAcquisition:
+    """Shared plumbing: t-batch handling, device buffers, C ABI calls."""
+
+    acqf_id = -1
+
+    def __init__(self, model: SingleTaskGP, sampler: SobolQMCNormalSampler | None,
+                 objective, posterior_transform, constraints, precision: str) -> None:
+        if not isinstance(model, SingleTaskGP):
+            raise UnsupportedError("model must be a botorch_gb300 SingleTaskGP")
+        if objective is not None and type(objective).__name__ != "IdentityMCObjective":
+            raise UnsupportedError("only the identity MC objective is supported on this path")
+        if posterior_transform is not None or constraints is not None:
+            raise UnsupportedError("posterior transforms and constraints are not supported")
+        if precision not in nat.PRECISIONS:
+            raise ValueError(f"precision must be one of {list(nat.PRECISIONS)}")
+        self.model = model
+        self.sampler = sampler
+        self.precision = precision
+        self.device = model.device
+        self._ws = nat.Workspace(self.device)
+        self._Z: dict[int, Tensor] = {}
+        self.check_status = True
+        self.use_tensor_cores = True  # mixed path: tcgen05 GEMMs (False: FFMA GEMMs)
+        self.X_pending: Tensor | None = None
+
+    # -------------------------------------------------------------- override
+    def _base_samples(self, q: int) -> Tensor:
+        raise NotImplementedError
+
+    def _acq_struct(self, q: int) -> nat.BgbAcq:
+        raise NotImplementedError
+
+    # ------------------------------------------------------------------ call
+    def __call__(self, X: Tensor) -> Tensor:
+        return self.forward(X)
+
+    def forward(self, X: Tensor) -> Tensor:
+        if X.dim() < 2:
+            raise ValueError(f"{type(self).__name__} requires X to have at least 2 dimensions,"
+                             f" but received X with only {X.dim()} dimensions.")
+        X3 = X if X.dim() > 2 else X.unsqueeze(0)
+        return _FusedValueGrad.apply(X3, self)
+
+    def _prepare_X(self, X: Tensor) -> Tensor:
+        return X
+
+    def _run(self, X: Tensor, need_grad: bool) -> tuple[Tensor, Tensor | None]:
+        batch_shape = X.shape[:-2]
+        Xf = self._prepare_X(X)
+        q, d = Xf.shape[-2], Xf.shape[-1]
+        if d != self.model.d:
+            raise ValueError(f"expected d={self.model.d}, got {d}")
+        Xd = Xf.detach().reshape(-1, q, d).to(self.device, torch.float64).contiguous()
+        b = Xd.shape[0]
+        value, grad = self.value_and_grad_raw(Xd, need_grad)
+        value = value.reshape(batch_shape).to(X.dtype)
+        if grad is not None:
+            grad = grad[:, : X.shape[-2], :]  # pending points (appended last) carry no gradient
+            grad = grad.reshape(X.shape).to(X.dtype)
+        return value, grad
+
+    def value_and_grad_raw(self, Xd: Tensor, need_grad: bool, check: bool | None = None,
+                           out: tuple | None = None):
+        """Native call on a contiguous float64 ``b x q x d`` device tensor."""
+        lib = nat.lib()
+        b, q, d = Xd.shape
+        if b == 0:
+            empty = torch.empty(0, dtype=torch.float64, device=self.device)
+            return empty, (torch.empty(0, q, d, dtype=torch.float64, device=self.device) if need_grad else None)
+        acq = self._acq_struct(q)
+        if out is None:
+            value = torch.empty(b, dtype=torch.float64, device=self.device)
+            grad = torch.empty(b, q, d, dtype=torch.float64, device=self.device) if need_grad else None
+            status = torch.empty(b, dtype=torch.int32, device=self.device)
+        else:
+            value, grad, status = out
+        wp, wb = self._ws.get(lib.bgb_acq_workspace_bytes(ctypes.byref(acq), b))
+        stream = nat.stream_handle(self.device)
+        if need_grad:
+            rc = lib.bgb_acq_forward_backward(ctypes.byref(acq), nat.ptr(Xd), b, nat.ptr(value),
+                                              nat.ptr(grad), nat.ptr(status), wp, wb, stream)
+        else:
+            rc = lib.bgb_acq_forward(ctypes.byref(acq), nat.ptr(Xd), b, nat.ptr(value),
+                                     nat.ptr(status), wp, wb, stream)
+        nat.check(rc, type(self).__name__)
+        if (self.check_status if check is None else check):
+            worst = int(status.max().item()) if b > 0 else 0
+            if worst == nat.BGB_NOT_PSD:
+                raise NotPSDError("q x q posterior covariance not positive definite after jitter")
+            if worst == nat.BGB_NAN:
+                raise NanError("Samples contain nans or infs.")
+            if worst == nat.BGB_DEVICE_TIMEOUT:
+                raise RuntimeError("a bounded wait in a tensor-core GEMM expired")
+        return value, grad
+
+    def _device_Z(self, q: int) -> Tensor:
+        if q not in self._Z:
+            self._Z[q] = self._base_samples(q).to(self.device, torch.float64).contiguous()
+        return self._Z[q]
+
+
+class qExpectedImprovement(_MCAcquisition):
+    """MC-based batch Expected Improvement (botorch/acquisition/monte_carlo.py:374-437).
+
+    qEI(X) = mean_s max_q (Y_s - best_f)_+ with Y_s = mu + chol(Sigma) z_s.
+    """
+
+    acqf_id = nat.ACQF_QEI
+
+    def __init__(self, model: SingleTaskGP, best_f: float | Tensor,
+                 sampler: SobolQMCNormalSampler | None = None, objective=None,
+                 posterior_transform=None, X_pending: Tensor | None = None, constraints=None,
+                 eta: float = 1e-3, precision: str = "mixed") -> None:
+        super().__init__(model, sampler, objective, posterior_transform, constraints, precision)
+        bf = torch.as_tensor(best_f, dtype=torch.float64)
+        if bf.numel() != 1:
+            raise UnsupportedError("a scalar best_f is supported")
+        self.best_f = bf.reshape(())
+        self._best_f_dev = bf.reshape(1).to(self.device)
+        self.set_X_pending(X_pending)
+
+    def set_X_pending(self, X_pending: Tensor | None = None) -> None:
+        self.X_pending = None if X_pending is None else X_pending.detach().clone()
+
+    def _prepare_X(self, X: Tensor) -> Tensor:
+        if self.X_pending is None:
+            return X
+        Xp = self.X_pending.to(X).expand(*X.shape[:-2], *self.X_pending.shape)
+        return torch.cat([X, Xp], dim=-2)
+
+    def _base_samples(self, q: int) -> Tensor:
+        if self.sampler is None:
+            self.sampler = SobolQMCNormalSampler(torch.Size([512]))
+        return self.sampler.base_samples(q)
+
+    def _acq_struct(self, q: int) -> nat.BgbAcq:
+        m = self.model
+        Z = self._device_Z(q)
+        return nat.BgbAcq(acqf=nat.ACQF_QEI, q=q, r=0, n_samples=Z.shape[0], Z=nat.ptr(Z),
+                          best_f=nat.ptr(self._best_f_dev), tau_relu=TAU_RELU, tau_max=TAU_MAX,
+                          **m.acq_struct_base(self.precision, self.use_tensor_cores))
+
+
+def prune_inferior_points(model: SingleTaskGP, X: Tensor, num_samples: int = 2048,
+                          max_frac: float = 1.0, sampler: SobolQMCNormalSampler | None = None) -> Tensor:
+    """Points of X that are the sampled argmax at least once (acquisition/utils.py:347-437).
+
+    The posterior, its psd_safe_cholesky, the samples and the argmax counts
+    run in the CUDA library; the sampler seed comes from the global torch RNG
+    when no sampler is given, as in the reference.
+    """
+    if X.dim() != 2:
+        raise UnsupportedError("Batched inputs `X` are currently unsupported by `prune_inferior_points`")
+    if X.shape[-2] == 0:
+        raise ValueError("X must have at least one point.")
+    if max_frac <= 0 or max_frac > 1.0:
+        raise ValueError(f"max_frac must take values in (0, 1], is {max_frac}")
+    max_points = math.ceil(max_frac * X.shape[-2])
+    m = X.shape[0]
+    if sampler is None:
+        sampler = SobolQMCNormalSampler(torch.Size([num_samples]))
+    Z = sampler.base_samples(m).to(model.device).contiguous()
+    Xd = X.detach().to(model.device, torch.float64).contiguous()
+    counts = torch.empty(m, dtype=torch.int32, device=model.device)
+    lib = nat.lib()
+    ws = nat.Workspace(model.device)
+    wp, wb = ws.get(lib.bgb_prune_counts_workspace_bytes(model.n, m, sampler.num_samples))
+    gp = model.gp_struct()
+    with torch.cuda.device(model.device):
+        rc = lib.bgb_prune_counts(ctypes.byref(gp), nat.ptr(model.Linv), nat.ptr(model.alpha),
+                                  nat.ptr(Xd), m, nat.ptr(Z), sampler.num_samples, 6,
+                                  nat.ptr(counts), wp, wb, nat.stream_handle(model.device))
+    nat.check(rc, "prune_inferior_points")
+    counts = counts.cpu()
+    idcs = torch.nonzero(counts > 0).squeeze(-1)
+    if len(idcs) > max_points:
+        # the reference's ordering step (acquisition/utils.py:432-434)
+        sel_counts, order_idcs = torch.sort(counts[idcs], stable=True, descending=True)
+        idcs = order_idcs[:max_points]
+    return X[idcs.to(X.device)]
+
+
+class qLogNoisyExpectedImprovement(_MCAcquisition):
+    """MC-based batch Log Noisy Expected Improvement with cached root (logei.py:246-565)."""
+
+    acqf_id = nat.ACQF_QLOGNEI
+
+    def __init__(self, model: SingleTaskGP, X_baseline: Tensor,
+                 sampler: SobolQMCNormalSampler | None = None, objective=None,
+                 posterior_transform=None, X_pending: Tensor | None = None, constraints=None,
+                 eta: float = 1e-3, fat: bool = True, prune_baseline: bool = True,
+                 cache_root: bool | None = None, tau_max: float = TAU_MAX,
+                 tau_relu: float = TAU_RELU, marginalize_dim: int | None = None,
+                 incremental: bool = True, precision: str = "mixed") -> None:
+        super().__init__(model, sampler, objective, posterior_transform, constraints, precision)
+        if not fat:
+            raise UnsupportedError("fat=False (logsumexp q-reduction) is not supported on this path")
+        if cache_root is False:
+            raise UnsupportedError("only the cached-root form is implemented on this path")
+        if not incremental:
+            raise UnsupportedError("incremental=False is not supported on this path")
+        if not (tau_max > 0 and tau_relu > 0):
+            raise ValueError("tau_max and tau_relu must be positive")
+        self.tau_max = float(tau_max)
+        self.tau_relu = float(tau_relu)
+        self.prune_baseline = prune_baseline
+        self._init_baseline(X_baseline, X_pending)
+
+    def _init_baseline(self, X_baseline: Tensor, X_pending: Tensor | None) -> None:
+        m = self.model
+        X_baseline = X_baseline.detach()
+        if self.prune_baseline:
+            X_baseline = prune_inferior_points(m, X_baseline)
+        self._X_baseline = X_baseline
+        full = X_baseline if X_pending is None else torch.cat([X_baseline, X_pending.detach().to(X_baseline)], dim=-2)
+        self._full_X_baseline = full
+        if self.sampler is None:
+            self.sampler = SobolQMCNormalSampler(torch.Size([512]))
+        r = full.shape[0]
+        self.r = r
+        S = self.sampler.num_samples
+        dev = self.device
+        self._Xb = full.to(dev, torch.float64).contiguous()
+        Zb = self.sampler.base_samples(r)
+        self._Zb = Zb
+        self._Lb = torch.empty(r, r, dtype=torch.float64, device=dev)
+        self._Lb_inv = torch.empty(r, r, dtype=torch.float64, device=dev)
+        self._best_f = torch.empty(S, dtype=torch.float64, device=dev)
+        Zb_dev = Zb.to(dev).contiguous()
+        lib = nat.lib()
+        ws = nat.Workspace(dev)
+        wp, wb = ws.get(lib.bgb_qlognei_baseline_workspace_bytes(m.n, r, S))
+        jit = ctypes.c_double(0.0)
+        gp = m.gp_struct()
+        with torch.cuda.device(dev):
+            rc = lib.bgb_qlognei_baseline(ctypes.byref(gp), nat.ptr(m.Linv), nat.ptr(m.alpha),
+                                          nat.ptr(self._Xb), r, nat.ptr(Zb_dev), S, 6,
+                                          nat.ptr(self._Lb), nat.ptr(self._Lb_inv),
+                                          nat.ptr(self._best_f), ctypes.byref(jit), wp, wb,
+                                          nat.stream_handle(dev))
+        nat.check(rc, "qLogNEI baseline")
+        self.baseline_jitter = jit.value
+        self._Vb64, self._Vb32, self._VbT64, self._VbT32 = m.baseline_operands(self._Xb, self.precision)
+        self._Z = {}
+
+    @property
+    def X_baseline(self) -> Tensor:
+        return self._full_X_baseline
+
+    @property
+    def best_f(self) -> Tensor:
+        """Per-sample incumbent max over the baseline samples (acquisition/utils.py:137-141)."""
+        return self._best_f
+
+    def set_X_pending(self, X_pending: Tensor | None = None) -> None:
+        """Pending points join the baseline (incremental qLogNEI, logei.py:470-499)."""
+        if X_pending is None and self._full_X_baseline.shape[-2] == self._X_baseline.shape[-2]:
+            return
+        saved = self.prune_baseline
+        self.prune_baseline = False
+        try:
+            self._init_baseline(self._X_baseline, X_pending)
+        finally:
+            self.prune_baseline = saved
+
+    def _base_samples(self, q: int) -> Tensor:
+        """S x (r+q): the (r+q)-dim draw with its first r columns replaced by the baseline draw."""
+        full = draw_sobol_normal_samples(self.r + q, self.sampler.num_samples, self.sampler.seed)
+        full[:, : self.r] = self._Zb
+        return full
+
+    def _acq_struct(self, q: int) -> nat.BgbAcq:
+        m = self.model
+        Z = self._device_Z(q)
+        return nat.BgbAcq(acqf=nat.ACQF_QLOGNEI, q=q, r=self.r, n_samples=Z.shape[0],
+                          Vb64=nat.ptr(self._Vb64), Vb32=nat.ptr(self._Vb32),
+                          VbT64=nat.ptr(self._VbT64), VbT32=nat.ptr(self._VbT32),
+                          X_baseline=nat.ptr(self._Xb), Lb_inv=nat.ptr(self._Lb_inv), Z=nat.ptr(Z),
+                          best_f=nat.ptr(self._best_f), tau_relu=self.tau_relu, tau_max=self.tau_max,
+                          **m.acq_struct_base(self.precision, self.use_tensor_cores))

@@ -1,0 +1,62 @@
+// Arguments of the per-t-batch kernels (device pointers, float64 unless noted).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bgb {
+
+constexpr int kMaxQ = 32;  // largest q of the fused per-batch kernel
+
+struct QBatchArgs {
+    int64_t b;          // t-batches
+    int64_t n;          // training points
+    int q, r, S, d;
+    int kernel;
+    int acqf;
+    int max_tries;
+    double jitter;      // first jitter of psd_safe_cholesky (float64: 1e-8)
+    double outputscale, mean_constant, y_mean, y_std;
+    double tau_relu, tau_max;
+    const double* X;        // b*q x d candidates
+    const double* Xt;       // n x d training inputs
+    const double* Xb;       // r x d baseline
+    const double* inv_ls;   // d
+    const double* Lb_inv;   // r x r
+    const double* Z;        // S x (r+q)
+    const double* best_f;   // S (qLogNEI) or 1 (qEI)
+    // intermediates (standardised space)
+    double* sig;            // b x q x q
+    double* sqb;            // b x q x r
+    double* mu;             // b x q
+    double* gqq;            // b x q x q   d value / d Sigma_qq (standardised)
+    double* gqb;            // b x q x r
+    double* gmu;            // b x q
+    // outputs
+    double* value;          // b
+    double* grad;           // b x q x d
+    int32_t* status;        // b
+    const int* dev_err;     // non-zero: a bounded wait in a tensor-core GEMM expired
+};
+
+// mu (into a.mu) = m + V beta and P (b*q x r) = V Vb^T
+template <typename T>
+int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb, T* P,
+                    cudaStream_t stream);
+// P: b*q x r (V Vb^T) or null when r = 0; C: b*q x ldc holding V.
+template <typename T>
+int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc,
+                        cudaStream_t stream);
+int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream);
+size_t batch_step_smem_bytes(int q, int r, int S);
+// H (b*q x n) = gmu beta^T - 2 Gqq V - Gqb Vb per t-batch
+// H_lo non-null (float32): write the tf32 hi/lo split (H = hi) with leading dimension ldh.
+template <typename T>
+int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, const T* beta, T* H,
+                    cudaStream_t stream, T* H_lo = nullptr, int64_t ldh = 0);
+// d value / d X from D (b*q x n) = H L^-1
+template <typename T>
+int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, cudaStream_t stream);
+int launch_posterior_out(const QBatchArgs& a, double* mean, double* covar, cudaStream_t stream);
+
+}  // namespace bgb

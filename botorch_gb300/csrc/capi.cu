@@ -1,0 +1,559 @@
+// extern "C" entry points of libbotorch_gb300.so (declared in include/botorch_gb300.h).
+#include <math.h>
+#include <string.h>
+
+#include <atomic>
+
+#include "bgb_common.cuh"
+#include "bgb_kernels.cuh"
+#include "bgb_qbatch.cuh"
+
+using namespace bgb;
+
+namespace bgb {
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace bgb
+
+namespace {
+
+__global__ void sub_const_kernel(const double* x, double c, double* y, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i] - c;
+}
+
+// B = [Linv^T | 0]: B[k][j] = Linv[j][k] for j < n
+__global__ void fill_b_kernel(const double* Linv, int64_t n, double* B, int64_t ldb) {
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * ldb) return;
+    int64_t k = idx / ldb, j = idx % ldb;
+    B[idx] = (j < n) ? Linv[j * n + k] : 0.0;
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int valid_gp(const bgb_gp_t* gp) {
+    if (gp == nullptr || gp->n <= 0 || gp->d <= 0 || gp->train_X == nullptr ||
+        gp->inv_lengthscale == nullptr)
+        return 0;
+    if (gp->kernel < BGB_KERNEL_MATERN52 || gp->kernel > BGB_KERNEL_RBF) return 0;
+    return 1;
+}
+
+// The mixed path runs its GEMMs on the tensor cores when the tf32 operands are set.
+bool use_tc(const bgb_acq_t* a) {
+    return a->precision == BGB_PREC_MIXED && !(a->flags & BGB_FLAG_SIMT) && a->Lhi != nullptr &&
+           a->Llo != nullptr && a->LThi != nullptr && a->LTlo != nullptr && a->ldl >= a->gp.n &&
+           (a->ldl % 8) == 0 && (a->ldb % 4) == 0 && tc_gemm_available();
+}
+
+// Workspace of one call: Kc (later H) rows x n (tensor-core path: hi and lo,
+// rows x ldl each), C = V (later D) rows x ldb, P rows x r, the float64
+// per-batch blocks and the device error word.
+size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, void** Kc,
+                     void** C, void** P, int** err = nullptr) {
+    const int64_t n = a->gp.n;
+    const int64_t rows = b * a->q;
+    const int64_t rr = a->r > 0 ? a->r : 1;
+    const size_t es = (a->precision == BGB_PREC_MIXED) ? sizeof(float) : sizeof(double);
+    const bool tc = use_tc(a);
+    const int64_t kc_elems = tc ? 2 * rows * a->ldl : rows * n;
+    size_t total = 0;
+    total += align_up(kc_elems * es);
+    total += align_up(rows * a->ldb * es);
+    total += align_up(rows * rr * es);
+    total += align_up(sizeof(double) * b * a->q * a->q) * 2;
+    total += align_up(sizeof(double) * b * a->q * rr) * 2;
+    total += align_up(sizeof(double) * b * a->q) * 2;
+    total += align_up(sizeof(int));
+    if (ar == nullptr) return total;
+    if (ar->cap < total) return 0;
+    if (es == sizeof(float)) {
+        *Kc = ar->take<float>(kc_elems);
+        *C = ar->take<float>(rows * a->ldb);
+        *P = ar->take<float>(rows * rr);
+    } else {
+        *Kc = ar->take<double>(kc_elems);
+        *C = ar->take<double>(rows * a->ldb);
+        *P = ar->take<double>(rows * rr);
+    }
+    qa->sig = ar->take<double>(b * a->q * a->q);
+    qa->gqq = ar->take<double>(b * a->q * a->q);
+    qa->sqb = ar->take<double>(b * a->q * rr);
+    qa->gqb = ar->take<double>(b * a->q * rr);
+    qa->mu = ar->take<double>(b * a->q);
+    qa->gmu = ar->take<double>(b * a->q);
+    int* e = ar->take<int>(1);
+    if (err != nullptr) *err = e;
+    return total;
+}
+
+void fill_qargs(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa) {
+    qa->b = b;
+    qa->n = a->gp.n;
+    qa->q = a->q;
+    qa->r = a->r;
+    qa->S = a->n_samples;
+    qa->d = a->gp.d;
+    qa->kernel = a->gp.kernel;
+    qa->acqf = a->acqf;
+    qa->max_tries = 6;     // botorch/__init__.py:54, utils/low_rank.py:90
+    qa->jitter = 1e-8;     // float64 jitter of psd_safe_cholesky
+    qa->outputscale = a->gp.outputscale;
+    qa->mean_constant = a->gp.mean_constant;
+    qa->y_mean = a->gp.y_mean;
+    qa->y_std = a->gp.y_std;
+    qa->tau_relu = a->tau_relu;
+    qa->tau_max = a->tau_max;
+    qa->X = X;
+    qa->Xt = a->gp.train_X;
+    qa->Xb = a->X_baseline;
+    qa->inv_ls = a->gp.inv_lengthscale;
+    qa->Lb_inv = a->Lb_inv;
+    qa->Z = a->Z;
+    qa->best_f = a->best_f;
+}
+
+int valid_acq(const bgb_acq_t* a) {
+    if (a == nullptr || !valid_gp(&a->gp)) return 0;
+    if (a->q <= 0 || a->r < 0 || a->ldb < a->gp.n) return 0;
+    if (a->precision == BGB_PREC_FP64) {
+        if (a->B64 == nullptr || a->Linv64 == nullptr || a->beta64 == nullptr) return 0;
+        if (a->r > 0 && (a->Vb64 == nullptr || a->VbT64 == nullptr)) return 0;
+    } else if (a->precision == BGB_PREC_MIXED) {
+        if (a->B32 == nullptr || a->Linv32 == nullptr || a->beta32 == nullptr) return 0;
+        if (a->r > 0 && (a->Vb32 == nullptr || a->VbT32 == nullptr)) return 0;
+    } else {
+        return 0;
+    }
+    if (a->r > 0 && (a->X_baseline == nullptr || a->Lb_inv == nullptr)) return 0;
+    return 1;
+}
+
+// Typed pieces of the per-call pipeline.
+template <typename T> struct Ops;
+template <> struct Ops<float> {
+    static const float* B(const bgb_acq_t* a) { return a->B32; }
+    static const float* Linv(const bgb_acq_t* a) { return a->Linv32; }
+    static const float* Vb(const bgb_acq_t* a) { return a->Vb32; }
+    static const float* VbT(const bgb_acq_t* a) { return a->VbT32; }
+    static const float* beta(const bgb_acq_t* a) { return a->beta32; }
+    static int gemm(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,
+                    int64_t ldb, float* C, int64_t ldc, int kmode, int64_t n_tri, cudaStream_t st) {
+        return gemm_f32(M, N, K, A, lda, B, ldb, C, ldc, kmode, n_tri, st);
+    }
+    static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, float* K, cudaStream_t st) {
+        return launch_kernel_matrix<double, float, float>(X, rows, a->gp.train_X, a->gp.n, a->gp.d,
+                                                          a->gp.inv_lengthscale, a->gp.outputscale,
+                                                          a->gp.kernel, 0.0, 0, K, a->gp.n, st);
+    }
+};
+template <> struct Ops<double> {
+    static const double* B(const bgb_acq_t* a) { return a->B64; }
+    static const double* Linv(const bgb_acq_t* a) { return a->Linv64; }
+    static const double* Vb(const bgb_acq_t* a) { return a->Vb64; }
+    static const double* VbT(const bgb_acq_t* a) { return a->VbT64; }
+    static const double* beta(const bgb_acq_t* a) { return a->beta64; }
+    static int gemm(int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
+                    const double* B, int64_t ldb, double* C, int64_t ldc, int kmode, int64_t n_tri,
+                    cudaStream_t st) {
+        return gemm_f64(M, N, K, 1.0, A, lda, 0, B, ldb, 0, 0.0, C, ldc, kmode, 0, nullptr, st,
+                        n_tri);
+    }
+    static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, double* K,
+                    cudaStream_t st) {
+        return launch_kernel_matrix<double, double, double>(
+            X, rows, a->gp.train_X, a->gp.n, a->gp.d, a->gp.inv_lengthscale, a->gp.outputscale,
+            a->gp.kernel, 0.0, 0, K, a->gp.n, st);
+    }
+};
+
+// Kernel build, V = K(X,Xt) L^-T, mu = m + V beta and P = V Vb^T, covariance reduction.
+template <typename T>
+int run_front(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa, T* Kc, T* C, T* P,
+              cudaStream_t st, cudaEvent_t* ev) {
+    const int64_t n = a->gp.n, rows = b * a->q;
+    if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[0], st));
+    int rc;
+    if constexpr (sizeof(T) == 4) {
+        if (use_tc(a)) {
+            // tensor cores: K(X, Xt) as its tf32 split, then V = K L^-T
+            float* Khi = Kc;
+            float* Klo = Kc + rows * a->ldl;
+            rc = launch_kernel_matrix<double, float, float>(
+                X, rows, a->gp.train_X, n, a->gp.d, a->gp.inv_lengthscale, a->gp.outputscale,
+                a->gp.kernel, 0.0, 0, Khi, a->ldl, st, Klo);
+            if (rc) return rc;
+            if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[1], st));
+            rc = tc_gemm_tf32x3(rows, n, n, Khi, Klo, a->ldl, a->Lhi, a->Llo, a->ldl, C, a->ldb,
+                                KB_UPPER, const_cast<int*>(qa->dev_err), st);
+            if (rc) return rc;
+            goto after_gemm;
+        }
+    }
+    rc = Ops<T>::kmat(a, X, rows, Kc, st);
+    if (rc) return rc;
+    if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[1], st));
+    rc = Ops<T>::gemm(rows, n, n, Kc, n, Ops<T>::B(a), a->ldb, C, a->ldb, KB_UPPER, n, st);
+    if (rc) return rc;
+after_gemm:
+    if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[2], st));
+    rc = launch_row_dots<T>(*qa, C, a->ldb, Ops<T>::beta(a), Ops<T>::Vb(a), P, st);
+    if (rc) return rc;
+    rc = launch_sigma_reduce<T>(*qa, P, C, a->ldb, st);
+    if (rc) return rc;
+    if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[3], st));
+    return BGB_OK;
+}
+
+// Stage boundaries of the per-stage timing variant: kernel build, forward
+// cross-covariance GEMMs, covariance reduction, per-batch step, row mix,
+// adjoint GEMM, adjoint contraction.
+constexpr int kStages = 7;
+
+template <typename T>
+int run_call(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs& qa, T* Kc, T* C, T* P,
+             int backward, cudaStream_t st, cudaEvent_t* ev) {
+    const int64_t n = a->gp.n, rows = b * a->q;
+    int rc = run_front<T>(a, X, b, &qa, Kc, C, P, st, ev);
+    if (rc) return rc;
+    rc = launch_batch_step(qa, backward, st);
+    if (rc) return rc;
+    if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[4], st));
+    if (!backward) return BGB_OK;
+    // H = gmu beta^T - 2 Gqq V - Gqb Vb into the Kc buffer; D = H L^-1 into the V buffer
+    T* H = Kc;
+    bool tc = false;
+    if constexpr (sizeof(T) == 4) tc = use_tc(a);
+    if (tc) {
+        T* Hlo = Kc + rows * a->ldl;
+        rc = launch_mix_rows<T>(qa, C, a->ldb, Ops<T>::Vb(a), Ops<T>::beta(a), H, st, Hlo, a->ldl);
+        if (rc) return rc;
+        if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[5], st));
+        if constexpr (sizeof(T) == 4) {
+            rc = tc_gemm_tf32x3(rows, n, n, H, Hlo, a->ldl, a->LThi, a->LTlo, a->ldl, C, a->ldb,
+                                KB_LOWER, const_cast<int*>(qa.dev_err), st);
+            if (rc) return rc;
+        }
+    } else {
+        rc = launch_mix_rows<T>(qa, C, a->ldb, Ops<T>::Vb(a), Ops<T>::beta(a), H, st);
+        if (rc) return rc;
+        if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[5], st));
+        rc = Ops<T>::gemm(rows, n, n, H, n, Ops<T>::Linv(a), n, C, a->ldb, KB_LOWER, 0, st);
+        if (rc) return rc;
+    }
+    if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[6], st));
+    rc = launch_adjoint<T>(qa, C, a->ldb, st);
+    if (rc) return rc;
+    if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[7], st));
+    return BGB_OK;
+}
+
+int acq_call(const bgb_acq_t* a, const double* X, int64_t b, double* value, double* grad,
+             int32_t* status, void* ws, size_t ws_bytes, cudaStream_t st,
+             cudaEvent_t* ev = nullptr) {
+    if (!valid_acq(a) || X == nullptr || value == nullptr || status == nullptr || b < 0)
+        return BGB_ERR_ARG;
+    if (a->n_samples <= 0 || a->Z == nullptr || a->best_f == nullptr) return BGB_ERR_ARG;
+    if (b == 0) return BGB_OK;
+    Arena ar{static_cast<char*>(ws), ws_bytes, 0};
+    QBatchArgs qa;
+    memset(&qa, 0, sizeof(qa));
+    void *Kc = nullptr, *C = nullptr, *P = nullptr;
+    int* err = nullptr;
+    if (ws == nullptr || acq_ws_layout(a, b, &ar, &qa, &Kc, &C, &P, &err) == 0)
+        return BGB_ERR_WORKSPACE;
+    fill_qargs(a, X, b, &qa);
+    BGB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+    qa.dev_err = err;
+    qa.value = value;
+    qa.grad = grad;
+    qa.status = status;
+    if (a->precision == BGB_PREC_MIXED)
+        return run_call<float>(a, X, b, qa, static_cast<float*>(Kc), static_cast<float*>(C),
+                               static_cast<float*>(P), grad != nullptr, st, ev);
+    return run_call<double>(a, X, b, qa, static_cast<double*>(Kc), static_cast<double*>(C),
+                            static_cast<double*>(P), grad != nullptr, st, ev);
+}
+
+}  // namespace
+
+extern "C" {
+
+int bgb_version(void) { return 200; }
+
+int bgb_kernel_matrix(const bgb_gp_t* gp, const double* X1, int64_t m, const double* X2,
+                      int64_t n2, double diag_add, double* K, int64_t ldk, void* stream) {
+    if (!valid_gp(gp) || X1 == nullptr || X2 == nullptr || K == nullptr || m < 0 || n2 < 0 ||
+        ldk < n2)
+        return BGB_ERR_ARG;
+    return launch_kernel_matrix<double, double, double>(X1, m, X2, n2, gp->d, gp->inv_lengthscale,
+                                                        gp->outputscale, gp->kernel, diag_add,
+                                                        X1 == X2, K, ldk, as_stream(stream));
+}
+
+size_t bgb_cholesky_workspace_bytes(int64_t n) {
+    (void)n;
+    return align_up(64 * 64 * sizeof(double)) + align_up(2 * sizeof(int));
+}
+
+int bgb_cholesky(double* A, int64_t n, int64_t lda, int32_t* info_host, void* workspace,
+                 size_t workspace_bytes, void* stream) {
+    if (A == nullptr || n <= 0 || lda < n || info_host == nullptr) return BGB_ERR_ARG;
+    if (workspace == nullptr || workspace_bytes < bgb_cholesky_workspace_bytes(n))
+        return BGB_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    Arena ar{static_cast<char*>(workspace), workspace_bytes, 0};
+    double* dws = ar.take<double>(64 * 64);
+    int* dinfo = ar.take<int>(2);
+    int rc = cholesky_f64(A, n, lda, dinfo, dws, st);
+    if (rc) return rc;
+    int hinfo[2] = {0, 0};
+    BGB_CUDA_TRY(cudaMemcpyAsync(hinfo, dinfo, sizeof(hinfo), cudaMemcpyDeviceToHost, st));
+    BGB_CUDA_TRY(cudaStreamSynchronize(st));
+    *info_host = hinfo[0];
+    return hinfo[0] == 0 ? BGB_OK : BGB_NOT_PSD;
+}
+
+int bgb_psd_safe_cholesky(const double* A, int64_t n, int64_t lda, double* L, int64_t ldl,
+                          int32_t max_tries, double jitter, double* jitter_host, void* workspace,
+                          size_t workspace_bytes, void* stream) {
+    if (A == nullptr || L == nullptr || n <= 0 || lda < n || ldl < n || max_tries < 0)
+        return BGB_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    if (jitter <= 0.0) jitter = 1e-8;
+    double total = 0.0;
+    int32_t info = 0;
+    for (int t = -1; t < max_tries; ++t) {
+        if (t >= 0) total = jitter * pow(10.0, (double)t);
+        int rc = copy_matrix_f64(A, lda, L, ldl, n, n, total, st);
+        if (rc) return rc;
+        rc = bgb_cholesky(L, n, ldl, &info, workspace, workspace_bytes, stream);
+        if (rc == BGB_OK) {
+            if (jitter_host) *jitter_host = total;
+            return BGB_OK;
+        }
+        if (rc != BGB_NOT_PSD) return rc;
+    }
+    if (jitter_host) *jitter_host = total;
+    return BGB_NOT_PSD;
+}
+
+size_t bgb_tri_inverse_workspace_bytes(int64_t n) {
+    const int64_t nb = ceil_div(n, 64);
+    return align_up(sizeof(double) * (nb * 64 * 64 + 64 * n));
+}
+
+int bgb_tri_inverse(double* L, int64_t n, int64_t lda, void* workspace, size_t workspace_bytes,
+                    void* stream) {
+    if (L == nullptr || n <= 0 || lda < n) return BGB_ERR_ARG;
+    if (workspace == nullptr || workspace_bytes < bgb_tri_inverse_workspace_bytes(n))
+        return BGB_ERR_WORKSPACE;
+    return tri_inverse_f64(L, n, lda, static_cast<double*>(workspace), as_stream(stream));
+}
+
+size_t bgb_gp_fit_workspace_bytes(int64_t n) {
+    return align_up(sizeof(double) * n * n) + bgb_cholesky_workspace_bytes(n) +
+           bgb_tri_inverse_workspace_bytes(n) + 3 * align_up(sizeof(double) * n);
+}
+
+int bgb_gp_fit(const bgb_gp_t* gp, const double* y, double noise, int32_t max_tries, double* L,
+               double* Linv, double* alpha, double* beta, double* jitter_host, void* workspace,
+               size_t workspace_bytes, void* stream) {
+    if (!valid_gp(gp) || y == nullptr || L == nullptr || Linv == nullptr || alpha == nullptr ||
+        beta == nullptr)
+        return BGB_ERR_ARG;
+    const int64_t n = gp->n;
+    if (workspace == nullptr || workspace_bytes < bgb_gp_fit_workspace_bytes(n))
+        return BGB_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    Arena ar{static_cast<char*>(workspace), workspace_bytes, 0};
+    double* K = ar.take<double>(n * n);
+    void* chol_ws = ar.take<char>(bgb_cholesky_workspace_bytes(n));
+    double* tri_ws = ar.take<double>(bgb_tri_inverse_workspace_bytes(n) / sizeof(double));
+    double* yc = ar.take<double>(n);
+    double* res = ar.take<double>(n);
+    double* t = ar.take<double>(n);
+    // K = k(Xt, Xt) + noise I
+    int rc = launch_kernel_matrix<double, double, double>(gp->train_X, n, gp->train_X, n, gp->d,
+                                                          gp->inv_lengthscale, gp->outputscale,
+                                                          gp->kernel, noise, 1, K, n, st);
+    if (rc) return rc;
+    double jit = 0.0;
+    rc = bgb_psd_safe_cholesky(K, n, n, L, n, max_tries, 1e-8, &jit, chol_ws,
+                               bgb_cholesky_workspace_bytes(n), stream);
+    if (rc) return rc;
+    if (jitter_host) *jitter_host = jit;
+    // Linv = L^-1
+    rc = copy_matrix_f64(L, n, Linv, n, n, n, 0.0, st);
+    if (rc) return rc;
+    rc = tri_inverse_f64(Linv, n, n, tri_ws, st);
+    if (rc) return rc;
+    // alpha = Linv^T (Linv (y - m)), then one refinement step against K_eff = K + jitter I
+    sub_const_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(y, gp->mean_constant, yc, n);
+    BGB_CHECK_LAUNCH();
+    rc = gemv_f64(n, n, 1.0, Linv, n, yc, 0.0, t, st);
+    if (rc) return rc;
+    rc = gemm_f64(n, 1, n, 1.0, Linv, n, 1, t, 1, 0, 0.0, alpha, 1, KFULL, 0, nullptr, st);
+    if (rc) return rc;
+    if (jit > 0.0) {
+        rc = launch_kernel_matrix<double, double, double>(gp->train_X, n, gp->train_X, n, gp->d,
+                                                          gp->inv_lengthscale, gp->outputscale,
+                                                          gp->kernel, noise + jit, 1, K, n, st);
+        if (rc) return rc;
+    }
+    // res = yc - K alpha;  alpha += Linv^T (Linv res)
+    BGB_CUDA_TRY(cudaMemcpyAsync(res, yc, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    rc = gemv_f64(n, n, -1.0, K, n, alpha, 1.0, res, st);
+    if (rc) return rc;
+    rc = gemv_f64(n, n, 1.0, Linv, n, res, 0.0, t, st);
+    if (rc) return rc;
+    rc = gemm_f64(n, 1, n, 1.0, Linv, n, 1, t, 1, 0, 1.0, alpha, 1, KFULL, 0, nullptr, st);
+    if (rc) return rc;
+    // beta = L^T alpha (= L^-1 (y - m) for the refined alpha)
+    rc = gemm_f64(n, 1, n, 1.0, L, n, 1, alpha, 1, 0, 0.0, beta, 1, KFULL, 0, nullptr, st);
+    if (rc) return rc;
+    BGB_CUDA_TRY(cudaStreamSynchronize(st));
+    return BGB_OK;
+}
+
+int bgb_gp_operands(const bgb_gp_t* gp, const double* Linv, const double* beta, double* B64,
+                    float* B32, int64_t ldb, float* Linv32, float* beta32, void* stream) {
+    if (!valid_gp(gp) || Linv == nullptr || beta == nullptr || B64 == nullptr) return BGB_ERR_ARG;
+    const int64_t n = gp->n;
+    if (ldb < n) return BGB_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    fill_b_kernel<<<(unsigned)ceil_div(n * ldb, 256), 256, 0, st>>>(Linv, n, B64, ldb);
+    BGB_CHECK_LAUNCH();
+    int rc;
+    if (B32 != nullptr && (rc = convert_f64_f32(B64, B32, n * ldb, st)) != BGB_OK) return rc;
+    if (Linv32 != nullptr && (rc = convert_f64_f32(Linv, Linv32, n * n, st)) != BGB_OK) return rc;
+    if (beta32 != nullptr && (rc = convert_f64_f32(beta, beta32, n, st)) != BGB_OK) return rc;
+    return BGB_OK;
+}
+
+int bgb_gp_tc_operands(const bgb_gp_t* gp, const double* Linv, int64_t ldl, float* Lhi,
+                       float* Llo, float* LThi, float* LTlo, void* stream) {
+    if (!valid_gp(gp) || Linv == nullptr || Lhi == nullptr || Llo == nullptr || LThi == nullptr ||
+        LTlo == nullptr)
+        return BGB_ERR_ARG;
+    const int64_t n = gp->n;
+    if (ldl < n || (ldl % 8) != 0) return BGB_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    int rc = split_f64_tf32(Linv, n, n, n, 0, Lhi, Llo, ldl, st);
+    if (rc) return rc;
+    return split_f64_tf32(Linv, n, n, n, 1, LThi, LTlo, ldl, st);
+}
+
+int bgb_crosscov_gemm_tf32x3(int64_t M, int64_t N, int64_t K, const float* A_hi,
+                             const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
+                             int64_t ldbs, float* C, int64_t ldc, int32_t kmode, int32_t* err_dev,
+                             void* stream) {
+    if (M < 0 || N < 0 || K <= 0 || A_hi == nullptr || A_lo == nullptr || B_hi == nullptr ||
+        B_lo == nullptr || C == nullptr || (lda % 4) || (ldbs % 4) || (ldc % 4) || lda < K ||
+        ldbs < K || ldc < N)
+        return BGB_ERR_ARG;
+    if (kmode != KB_UPPER && kmode != KB_LOWER && kmode != KFULL) return BGB_ERR_ARG;
+    if (!tc_gemm_available()) return BGB_ERR_UNSUPPORTED;
+    return tc_gemm_tf32x3(M, N, K, A_hi, A_lo, lda, B_hi, B_lo, ldbs, C, ldc, kmode, err_dev,
+                          as_stream(stream));
+}
+
+size_t bgb_baseline_operands_workspace_bytes(int64_t n, int32_t r) {
+    return align_up(sizeof(double) * n * (r > 0 ? r : 1));
+}
+
+int bgb_baseline_operands(const bgb_gp_t* gp, const double* Linv, const double* X_baseline,
+                          int32_t r, double* Vb64, float* Vb32, double* VbT64, float* VbT32,
+                          void* workspace, size_t workspace_bytes, void* stream) {
+    if (!valid_gp(gp) || Linv == nullptr || X_baseline == nullptr || r <= 0 || Vb64 == nullptr ||
+        VbT64 == nullptr)
+        return BGB_ERR_ARG;
+    const int64_t n = gp->n;
+    if (workspace == nullptr || workspace_bytes < bgb_baseline_operands_workspace_bytes(n, r))
+        return BGB_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    double* Kbt = static_cast<double*>(workspace);
+    int rc = launch_kernel_matrix<double, double, double>(X_baseline, r, gp->train_X, n, gp->d,
+                                                          gp->inv_lengthscale, gp->outputscale,
+                                                          gp->kernel, 0.0, 0, Kbt, n, st);
+    if (rc) return rc;
+    rc = gemm_f64(r, n, n, 1.0, Kbt, n, 0, Linv, n, 1, 0.0, Vb64, n, KB_UPPER, 0, nullptr, st, n);
+    if (rc) return rc;
+    rc = transpose_f64(Vb64, r, n, n, VbT64, r, st);
+    if (rc) return rc;
+    if (Vb32 != nullptr && (rc = convert_f64_f32(Vb64, Vb32, (int64_t)r * n, st)) != BGB_OK)
+        return rc;
+    if (VbT32 != nullptr && (rc = convert_f64_f32(VbT64, VbT32, (int64_t)r * n, st)) != BGB_OK)
+        return rc;
+    return BGB_OK;
+}
+
+size_t bgb_acq_workspace_bytes(const bgb_acq_t* acq, int64_t b) {
+    if (acq == nullptr || b <= 0) return 0;
+    return acq_ws_layout(acq, b, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+int bgb_posterior(const bgb_acq_t* acq, const double* X, int64_t b, double* mean, double* covar,
+                  void* workspace, size_t workspace_bytes, void* stream) {
+    if (!valid_acq(acq) || X == nullptr || mean == nullptr || covar == nullptr || b < 0 ||
+        acq->r != 0)
+        return BGB_ERR_ARG;
+    if (b == 0) return BGB_OK;
+    cudaStream_t st = as_stream(stream);
+    Arena ar{static_cast<char*>(workspace), workspace_bytes, 0};
+    QBatchArgs qa;
+    memset(&qa, 0, sizeof(qa));
+    void *Kc = nullptr, *C = nullptr, *P = nullptr;
+    int* err = nullptr;
+    if (workspace == nullptr || acq_ws_layout(acq, b, &ar, &qa, &Kc, &C, &P, &err) == 0)
+        return BGB_ERR_WORKSPACE;
+    fill_qargs(acq, X, b, &qa);
+    BGB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+    qa.dev_err = err;
+    int rc;
+    if (acq->precision == BGB_PREC_MIXED)
+        rc = run_front<float>(acq, X, b, &qa, static_cast<float*>(Kc), static_cast<float*>(C),
+                              static_cast<float*>(P), st, nullptr);
+    else
+        rc = run_front<double>(acq, X, b, &qa, static_cast<double*>(Kc), static_cast<double*>(C),
+                               static_cast<double*>(P), st, nullptr);
+    if (rc) return rc;
+    return launch_posterior_out(qa, mean, covar, st);
+}
+
+int bgb_acq_forward(const bgb_acq_t* acq, const double* X, int64_t b, double* value,
+                    int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
+    return acq_call(acq, X, b, value, nullptr, status, workspace, workspace_bytes,
+                    as_stream(stream));
+}
+
+int bgb_acq_forward_backward(const bgb_acq_t* acq, const double* X, int64_t b, double* value,
+                             double* grad, int32_t* status, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+    if (grad == nullptr) return BGB_ERR_ARG;
+    return acq_call(acq, X, b, value, grad, status, workspace, workspace_bytes,
+                    as_stream(stream));
+}
+
+unsigned long long bgb_launch_count(void) { return g_launches.load(); }
+
+int bgb_acq_forward_backward_timed(const bgb_acq_t* acq, const double* X, int64_t b,
+                                   double* value, double* grad, int32_t* status, void* workspace,
+                                   size_t workspace_bytes, float* stage_ms_host, void* stream) {
+    if (grad == nullptr || stage_ms_host == nullptr) return BGB_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    cudaEvent_t ev[kStages + 1];
+    for (int i = 0; i <= kStages; ++i) BGB_CUDA_TRY(cudaEventCreate(&ev[i]));
+    int rc = acq_call(acq, X, b, value, grad, status, workspace, workspace_bytes, st, ev);
+    if (rc == BGB_OK) {
+        if (cudaEventSynchronize(ev[kStages]) != cudaSuccess) rc = BGB_ERR_CUDA;
+        for (int i = 0; rc == BGB_OK && i < kStages; ++i)
+            if (cudaEventElapsedTime(&stage_ms_host[i], ev[i], ev[i + 1]) != cudaSuccess)
+                rc = BGB_ERR_CUDA;
+    }
+    for (int i = 0; i <= kStages; ++i) cudaEventDestroy(ev[i]);
+    return rc;
+}
+
+}  // extern "C"

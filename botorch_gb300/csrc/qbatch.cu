@@ -1,0 +1,799 @@
+// (d) + (e) + adjoint: the per-t-batch part of the path.
+//
+// The cross-covariance enters through V = K(X, Xt) L^-T (the triangular solve
+// against the training Cholesky factor, computed by the GEMM before these
+// kernels), as in the reference's root-inverse form of the predictive
+// covariance:
+//  row_dots       mu = m + V beta (beta = L^-1 (y - m)) and P = V Vb^T, one warp per row.
+//  sigma_reduce   Sigma_qq = K(X,X) - V V^T, Sigma_qb = K(X,Xb) - P. Reads the q rows of
+//                 V of each t-batch once.
+//  batch_step     one CTA per t-batch, float64: untransform, bl = Sigma_qb Lb^-T,
+//                 br = psd_safe_cholesky(Sigma_qq - bl bl^T) with per-batch jitter
+//                 retries, Y = mu + [bl, br] z over the S base samples, the qLogNEI
+//                 reduction (log_fatplus, fatmax over q, logmeanexp over S) or the
+//                 qEI reduction, and in reverse the seeds of the adjoint
+//                 (d value / d Sigma_qq, d Sigma_qb, d mu) through the sample
+//                 reduction, the sample step and the q x q Cholesky.
+//  mix_rows       H = gmu beta^T - 2 Gqq V - Gqb Vb  (d value / d V), per t-batch.
+//  adjoint        d value / d X with dKc = H L^-1 (the second triangular GEMM, D),
+//                 contracted with d K(X, Xt) / d X while recomputing
+//                 the scaled distances to Xt instead of storing K(X, Xt); plus the
+//                 K(X, X) and K(X, Xb) terms.
+#include <math.h>
+
+#include "bgb_common.cuh"
+#include "bgb_kernels.cuh"
+#include "bgb_qbatch.cuh"
+
+namespace bgb {
+
+namespace {
+
+// ---------------------------------------------------------------- sigma_reduce
+template <typename T, int QMAX>
+__global__ void __launch_bounds__(256) sigma_reduce_kernel(QBatchArgs a, const T* __restrict__ P,
+                                                           const T* __restrict__ C, int64_t ldc) {
+    constexpr int NP = QMAX * (QMAX + 1) / 2;
+    const int q = a.q;
+    const int64_t n = a.n;
+    const int64_t bidx = blockIdx.x;
+    const int64_t rbase = bidx * q;
+    // Each thread sums n / blockDim terms per pair in T (float64 for the plain
+    // path, float32 for the mixed one); the cross-thread reduction is float64.
+    T acc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[p] = T(0);
+    for (int64_t c = threadIdx.x; c < n; c += blockDim.x) {
+        T w[QMAX], k[QMAX];
+#pragma unroll
+        for (int i = 0; i < QMAX; ++i) {
+            w[i] = (i < q) ? C[(rbase + i) * ldc + c] : T(0);
+            k[i] = w[i];
+        }
+        int p = 0;
+#pragma unroll
+        for (int i = 0; i < QMAX; ++i)
+#pragma unroll
+            for (int j = 0; j <= i; ++j) {
+                acc[p] = fma(w[i], k[j], acc[p]);
+                ++p;
+            }
+    }
+    __shared__ double red[8][NP];
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        double v = (double)acc[p];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][p] = v;
+    }
+    __syncthreads();
+    const int nw = blockDim.x / 32;
+    const int d = a.d;
+    for (int p = threadIdx.x; p < NP; p += blockDim.x) {
+        // p -> (i, j), j <= i
+        int i = 0;
+        while ((i + 1) * (i + 2) / 2 <= p) ++i;
+        int j = p - i * (i + 1) / 2;
+        if (i >= q) continue;
+        double s = 0.0;
+        for (int w = 0; w < nw; ++w) s += red[w][p];
+        // K(x_i, x_j)
+        const double* xi = a.X + (rbase + i) * d;
+        const double* xj = a.X + (rbase + j) * d;
+        double r2 = 0.0;
+        for (int k = 0; k < d; ++k) {
+            double df = (xi[k] - xj[k]) * a.inv_ls[k];
+            r2 = fma(df, df, r2);
+        }
+        double kij = a.outputscale * kappa<double>(a.kernel, r2);
+        double v = kij - s;
+        a.sig[(bidx * q + i) * q + j] = v;
+        a.sig[(bidx * q + j) * q + i] = v;
+    }
+    const int r = a.r;
+    for (int p = threadIdx.x; p < q * (r + 1); p += blockDim.x) {
+        int i = p / (r + 1), kb = p % (r + 1);
+        if (kb < r) {
+            const double cval = (double)P[(rbase + i) * r + kb];
+            const double* xi = a.X + (rbase + i) * d;
+            const double* xb = a.Xb + (int64_t)kb * d;
+            double r2 = 0.0;
+            for (int k = 0; k < d; ++k) {
+                double df = (xi[k] - xb[k]) * a.inv_ls[k];
+                r2 = fma(df, df, r2);
+            }
+            a.sqb[(bidx * q + i) * r + kb] = a.outputscale * kappa<double>(a.kernel, r2) - cval;
+        }
+    }
+}
+
+// Fallback for q > 8: one warp per (t-batch, pair).
+template <typename T>
+__global__ void sigma_reduce_pairs_kernel(QBatchArgs a, const T* __restrict__ P,
+                                          const T* __restrict__ C, int64_t ldc) {
+    const int q = a.q;
+    const int64_t n = a.n;
+    const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    const int64_t npairs = (int64_t)q * q;
+    if (warp_id >= a.b * npairs) return;
+    const int64_t bidx = warp_id / npairs;
+    const int i = (int)((warp_id % npairs) / q), j = (int)(warp_id % q);
+    if (j > i) return;
+    const int64_t rbase = bidx * q;
+    double s = 0.0;
+    for (int64_t c = lane; c < n; c += 32)
+        s += (double)(C[(rbase + i) * ldc + c] * C[(rbase + j) * ldc + c]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane != 0) return;
+    const int d = a.d;
+    const double* xi = a.X + (rbase + i) * d;
+    const double* xj = a.X + (rbase + j) * d;
+    double r2 = 0.0;
+    for (int k = 0; k < d; ++k) {
+        double df = (xi[k] - xj[k]) * a.inv_ls[k];
+        r2 = fma(df, df, r2);
+    }
+    double v = a.outputscale * kappa<double>(a.kernel, r2) - s;
+    a.sig[(bidx * q + i) * q + j] = v;
+    a.sig[(bidx * q + j) * q + i] = v;
+    if (j == 0) {
+        const int r = a.r;
+        for (int kb = 0; kb < r; ++kb) {
+            const double cval = (double)P[(rbase + i) * r + kb];
+            {
+                const double* xb = a.Xb + (int64_t)kb * d;
+                double rb2 = 0.0;
+                for (int k = 0; k < d; ++k) {
+                    double df = (xi[k] - xb[k]) * a.inv_ls[k];
+                    rb2 = fma(df, df, rb2);
+                }
+                a.sqb[(bidx * q + i) * r + kb] = a.outputscale * kappa<double>(a.kernel, rb2) - cval;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- row_dots
+// mu[i] = m + V[i,:] . beta and P[i,k] = V[i,:] . Vb[k,:] (k < r), one warp per
+// row of V. float32 inputs use compensated per-lane sums; the cross-lane sum is
+// float64. (mu = K(X,Xt) alpha = V beta with beta = L^-1 (y - m): the bounded
+// factor avoids the cancellation of K(X,Xt) alpha.)
+template <typename T>
+__device__ __forceinline__ void comp_add(T& s, T& c, T x) {
+    T y = x - c;
+    T t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) row_dots_kernel(QBatchArgs a, const T* __restrict__ V,
+                                                       int64_t ldv, const T* __restrict__ beta,
+                                                       const T* __restrict__ Vb, T* __restrict__ P) {
+    const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+    const int64_t rows = a.b * a.q, n = a.n;
+    if (row >= rows) return;
+    const int r = a.r;
+    const T* v = V + row * ldv;
+    for (int k0 = -1; k0 < r; k0 += 8) {
+        // k = -1 is the beta dot product, k >= 0 the baseline rows
+        T s[8], c[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) { s[u] = T(0); c[u] = T(0); }
+        for (int64_t j = lane; j < n; j += 32) {
+            const T vj = v[j];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int k = k0 + u;
+                if (k < r) {
+                    const T w = (k < 0) ? beta[j] : Vb[(int64_t)k * n + j];
+                    comp_add<T>(s[u], c[u], vj * w);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            double tot = (double)s[u] - (double)c[u];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            const int k = k0 + u;
+            if (lane == 0 && k < r) {
+                if (k < 0) a.mu[row] = a.mean_constant + tot;
+                else P[row * r + k] = (T)tot;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- smooth pieces
+// softplus with torch's threshold 20 (beta = 1)
+__device__ __forceinline__ double softplus_t(double x) { return x > 20.0 ? x : log1p(exp(x)); }
+__device__ __forceinline__ double softplus_grad(double x) {
+    if (x > 20.0) return 1.0;
+    double z = exp(x);
+    return z / (z + 1.0);
+}
+// log_fatplus(u, tau) = log(tau * (softplus(u/tau) + 0.1 / (1 + (u/tau)^2)))
+__device__ __forceinline__ double log_fatplus(double u, double tau) {
+    double v = u / tau;
+    return log(tau * (softplus_t(v) + 0.1 / (1.0 + v * v)));
+}
+__device__ __forceinline__ double dlog_fatplus(double u, double tau) {
+    double v = u / tau;
+    double c = 1.0 / (1.0 + v * v);
+    double h = softplus_t(v) + 0.1 * c;
+    double hp = softplus_grad(v) - 0.2 * v * c * c;
+    return hp / (tau * h);
+}
+// pareto kernel of fatmax (alpha = 2): p(x) = 2 / (2 + 2x + x^2), p'(x) = -4 (1 + x) / (..)^2
+__device__ __forceinline__ double pareto2(double x) { return 2.0 / (2.0 + 2.0 * x + x * x); }
+__device__ __forceinline__ double dpareto2(double x) {
+    double den = 2.0 + 2.0 * x + x * x;
+    return -4.0 * (1.0 + x) / (den * den);
+}
+
+// In-place Cholesky of a q x q row-major matrix (lower). Returns 0 or pivot+1.
+__device__ int chol_small(double* A, int q) {
+    for (int j = 0; j < q; ++j) {
+        double v = A[j * q + j];
+        for (int k = 0; k < j; ++k) v -= A[j * q + k] * A[j * q + k];
+        if (!(v > 0.0)) return j + 1;
+        double djj = sqrt(v);
+        A[j * q + j] = djj;
+        for (int i = j + 1; i < q; ++i) {
+            double s = A[i * q + j];
+            for (int k = 0; k < j; ++k) s -= A[i * q + k] * A[j * q + k];
+            A[i * q + j] = s / djj;
+        }
+        for (int k = j + 1; k < q; ++k) A[j * q + k] = 0.0;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------- batch_step
+// Shared memory (doubles): Lq q*(r+q) | dLq q*(r+q) | M q*q | gA q*q | mu q | dmu q |
+//                          t S | dY SC*q | scratch q*q
+constexpr int kSampleChunk = 128;
+
+__global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backward) {
+    extern __shared__ double sm[];
+    const int q = a.q, r = a.r, S = a.S, D = r + q;
+    const int64_t bidx = blockIdx.x;
+    double* Lq = sm;
+    double* dLq = Lq + q * D;
+    double* M = dLq + q * D;
+    double* gA = M + q * q;
+    double* mu = gA + q * q;
+    double* dmu = mu + q;
+    double* tS = dmu + q;
+    double* dY = tS + S;
+    double* scr = dY + kSampleChunk * q;
+    __shared__ int s_status;
+    __shared__ double s_red[4];
+    __shared__ double s_lse;
+    const int tid = threadIdx.x;
+    const double sy = a.y_std, sy2 = a.y_std * a.y_std;
+    if (tid == 0) s_status = (a.dev_err != nullptr && *a.dev_err != 0) ? BGB_DEVICE_TIMEOUT : 0;
+    __syncthreads();
+    if (s_status != 0) {
+        if (tid == 0) {
+            a.status[bidx] = s_status;
+            a.value[bidx] = NAN;
+        }
+        return;
+    }
+    // (1) untransformed mean and covariance blocks
+    for (int i = tid; i < q; i += blockDim.x) mu[i] = a.y_mean + sy * a.mu[bidx * q + i];
+    for (int p = tid; p < q * q; p += blockDim.x) M[p] = sy2 * a.sig[bidx * q * q + p];
+    __syncthreads();
+    // (2) bl = Sigma_qb Lb^-T  (Lq[:, :r]);  Lb_inv lower triangular
+    for (int p = tid; p < q * r; p += blockDim.x) {
+        int i = p / r, k = p % r;
+        double s = 0.0;
+        for (int kk = 0; kk <= k; ++kk) s += sy2 * a.sqb[(bidx * q + i) * r + kk] * a.Lb_inv[k * r + kk];
+        Lq[i * D + k] = s;
+    }
+    __syncthreads();
+    // (3) M = Sigma_qq - bl bl^T
+    for (int p = tid; p < q * q; p += blockDim.x) {
+        int i = p / q, j = p % q;
+        double s = 0.0;
+        for (int k = 0; k < r; ++k) s += Lq[i * D + k] * Lq[j * D + k];
+        M[p] -= s;
+    }
+    __syncthreads();
+    // (4) psd_safe_cholesky(M): plain, then jitter j * 10^i (i < max_tries) for this batch only
+    if (tid == 0) {
+        int status = 0;
+        bool has_nan = false;
+        for (int p = 0; p < q * q; ++p) has_nan |= isnan(M[p]);
+        for (int p = 0; p < q * q; ++p) scr[p] = M[p];
+        int info = has_nan ? 1 : chol_small(scr, q);
+        if (info != 0) {
+            if (has_nan) {
+                status = BGB_NAN;
+            } else {
+                double jprev = 0.0;
+                status = BGB_NOT_PSD;
+                for (int t = 0; t < a.max_tries; ++t) {
+                    double jnew = a.jitter * pow(10.0, (double)t);
+                    for (int i = 0; i < q; ++i) M[i * q + i] += jnew - jprev;
+                    jprev = jnew;
+                    for (int p = 0; p < q * q; ++p) scr[p] = M[p];
+                    if (chol_small(scr, q) == 0) { status = 0; break; }
+                }
+            }
+        }
+        for (int i = 0; i < q; ++i)
+            for (int j = 0; j < q; ++j) Lq[i * D + r + j] = (j <= i) ? scr[i * q + j] : 0.0;
+        s_status = status;
+    }
+    __syncthreads();
+    if (s_status != 0) {
+        if (tid == 0) {
+            a.status[bidx] = s_status;
+            a.value[bidx] = NAN;
+        }
+        if (backward) {
+            for (int p = tid; p < q * q; p += blockDim.x) a.gqq[bidx * q * q + p] = 0.0;
+            for (int p = tid; p < q * r; p += blockDim.x) a.gqb[bidx * q * r + p] = 0.0;
+            for (int p = tid; p < q; p += blockDim.x) a.gmu[bidx * q + p] = 0.0;
+        }
+        return;
+    }
+    const bool qei = (a.acqf == BGB_ACQF_QEI);
+    const double tau = a.tau_relu, taum = a.tau_max;
+    // (5) forward over samples: t_s (per-sample reduced utility)
+    int local_bad = 0;
+    for (int s = tid; s < S; s += blockDim.x) {
+        const double* z = a.Z + (int64_t)s * D;
+        const double bf = qei ? a.best_f[0] : a.best_f[s];
+        double li[kMaxQ];
+        double Mx = -INFINITY;
+        for (int i = 0; i < q; ++i) {
+            double y = mu[i];
+            for (int k = 0; k < r + i + 1; ++k) y += Lq[i * D + k] * z[k];
+            if (!isfinite(y)) local_bad = 1;
+            if (qei) {
+                li[i] = fmax(y - bf, 0.0);
+            } else {
+                li[i] = log_fatplus(y - bf, tau);
+            }
+            Mx = fmax(Mx, li[i]);
+        }
+        double t;
+        if (qei) {
+            t = Mx;
+        } else if (isinf(Mx)) {
+            t = Mx;
+        } else {
+            double P = 0.0;
+            for (int i = 0; i < q; ++i) P += pareto2((Mx - li[i]) / taum);
+            t = Mx + taum * log(P);
+        }
+        tS[s] = t;
+    }
+    if (__syncthreads_or(local_bad)) {
+        if (tid == 0) {
+            a.status[bidx] = BGB_NAN;
+            a.value[bidx] = NAN;
+        }
+        if (backward) {
+            for (int p = tid; p < q * q; p += blockDim.x) a.gqq[bidx * q * q + p] = 0.0;
+            for (int p = tid; p < q * r; p += blockDim.x) a.gqb[bidx * q * r + p] = 0.0;
+            for (int p = tid; p < q; p += blockDim.x) a.gmu[bidx * q + p] = 0.0;
+        }
+        return;
+    }
+    // (6) sample reduction (float64): qEI mean, qLogNEI logmeanexp with inf handling
+    const int lane = tid % 32, warp = tid / 32;
+    double mx = -INFINITY;
+    for (int s = tid; s < S; s += blockDim.x) mx = fmax(mx, tS[s]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s_red[warp] = mx;
+    __syncthreads();
+    mx = fmax(fmax(s_red[0], s_red[1]), fmax(s_red[2], s_red[3]));
+    __syncthreads();
+    double acc = 0.0;
+    for (int s = tid; s < S; s += blockDim.x) {
+        if (qei) acc += tS[s];
+        else if (!isinf(mx)) acc += exp(tS[s] - mx);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_red[warp] = acc;
+    __syncthreads();
+    if (tid == 0) {
+        double tot = (s_red[0] + s_red[1]) + (s_red[2] + s_red[3]);
+        double v, lse;
+        if (qei) {
+            v = tot / S;
+            lse = 0.0;
+        } else if (isinf(mx)) {
+            v = mx;  // sum of the infinite maxima (same sign) minus log S
+            lse = mx;
+        } else {
+            lse = mx + log(tot);
+            v = lse - log((double)S);
+        }
+        a.value[bidx] = v;
+        a.status[bidx] = 0;
+        s_lse = lse;
+    }
+    if (!backward) return;
+    for (int p = tid; p < q * D; p += blockDim.x) dLq[p] = 0.0;
+    for (int p = tid; p < q; p += blockDim.x) dmu[p] = 0.0;
+    __syncthreads();
+    const double lse = s_lse;
+    // (7) reverse through the sample reduction and the sample step, SC samples at a time
+    for (int s0 = 0; s0 < S; s0 += kSampleChunk) {
+        const int sc = min(kSampleChunk, S - s0);
+        for (int ls = tid; ls < sc; ls += blockDim.x) {
+            const int s = s0 + ls;
+            const double* z = a.Z + (int64_t)s * D;
+            const double bf = qei ? a.best_f[0] : a.best_f[s];
+            double u[kMaxQ], li[kMaxQ], g[kMaxQ];
+            double Mx = -INFINITY;
+            for (int i = 0; i < q; ++i) {
+                double y = mu[i];
+                for (int k = 0; k < r + i + 1; ++k) y += Lq[i * D + k] * z[k];
+                u[i] = y - bf;
+                li[i] = qei ? fmax(u[i], 0.0) : log_fatplus(u[i], tau);
+                Mx = fmax(Mx, li[i]);
+            }
+            int nt = 0;
+            for (int i = 0; i < q; ++i) nt += (li[i] == Mx);
+            if (qei) {
+                const double w = 1.0 / S / nt;
+                for (int i = 0; i < q; ++i) g[i] = (li[i] == Mx && u[i] >= 0.0) ? w : 0.0;
+            } else {
+                const double ws = isinf(mx) ? (tS[s] == mx ? 1.0 : 0.0) : exp(tS[s] - lse);
+                if (isinf(Mx)) {
+                    for (int i = 0; i < q; ++i) g[i] = (li[i] == Mx) ? ws : 0.0;
+                } else {
+                    double P = 0.0, Pd = 0.0;
+                    for (int i = 0; i < q; ++i) {
+                        double x = (Mx - li[i]) / taum;
+                        P += pareto2(x);
+                        Pd += dpareto2(x);
+                    }
+                    const double top = (1.0 + Pd / P) / nt;
+                    for (int i = 0; i < q; ++i) {
+                        double x = (Mx - li[i]) / taum;
+                        double dt = -dpareto2(x) / P + (li[i] == Mx ? top : 0.0);
+                        g[i] = ws * dt * dlog_fatplus(u[i], tau);
+                    }
+                }
+            }
+            for (int i = 0; i < q; ++i) dY[ls * q + i] = g[i];
+        }
+        __syncthreads();
+        for (int p = tid; p < q * D; p += blockDim.x) {
+            const int i = p / D, k = p % D;
+            if (k >= r + i + 1) continue;  // upper part of br stays zero
+            double s = 0.0;
+            for (int ls = 0; ls < sc; ++ls) s += dY[ls * q + i] * a.Z[(int64_t)(s0 + ls) * D + k];
+            dLq[p] += s;
+        }
+        for (int i = tid; i < q; i += blockDim.x) {
+            double s = 0.0;
+            for (int ls = 0; ls < sc; ++ls) s += dY[ls * q + i];
+            dmu[i] += s;
+        }
+        __syncthreads();
+    }
+    // (8) reverse through br = chol(M): gA = L^-T Phi(L^T dL) L^-1 (symmetric)
+    if (tid == 0) {
+        // X = tril(L^T dL)   (L = br, dL = d br, both lower)
+        for (int i = 0; i < q; ++i)
+            for (int j = 0; j < q; ++j) {
+                double s = 0.0;
+                if (j <= i)
+                    for (int k = i; k < q; ++k) s += Lq[k * D + r + i] * dLq[k * D + r + j];
+                scr[i * q + j] = s;
+            }
+        // Phi = 0.5 * (X + tril(X, -1)^T)
+        for (int i = 0; i < q; ++i)
+            for (int j = 0; j < q; ++j) {
+                double v;
+                if (i == j) v = 0.5 * scr[i * q + i];
+                else if (j < i) v = 0.5 * scr[i * q + j];
+                else v = 0.5 * scr[j * q + i];
+                gA[i * q + j] = v;
+            }
+        // gA <- L^-T gA  (solve L^T Y = gA, upper triangular, column by column)
+        for (int c = 0; c < q; ++c)
+            for (int i = q - 1; i >= 0; --i) {
+                double s = gA[i * q + c];
+                for (int k = i + 1; k < q; ++k) s -= Lq[k * D + r + i] * gA[k * q + c];
+                gA[i * q + c] = s / Lq[i * D + r + i];
+            }
+        // gA <- gA L^-1  (solve Y L = gA, row by row)
+        for (int row = 0; row < q; ++row)
+            for (int j = q - 1; j >= 0; --j) {
+                double s = gA[row * q + j];
+                for (int k = j + 1; k < q; ++k) s -= gA[row * q + k] * Lq[k * D + r + j];
+                gA[row * q + j] = s / Lq[j * D + r + j];
+            }
+    }
+    __syncthreads();
+    // (9) d bl += -2 gA bl;  dSigma_qb = d bl * Lb^-1;  write seeds in standardised units
+    for (int p = tid; p < q * r; p += blockDim.x) {
+        const int i = p / r, k = p % r;
+        double s = dLq[i * D + k];
+        for (int j = 0; j < q; ++j) s -= 2.0 * gA[i * q + j] * Lq[j * D + k];
+        scr[p] = s;  // reuse: q*r <= scratch when r <= q; else spill to dLq block below
+    }
+    __syncthreads();
+    for (int p = tid; p < q * r; p += blockDim.x) dLq[(p / r) * D + (p % r)] = scr[p];
+    __syncthreads();
+    for (int p = tid; p < q * r; p += blockDim.x) {
+        const int i = p / r, kp = p % r;
+        double s = 0.0;
+        for (int k = kp; k < r; ++k) s += dLq[i * D + k] * a.Lb_inv[k * r + kp];
+        a.gqb[(bidx * q + i) * r + kp] = sy2 * s;
+    }
+    for (int p = tid; p < q * q; p += blockDim.x) a.gqq[bidx * q * q + p] = sy2 * gA[p];
+    for (int i = tid; i < q; i += blockDim.x) a.gmu[bidx * q + i] = sy * dmu[i];
+}
+
+// ---------------------------------------------------------------- mix_rows
+// H[row i of t-batch] = gmu_i beta - 2 sum_j Gqq[i,j] V[j,:] - sum_k Gqb[i,k] Vb[k,:]
+// (d value / d V through mu = V beta, Sigma_qq and Sigma_qb)
+template <typename T>
+__global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __restrict__ V,
+                                                       int64_t ldv, const T* __restrict__ Vb,
+                                                       const T* __restrict__ beta,
+                                                       T* __restrict__ H, T* __restrict__ H_lo,
+                                                       int64_t ldh) {
+    extern __shared__ double gs[];  // q*q + q*r + q seeds
+    const int q = a.q, r = a.r;
+    const int64_t n = a.n, bidx = blockIdx.y, rbase = bidx * q;
+    double* gq = gs;
+    double* gqb = gs + q * q;
+    double* gm = gqb + q * r;
+    for (int p = threadIdx.x; p < q * q; p += blockDim.x) gq[p] = a.gqq[bidx * q * q + p];
+    for (int p = threadIdx.x; p < q * r; p += blockDim.x) gqb[p] = a.gqb[bidx * q * r + p];
+    for (int p = threadIdx.x; p < q; p += blockDim.x) gm[p] = a.gmu[bidx * q + p];
+    __syncthreads();
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    T v[kMaxQ];
+    for (int j = 0; j < q; ++j) v[j] = V[(rbase + j) * ldv + c];
+    const T bc = beta[c];
+    for (int i = 0; i < q; ++i) {
+        T h = (T)gm[i] * bc;
+        for (int j = 0; j < q; ++j) h -= T(2) * (T)gq[i * q + j] * v[j];
+        for (int k = 0; k < r; ++k) h -= (T)gqb[i * r + k] * Vb[(int64_t)k * n + c];
+        if constexpr (sizeof(T) == 4) {
+            if (H_lo != nullptr) {  // tf32 split for the tensor-core adjoint GEMM
+                uint32_t hb, lb;
+                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"((float)h));
+                const float hh = __uint_as_float(hb);
+                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"((float)h - hh));
+                H[(rbase + i) * ldh + c] = hh;
+                H_lo[(rbase + i) * ldh + c] = __uint_as_float(lb);
+                continue;
+            }
+        }
+        H[(rbase + i) * ldh + c] = h;
+    }
+}
+
+// ---------------------------------------------------------------- adjoint
+constexpr int kAdjChunk = 64;
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(256) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
+                                                      int64_t ldd) {
+    // smem: D chunk [q][CH] (T), scaled Xt chunk [CH][d] (T)
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int q = a.q, r = a.r, d = a.d;
+    const int64_t n = a.n;
+    const int64_t bidx = blockIdx.x;
+    const int64_t rbase = bidx * q;
+    T* Dc = reinterpret_cast<T*>(smraw);
+    T* Xc = Dc + q * kAdjChunk;
+    double* gq = reinterpret_cast<double*>(Xc + kAdjChunk * d + 8);  // q*q + q*r + q seeds
+    double* gqb = gq + q * q;
+    double* gmu = gqb + q * r;
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32, nwarps = blockDim.x / 32;
+    for (int p = threadIdx.x; p < q * q; p += blockDim.x) gq[p] = a.gqq[bidx * q * q + p];
+    for (int p = threadIdx.x; p < q * r; p += blockDim.x) gqb[p] = a.gqb[bidx * q * r + p];
+    for (int p = threadIdx.x; p < q; p += blockDim.x) gmu[p] = a.gmu[bidx * q + p];
+    if (threadIdx.x == 0 && a.dev_err != nullptr && *a.dev_err != 0) a.status[bidx] = BGB_DEVICE_TIMEOUT;
+    const T os = (T)a.outputscale;
+    for (int i0 = 0; i0 < q; i0 += nwarps) {
+        const int i = i0 + warp;
+        const bool active = i < q;
+        T zx[DMAX], g[DMAX];
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k) {
+            zx[k] = (active && k < d) ? (T)(a.X[(rbase + i) * d + k] * a.inv_ls[k]) : T(0);
+            g[k] = T(0);
+        }
+        for (int64_t c0 = 0; c0 < n; c0 += kAdjChunk) {
+            const int cc = (int)((n - c0) < kAdjChunk ? (n - c0) : kAdjChunk);
+            __syncthreads();
+            for (int p = threadIdx.x; p < q * kAdjChunk; p += blockDim.x) {
+                int j = p / kAdjChunk, c = p % kAdjChunk;
+                Dc[p] = (c < cc) ? Dm[(rbase + j) * ldd + c0 + c] : T(0);
+            }
+            for (int p = threadIdx.x; p < kAdjChunk * d; p += blockDim.x) {
+                int c = p / d, k = p % d;
+                Xc[p] = (c < cc) ? (T)(a.Xt[(c0 + c) * d + k] * a.inv_ls[k]) : T(0);
+            }
+            __syncthreads();
+            if (!active) continue;
+            for (int c = lane; c < cc; c += 32) {
+                // dKc[i, c] = D[i, c] = (d value / d V  L^-1)[i, c]
+                const T dk = Dc[i * kAdjChunk + c];
+                T r2 = T(0);
+                T df[DMAX];
+#pragma unroll
+                for (int k = 0; k < DMAX; ++k) {
+                    df[k] = (k < d) ? zx[k] - Xc[c * d + k] : T(0);
+                    r2 += df[k] * df[k];
+                }
+                const T coef = dk * dkappa_dr2<T>(a.kernel, r2);
+#pragma unroll
+                for (int k = 0; k < DMAX; ++k) g[k] += coef * df[k];
+            }
+        }
+        if (active) {
+            // K(X, X) and K(X, Xb) terms, float64
+            double gx[DMAX];
+#pragma unroll
+            for (int k = 0; k < DMAX; ++k) gx[k] = (double)g[k];
+            for (int j = lane; j < q + r; j += 32) {
+                const double* y = (j < q) ? a.X + (rbase + j) * d : a.Xb + (int64_t)(j - q) * d;
+                const double w = (j < q) ? 2.0 * gq[i * q + j] : gqb[i * r + (j - q)];
+                double dfx[DMAX];
+                double r2 = 0.0;
+#pragma unroll
+                for (int k = 0; k < DMAX; ++k) {
+                    dfx[k] = (k < d) ? (a.X[(rbase + i) * d + k] - y[k]) * a.inv_ls[k] : 0.0;
+                    r2 += dfx[k] * dfx[k];
+                }
+                const double coef = w * dkappa_dr2<double>(a.kernel, r2);
+#pragma unroll
+                for (int k = 0; k < DMAX; ++k) gx[k] += coef * dfx[k];
+            }
+#pragma unroll
+            for (int k = 0; k < DMAX; ++k) {
+                double v = gx[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0 && k < d)
+                    a.grad[(rbase + i) * d + k] = 2.0 * (double)os * a.inv_ls[k] * v;
+            }
+        }
+    }
+}
+
+__global__ void posterior_out_kernel(QBatchArgs a, double* mean, double* covar) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = a.q;
+    if (idx >= a.b * q * q) return;
+    covar[idx] = a.y_std * a.y_std * a.sig[idx];
+    if (idx < a.b * q) mean[idx] = a.y_mean + a.y_std * a.mu[idx];
+}
+
+}  // namespace
+
+template <typename T>
+int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc,
+                        cudaStream_t stream) {
+    if (a.b <= 0) return BGB_OK;
+    if (a.q <= 4) sigma_reduce_kernel<T, 4><<<(unsigned)a.b, 256, 0, stream>>>(a, P, C, ldc);
+    else if (a.q <= 8) sigma_reduce_kernel<T, 8><<<(unsigned)a.b, 256, 0, stream>>>(a, P, C, ldc);
+    else {
+        const int64_t warps = a.b * a.q * a.q;
+        sigma_reduce_pairs_kernel<T><<<(unsigned)ceil_div(warps, 8), 256, 0, stream>>>(a, P, C, ldc);
+    }
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+size_t batch_step_smem_bytes(int q, int r, int S) {
+    const int D = r + q;
+    return sizeof(double) * (size_t)(2 * q * D + 3 * q * q + 2 * q + S + kSampleChunk * q +
+                                     (q * r > q * q ? q * r : 0));
+}
+
+int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream) {
+    if (a.b <= 0) return BGB_OK;
+    if (a.q > kMaxQ) return BGB_ERR_UNSUPPORTED;
+    size_t smem = batch_step_smem_bytes(a.q, a.r, a.S);
+    if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
+    if (smem > 48 * 1024)
+        BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    batch_step_kernel<<<(unsigned)a.b, 128, smem, stream>>>(a, backward);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+template <typename T>
+int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb, T* P,
+                    cudaStream_t stream) {
+    const int64_t rows = a.b * a.q;
+    if (rows <= 0) return BGB_OK;
+    row_dots_kernel<T><<<(unsigned)ceil_div(rows, 8), 256, 0, stream>>>(a, V, ldv, beta, Vb, P);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+template <typename T>
+int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, const T* beta, T* H,
+                    cudaStream_t stream, T* H_lo, int64_t ldh) {
+    if (a.b <= 0) return BGB_OK;
+    if (a.q > kMaxQ) return BGB_ERR_UNSUPPORTED;
+    const size_t smem = sizeof(double) * (size_t)(a.q * a.q + a.q * a.r + a.q);
+    if (smem > 48 * 1024) return BGB_ERR_UNSUPPORTED;
+    dim3 grid((unsigned)ceil_div(a.n, 256), (unsigned)a.b);
+    mix_rows_kernel<T><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ldh > 0 ? ldh : a.n);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+template <typename T>
+size_t adjoint_smem_bytes(int q, int r, int d) {
+    return sizeof(T) * (size_t)(q * kAdjChunk + kAdjChunk * d + 8) +
+           sizeof(double) * (size_t)(q * q + q * r + q) + 16;
+}
+
+template <typename T>
+int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, cudaStream_t stream) {
+    if (a.b <= 0) return BGB_OK;
+    size_t smem = adjoint_smem_bytes<T>(a.q, a.r, a.d);
+    if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
+    const unsigned grid = (unsigned)a.b;
+#define BGB_ADJ(DM)                                                                              \
+    do {                                                                                        \
+        if (smem > 48 * 1024)                                                                   \
+            BGB_CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel<T, DM>,                            \
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                              (int)smem));                                      \
+        adjoint_kernel<T, DM><<<grid, 256, smem, stream>>>(a, D, ldd);                          \
+    } while (0)
+    if (a.d <= 8) BGB_ADJ(8);
+    else if (a.d <= 16) BGB_ADJ(16);
+    else if (a.d <= 32) BGB_ADJ(32);
+    else if (a.d <= 64) BGB_ADJ(64);
+    else return BGB_ERR_UNSUPPORTED;
+#undef BGB_ADJ
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+int launch_posterior_out(const QBatchArgs& a, double* mean, double* covar, cudaStream_t stream) {
+    const int64_t tot = a.b * a.q * a.q;
+    if (tot <= 0) return BGB_OK;
+    posterior_out_kernel<<<(unsigned)ceil_div(tot, 256), 256, 0, stream>>>(a, mean, covar);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+template int launch_sigma_reduce<double>(const QBatchArgs&, const double*, const double*, int64_t,
+                                         cudaStream_t);
+template int launch_sigma_reduce<float>(const QBatchArgs&, const float*, const float*, int64_t,
+                                        cudaStream_t);
+template int launch_row_dots<double>(const QBatchArgs&, const double*, int64_t, const double*,
+                                     const double*, double*, cudaStream_t);
+template int launch_row_dots<float>(const QBatchArgs&, const float*, int64_t, const float*,
+                                    const float*, float*, cudaStream_t);
+template int launch_mix_rows<double>(const QBatchArgs&, const double*, int64_t, const double*,
+                                     const double*, double*, cudaStream_t, double*, int64_t);
+template int launch_mix_rows<float>(const QBatchArgs&, const float*, int64_t, const float*,
+                                    const float*, float*, cudaStream_t, float*, int64_t);
+template int launch_adjoint<double>(const QBatchArgs&, const double*, int64_t, cudaStream_t);
+template int launch_adjoint<float>(const QBatchArgs&, const float*, int64_t, cudaStream_t);
+
+}  // namespace bgb

@@ -1,0 +1,22 @@
+"""Exception types with the reference's names and meaning.
+
+``NotPSDError`` / ``NanError`` mirror linear_operator.utils.errors (raised by
+psd_safe_cholesky and by botorch/utils/low_rank.py:162-171);
+``UnsupportedError`` mirrors botorch/exceptions/errors.py.
+"""
+
+
+class BotorchError(Exception):
+    """Base exception (botorch/exceptions/errors.py:16)."""
+
+
+class UnsupportedError(BotorchError):
+    """Requested configuration is not supported by this path."""
+
+
+class NotPSDError(RuntimeError):
+    """psd_safe_cholesky failed after all jitter retries."""
+
+
+class NanError(RuntimeError):
+    """NaN input to a Cholesky or non-finite posterior samples."""

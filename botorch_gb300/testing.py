@@ -1,0 +1,99 @@
+"""Seeded synthetic workloads for the GP-posterior + MC-acquisition path.
+
+The reference publishes no benchmark data for this path, so every workload is
+synthetic, generated on the host in float64 from a seeded ``torch.Generator``
+(the role botorch/utils/testing.py and botorch/utils/test_helpers.py play in
+the reference). The generators are:
+
+* ``qei_small``: d=6, n=64, X ~ U[0,1]^6, y = sum_j sin(3 x_j) + N(0, 0.01^2);
+  Matern-5/2 ARD with lengthscales 0.5, outputscale 1, noise 1e-4, mean 0;
+  qEI with best_f = max(y) on 512 x 4 x 6 candidates, 256 Sobol samples.
+* ``qlognei_diff``: the same generator at d=12, n=1024; qLogNEI on
+  2048 x 4 x 12 candidates with 512 Sobol samples.
+* ``qlognei_branin``: d=20, y = sum of Branin over 10 disjoint random
+  coordinate pairs mapped to [-5,10] x [0,15] + N(0, 0.01^2); lengthscales
+  U[0.2, 1.0]; noise 1e-4; qLogNEI on b x 8 x 20 candidates, 512 samples.
+  n=4096 is the headline point, n=8192 the large-n precision case.
+* ``rff_draw``: y = sqrt(2/F) sum_i w_i cos(omega_i . x + beta_i) + noise,
+  the random-feature GP draw of the many-model and optimisation workloads.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import torch
+from torch import Tensor
+
+
+@dataclass
+class Workload:
+    name: str
+    train_X: Tensor
+    train_Y: Tensor
+    lengthscale: Tensor
+    outputscale: float
+    noise: float
+    mean_constant: float
+    kernel: str
+    X: Tensor                       # b x q x d candidates
+    n_samples: int
+    seed: int
+    acqf: str                       # "qEI" or "qLogNEI"
+    best_f: float | None = None
+    extra: dict = field(default_factory=dict)
+
+
+def _branin(x1: Tensor, x2: Tensor) -> Tensor:
+    """Branin on [-5,10] x [0,15] (formula of botorch/test_functions/synthetic.py:199)."""
+    b = 5.1 / (4 * math.pi ** 2)
+    c = 5 / math.pi
+    t = 1 / (8 * math.pi)
+    return (x2 - b * x1 ** 2 + c * x1 - 6) ** 2 + 10 * (1 - t) * torch.cos(x1) + 10
+
+
+def qei_small(b: int = 512, q: int = 4, seed: int = 0) -> Workload:
+    g = torch.Generator().manual_seed(seed)
+    d, n = 6, 64
+    X = torch.rand(n, d, generator=g, dtype=torch.float64)
+    y = torch.sin(3 * X).sum(-1) + 0.01 * torch.randn(n, generator=g, dtype=torch.float64)
+    Xc = torch.rand(b, q, d, generator=g, dtype=torch.float64)
+    return Workload("qei_small_d6_n64", X, y.unsqueeze(-1), torch.full((d,), 0.5, dtype=torch.float64),
+                    1.0, 1e-4, 0.0, "matern52", Xc, 256, 0, "qEI", best_f=float(y.max()))
+
+
+def qlognei_diff(b: int = 2048, q: int = 4, n: int = 1024, seed: int = 0) -> Workload:
+    g = torch.Generator().manual_seed(seed)
+    d = 12
+    X = torch.rand(n, d, generator=g, dtype=torch.float64)
+    y = torch.sin(3 * X).sum(-1) + 0.01 * torch.randn(n, generator=g, dtype=torch.float64)
+    Xc = torch.rand(b, q, d, generator=g, dtype=torch.float64)
+    return Workload(f"qlognei_d12_n{n}", X, y.unsqueeze(-1), torch.full((d,), 0.5, dtype=torch.float64),
+                    1.0, 1e-4, 0.0, "matern52", Xc, 512, 0, "qLogNEI")
+
+
+def qlognei_branin(n: int = 4096, b: int = 4096, q: int = 8, d: int = 20, seed: int = 0) -> Workload:
+    g = torch.Generator().manual_seed(seed)
+    X = torch.rand(n, d, generator=g, dtype=torch.float64)
+    perm = torch.randperm(d, generator=g)
+    y = torch.zeros(n, dtype=torch.float64)
+    for p in range(d // 2):
+        i, j = int(perm[2 * p]), int(perm[2 * p + 1])
+        y = y + _branin(-5 + 15 * X[:, i], 15 * X[:, j])
+    y = y + 0.01 * torch.randn(n, generator=g, dtype=torch.float64)
+    ls = 0.2 + 0.8 * torch.rand(d, generator=g, dtype=torch.float64)
+    Xc = torch.rand(b, q, d, generator=g, dtype=torch.float64)
+    return Workload(f"qlognei_branin_d{d}_n{n}_q{q}", X, y.unsqueeze(-1), ls, 1.0, 1e-4, 0.0,
+                    "matern52", Xc, 512, 0, "qLogNEI")
+
+
+def rff_draw(X: Tensor, n_features: int, lengthscale: Tensor, g: torch.Generator,
+             noise_std: float = 0.01) -> Tensor:
+    """Random Fourier feature draw of a squared-exponential GP at X (n x d), plus noise."""
+    d = X.shape[-1]
+    omega = torch.randn(n_features, d, generator=g, dtype=torch.float64) / lengthscale
+    beta = 2 * math.pi * torch.rand(n_features, generator=g, dtype=torch.float64)
+    w = torch.randn(n_features, generator=g, dtype=torch.float64)
+    f = math.sqrt(2.0 / n_features) * torch.cos(X @ omega.T + beta) @ w
+    return f + noise_std * torch.randn(X.shape[0], generator=g, dtype=torch.float64)

@@ -1,0 +1,263 @@
+/*
+ * botorch_gb300 — C ABI of the GB300 (sm_103a) GP-posterior + Monte-Carlo
+ * acquisition path.
+ *
+ * The reference (BoTorch 0.18.1) has no C/C++ interface for this path: it is
+ * reached through Python classes. Each entry point below replaces one step of
+ * that Python path and says which reference code it stands in for. All
+ * pointers are DEVICE pointers unless marked "host". Matrices are row-major
+ * with the stated leading dimension. Every call is asynchronous on `stream`
+ * (a cudaStream_t passed as void*) unless it says it synchronises; scratch
+ * memory is the caller's `workspace` (size from the matching *_bytes query);
+ * nothing here allocates device memory.
+ *
+ * Return codes: BGB_OK (0); positive values are numerical conditions
+ * (BGB_NOT_PSD, BGB_NAN) that the Python layer maps to the reference's
+ * NotPSDError / NanError; negative values are argument or launch errors.
+ */
+#ifndef BOTORCH_GB300_H
+#define BOTORCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BGB_OK 0
+#define BGB_NOT_PSD 1          /* psd_safe_cholesky gave up (linear_operator NotPSDError) */
+#define BGB_NAN 2              /* NaN input / non-finite samples (linear_operator NanError) */
+#define BGB_DEVICE_TIMEOUT 3   /* a bounded wait inside a tensor-core GEMM expired */
+#define BGB_ERR_ARG (-1)       /* invalid size, pointer or option */
+#define BGB_ERR_WORKSPACE (-2) /* workspace smaller than the *_bytes query */
+#define BGB_ERR_CUDA (-3)      /* a CUDA launch or runtime call failed */
+#define BGB_ERR_UNSUPPORTED (-4)
+
+/* Stationary kernels (gpytorch ScaleKernel over MaternKernel(nu) / RBFKernel, ARD). */
+#define BGB_KERNEL_MATERN52 0
+#define BGB_KERNEL_MATERN32 1
+#define BGB_KERNEL_MATERN12 2
+#define BGB_KERNEL_RBF 3
+
+/* Arithmetic of the per-call path. FP64: every step in float64 (the plain
+ * FP64 GPU path). MIXED: kernel build, cross-covariance GEMM and adjoint in
+ * float32, everything that stability needs (q x q Cholesky, sample step,
+ * log-mean-exp, all reductions across tiles) in float64. */
+#define BGB_PREC_FP64 0
+#define BGB_PREC_MIXED 1
+
+#define BGB_ACQF_QEI 0
+#define BGB_ACQF_QLOGNEI 1
+
+/* bgb_acq_t.flags */
+#define BGB_FLAG_SIMT 1        /* MIXED: use the FFMA GEMM even when tensor-core operands are set */
+
+/* An exact GP with fixed hyperparameters (SingleTaskGP, gp_regression.py:108-214).
+ * Hyperparameters live in the standardised outcome space; y_mean / y_std
+ * undo the Standardize outcome transform (transforms/outcome.py:431-511). */
+typedef struct bgb_gp {
+    int64_t n;                     /* training points */
+    int32_t d;                     /* input dimension */
+    int32_t kernel;                /* BGB_KERNEL_* */
+    double outputscale;            /* sigma_f^2 */
+    double mean_constant;          /* constant prior mean */
+    double y_mean;                 /* Standardize offset */
+    double y_std;                  /* Standardize scale */
+    const double* train_X;         /* n x d */
+    const double* inv_lengthscale; /* d: 1 / lengthscale */
+} bgb_gp_t;
+
+/* Everything one acquisition call needs besides the candidates.
+ * With L the Cholesky factor of K = K(Xt,Xt) + noise I:
+ *   B (n x ldb)  L^-T: right operand of the cross-covariance GEMM
+ *                V = K(X,Xt) L^-T (the reference's root-inverse form of the
+ *                predictive covariance: Sigma = K(X,X) - V V^T);
+ *   Linv (n x n) L^-1, right operand of the adjoint GEMM dK = (d value / d V) L^-1;
+ *   beta (n)     L^-1 (y - m), so that the mean is m + V beta;
+ *   Vb (r x n)   K(X_baseline, Xt) L^-T and VbT (n x r) its transpose.
+ * (built by bgb_gp_operands and bgb_baseline_operands). The *32 copies are
+ * used by BGB_PREC_MIXED, the *64 ones by BGB_PREC_FP64. */
+typedef struct bgb_acq {
+    bgb_gp_t gp;
+    int32_t acqf;            /* BGB_ACQF_* */
+    int32_t precision;       /* BGB_PREC_* */
+    int32_t q;               /* points per t-batch */
+    int32_t r;               /* baseline points (0 for qEI) */
+    int32_t n_samples;       /* MC samples S */
+    int32_t flags;           /* BGB_FLAG_* */
+    int64_t ldb;             /* leading dimension of B, >= n */
+    const double* B64;
+    const float* B32;
+    const double* Linv64;
+    const float* Linv32;
+    const double* Vb64;
+    const float* Vb32;
+    const double* VbT64;
+    const float* VbT32;
+    const double* beta64;
+    const float* beta32;
+    /* tensor-core operands of MIXED (tf32 hi/lo, n x ldl, ldl >= n, ldl % 8 == 0):
+     * L^-1 for the forward GEMM and L^-T for the adjoint GEMM; NULL: FFMA GEMM */
+    const float* Lhi;
+    const float* Llo;
+    const float* LThi;
+    const float* LTlo;
+    int64_t ldl;
+    const double* X_baseline;/* r x d */
+    const double* Lb_inv;    /* r x r: inverse of the Cholesky factor of the
+                                untransformed baseline posterior covariance */
+    const double* Z;         /* S x (r+q) base samples */
+    const double* best_f;    /* S values (qLogNEI) or 1 value (qEI) */
+    double tau_relu;         /* logei.py:67 */
+    double tau_max;          /* logei.py:68 */
+} bgb_acq_t;
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int bgb_version(void);
+
+/* (a) Kernel matrix K[i,j] = outputscale * kappa(|(X1_i - X2_j) / l|^2)
+ *     (+ diag_add on i == j when X1 and X2 are the same pointer).
+ * Replaces the evaluation of the covariance module in SingleTaskGP.forward
+ * (botorch/models/gp_regression.py:209-214; gpytorch MaternKernel/RBFKernel). */
+int bgb_kernel_matrix(const bgb_gp_t* gp, const double* X1, int64_t m, const double* X2,
+                      int64_t n2, double diag_add, double* K, int64_t ldk, void* stream);
+
+/* (b) Blocked Cholesky of one SPD matrix in place (lower factor; the strict
+ * upper triangle is zeroed). On failure *info_host = first failing pivot
+ * (1-based) and BGB_NOT_PSD is returned. Synchronises `stream`.
+ * Replaces torch.linalg.cholesky_ex inside linear_operator's psd_safe_cholesky. */
+int bgb_cholesky(double* A, int64_t n, int64_t lda, int32_t* info_host, void* workspace,
+                 size_t workspace_bytes, void* stream);
+size_t bgb_cholesky_workspace_bytes(int64_t n);
+
+/* (b) psd_safe_cholesky for one matrix: plain factorisation, then jitter
+ * j * 10^i added to the diagonal for i < max_tries (j = 1e-8 when jitter <= 0).
+ * `A` is preserved; the factor goes to `L` (ldl). *jitter_host = total jitter.
+ * Synchronises `stream`. Replaces linear_operator psd_safe_cholesky as called
+ * by the exact prediction strategy, cached_cholesky.py:98-124 and
+ * low_rank.py:137-140. */
+int bgb_psd_safe_cholesky(const double* A, int64_t n, int64_t lda, double* L, int64_t ldl,
+                          int32_t max_tries, double jitter, double* jitter_host,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+/* (b) Lower-triangular inverse in place (blocked). */
+int bgb_tri_inverse(double* L, int64_t n, int64_t lda, void* workspace, size_t workspace_bytes,
+                    void* stream);
+size_t bgb_tri_inverse_workspace_bytes(int64_t n);
+
+/* (b) Exact-GP training cache: L = psd_safe_cholesky(K + noise I), Linv = L^-1
+ * (blocked triangular inverse), alpha = K^-1 (y - mean_constant) = L^-T L^-1
+ * (y - m) with one step of iterative refinement, and beta = L^T alpha. y is the
+ * standardised training target (n). Synchronises `stream`. Replaces the
+ * training-side caches of gpytorch's exact prediction strategy (mean cache and
+ * root-inverse cache) under the settings of botorch/__init__.py:51-56. */
+int bgb_gp_fit(const bgb_gp_t* gp, const double* y, double noise, int32_t max_tries,
+               double* L, double* Linv, double* alpha, double* beta, double* jitter_host,
+               void* workspace, size_t workspace_bytes, void* stream);
+size_t bgb_gp_fit_workspace_bytes(int64_t n);
+
+/* (c) Model-level operands: B = Linv^T (n x ldb, ldb >= n) in float64 and
+ * float32 (B32 may be NULL), and float32 copies of Linv and beta (may be NULL). */
+int bgb_gp_operands(const bgb_gp_t* gp, const double* Linv, const double* beta, double* B64,
+                    float* B32, int64_t ldb, float* Linv32, float* beta32, void* stream);
+
+/* (c) Tensor-core operands of the mixed path: the tf32 hi/lo split of L^-1
+ * (Lhi, Llo) and of L^-T (LThi, LTlo), n x ldl each (ldl >= n, ldl % 8 == 0). */
+int bgb_gp_tc_operands(const bgb_gp_t* gp, const double* Linv, int64_t ldl, float* Lhi,
+                       float* Llo, float* LThi, float* LTlo, void* stream);
+
+/* (c) The tensor-core GEMM of the mixed path on caller operands:
+ * C (M x N, ldc) = A (M x K) op(B), with A given as its tf32 hi/lo split (lda)
+ * and B by its K-major storage Bs (N x K, hi/lo, ldbs): op(B)[k][j] = Bs[j][k].
+ * kmode 3: op(B) upper triangular (k <= j); kmode 1: op(B) lower triangular
+ * (k >= j). 3xTF32 products accumulated in float32 TMEM. *err_dev (device
+ * int, may be NULL) is set non-zero if a bounded wait expired. lda, ldbs and
+ * ldc must be multiples of 4 and the pointers 16-byte aligned. Exposed for
+ * tests and for callers with their own operands. */
+int bgb_crosscov_gemm_tf32x3(int64_t M, int64_t N, int64_t K, const float* A_hi,
+                             const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
+                             int64_t ldbs, float* C, int64_t ldc, int32_t kmode, int32_t* err_dev,
+                             void* stream);
+
+/* (c) Baseline operands of qLogNEI: Vb = K(X_baseline, Xt) L^-T (r x n) and
+ * VbT (n x r), float64 and float32 (the float32 pointers may be NULL). */
+int bgb_baseline_operands(const bgb_gp_t* gp, const double* Linv, const double* X_baseline,
+                          int32_t r, double* Vb64, float* Vb32, double* VbT64, float* VbT32,
+                          void* workspace, size_t workspace_bytes, void* stream);
+size_t bgb_baseline_operands_workspace_bytes(int64_t n, int32_t r);
+
+/* (c)+(d) Posterior mean (b x q) and covariance (b x q x q), untransformed
+ * (acq->r must be 0). Replaces
+ * BatchedMultiOutputGPyTorchModel.posterior (botorch/models/gpytorch.py:544-611)
+ * followed by Standardize.untransform_posterior. */
+int bgb_posterior(const bgb_acq_t* acq, const double* X, int64_t b, double* mean, double* covar,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* Joint posterior over m points (mean m, covariance m x m, untransformed):
+ * Kc = K(X, Xt), V = Kc L^-T, covar = K(X, X) - V V^T, mean = m + Kc alpha,
+ * float64. Used at initialisation for the baseline posterior and for pruning
+ * (botorch/acquisition/logei.py:393-459, acquisition/utils.py:276-437). */
+int bgb_posterior_joint(const bgb_gp_t* gp, const double* Linv, const double* alpha,
+                        const double* X, int64_t m, double* mean, double* covar, void* workspace,
+                        size_t workspace_bytes, void* stream);
+size_t bgb_posterior_joint_workspace_bytes(int64_t n, int64_t m);
+
+/* prune_inferior_points (botorch/acquisition/utils.py:347-437): joint posterior
+ * at X (m x d), L = psd_safe_cholesky(covar), samples = mean + Z L^T for the S
+ * base samples Z (S x m), and counts[j] = number of samples whose argmax (first
+ * maximal index, as torch.argmax) is j. counts is int32 (m). Synchronises. */
+int bgb_prune_counts(const bgb_gp_t* gp, const double* Linv, const double* alpha, const double* X,
+                     int64_t m, const double* Z, int32_t S, int32_t max_tries, int32_t* counts,
+                     void* workspace, size_t workspace_bytes, void* stream);
+size_t bgb_prune_counts_workspace_bytes(int64_t n, int64_t m, int32_t S);
+
+/* qLogNEI baseline with cached root (logei.py:393-459, cached_cholesky.py:98-124):
+ * joint posterior at X_baseline (r x d), Lb = psd_safe_cholesky(covar) (r x r),
+ * Lb_inv = Lb^-1, baseline samples mean + Zb Lb^T and best_f[s] = max over r
+ * (acquisition/utils.py:137-141). Synchronises. */
+int bgb_qlognei_baseline(const bgb_gp_t* gp, const double* Linv, const double* alpha,
+                         const double* X_baseline, int32_t r, const double* Zb, int32_t S,
+                         int32_t max_tries, double* Lb, double* Lb_inv, double* best_f,
+                         double* jitter_host, void* workspace, size_t workspace_bytes,
+                         void* stream);
+size_t bgb_qlognei_baseline_workspace_bytes(int64_t n, int32_t r, int32_t S);
+
+/* Workspace for bgb_acq_forward / bgb_acq_forward_backward / bgb_posterior at b t-batches. */
+size_t bgb_acq_workspace_bytes(const bgb_acq_t* acq, int64_t b);
+
+/* (c)-(e) Acquisition value (b) at X (b x q x d). status (b, int32): 0 ok,
+ * BGB_NOT_PSD / BGB_NAN per t-batch (value NaN there).
+ * Replaces qExpectedImprovement.forward / qLogNoisyExpectedImprovement.forward
+ * (botorch/acquisition/monte_carlo.py:268-305; logei.py:376-391, 527-565;
+ * cached_cholesky.py:126-170; utils/low_rank.py:84-172). Asynchronous: the
+ * return code covers the launches, the per-batch outcome is in `status`. */
+int bgb_acq_forward(const bgb_acq_t* acq, const double* X, int64_t b, double* value,
+                    int32_t* status, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Value (b) and gradient d value / d X (b x q x d) by the hand-written adjoint:
+ * reverse through the sample reduction, the sample step, the q x q Cholesky and
+ * the cross-covariance solve, recomputing K(X, Xt). Replaces
+ * torch.autograd.grad(acqf(X).sum(), X) in botorch/generation/gen.py:466-469. */
+int bgb_acq_forward_backward(const bgb_acq_t* acq, const double* X, int64_t b, double* value,
+                             double* grad, int32_t* status, void* workspace,
+                             size_t workspace_bytes, void* stream);
+
+/* Same as bgb_acq_forward_backward, with CUDA events recorded on `stream`
+ * between its seven stages (kernel build, forward cross-covariance GEMMs,
+ * covariance reduction, per-batch step, row mix, adjoint GEMM, adjoint
+ * contraction); stage_ms_host (7 floats, host) gets the stage durations.
+ * Synchronises. Measurement aid; no reference counterpart. */
+int bgb_acq_forward_backward_timed(const bgb_acq_t* acq, const double* X, int64_t b,
+                                   double* value, double* grad, int32_t* status, void* workspace,
+                                   size_t workspace_bytes, float* stage_ms_host, void* stream);
+
+/* Number of kernel launches this library has issued in the process so far.
+ * Measurement aid; no reference counterpart. */
+unsigned long long bgb_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BOTORCH_GB300_H */

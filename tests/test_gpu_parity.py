@@ -1,0 +1,289 @@
+"""Parity of the CUDA path (through the C ABI) with the float64 CPU oracle.
+
+Tolerances (from the target of this path): the plain float64 kernels within
+1e-9 relative; the mixed-precision form within 1e-5 relative on the
+acquisition value and 1e-4 on the gradient. "Relative" is the norm-wise
+relative error ||x - x_ref|| / ||x_ref|| over the t-batches of a call; the
+elementwise checks use max |x - x_ref| / max(|x_ref|, 1).
+"""
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+from botorch_gb300 import (ConstantMean, GaussianLikelihood, MaternKernel, NanError, RBFKernel,
+                           ScaleKernel, SingleTaskGP, SobolQMCNormalSampler, qExpectedImprovement,
+                           qLogNoisyExpectedImprovement, prune_inferior_points)
+from botorch_gb300 import _native as nat
+from botorch_gb300 import testing as T
+from oracle.acquisition import (QExpectedImprovement as OQEI, QLogNoisyExpectedImprovement as OQLogNEI,
+                                prune_inferior_points as oracle_prune, qei_value_and_grad)
+from oracle.gp import ExactGP, kernel_matrix
+
+pytestmark = pytest.mark.gpu
+DEV = torch.device("cuda:0")
+TOL = {"fp64": (1e-9, 1e-9), "mixed": (1e-5, 1e-4)}
+# float64 oracle outputs pinned on the x86 host (tests/golden/make_parity_fixtures.py)
+FIX = np.load(Path(__file__).resolve().parent / "golden" / "parity_fixtures.npz")
+
+
+def fixture(name):
+    return torch.from_numpy(FIX[name])
+
+
+def check_inputs(w, key):
+    """The seeded generator must reproduce the inputs the fixture was made from."""
+    from tests.golden.make_parity_fixtures import checksum
+
+    assert np.allclose(checksum(w.X), FIX[key], rtol=1e-12, atol=0), "workload inputs differ"
+
+
+def rel(a, b):
+    a, b = a.detach().double().cpu(), b.detach().double().cpu()
+    return float((a - b).norm() / b.norm().clamp_min(1e-300))
+
+
+def elem(a, b):
+    a, b = a.detach().double().cpu(), b.detach().double().cpu()
+    return float(((a - b).abs() / b.abs().clamp_min(1.0)).max())
+
+
+def gpu_model(w, kernel_cls=None):
+    d = w.train_X.shape[-1]
+    if w.kernel == "rbf":
+        base = RBFKernel(ard_num_dims=d, lengthscale=w.lengthscale)
+    else:
+        nu = {"matern52": 2.5, "matern32": 1.5, "matern12": 0.5}[w.kernel]
+        base = MaternKernel(nu=nu, ard_num_dims=d, lengthscale=w.lengthscale)
+    return SingleTaskGP(w.train_X, w.train_Y, likelihood=GaussianLikelihood(w.noise),
+                        covar_module=ScaleKernel(base, outputscale=w.outputscale),
+                        mean_module=ConstantMean(w.mean_constant), device=DEV)
+
+
+def oracle_model(w):
+    return ExactGP(w.train_X, w.train_Y, w.lengthscale, w.outputscale, w.noise, w.mean_constant, w.kernel)
+
+
+@pytest.mark.parametrize("kind", ["matern52", "matern32", "matern12", "rbf"])
+def test_kernel_matrix(cuda_lib, kind):
+    g = torch.Generator().manual_seed(3)
+    m, n, d = 77, 131, 7
+    X1 = torch.rand(m, d, generator=g, dtype=torch.float64)
+    X2 = torch.rand(n, d, generator=g, dtype=torch.float64)
+    ls = 0.3 + torch.rand(d, generator=g, dtype=torch.float64)
+    ref = kernel_matrix(X1, X2, ls, 1.7, kind)
+    X1d, X2d, il = X1.to(DEV), X2.to(DEV), (1 / ls).to(DEV)
+    K = torch.empty(m, n, dtype=torch.float64, device=DEV)
+    gp = nat.BgbGP(n=n, d=d, kernel=nat.KERNELS[kind], outputscale=1.7, mean_constant=0.0,
+                   y_mean=0.0, y_std=1.0, train_X=X2d.data_ptr(), inv_lengthscale=il.data_ptr())
+    rc = cuda_lib.bgb_kernel_matrix(ctypes.byref(gp), X1d.data_ptr(), m, X2d.data_ptr(), n, 0.0,
+                                    K.data_ptr(), n, nat.stream_handle(DEV))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert elem(K, ref) < 1e-13
+
+
+@pytest.mark.parametrize("n", [65, 300])
+def test_gp_fit_matches_oracle(cuda_lib, n):
+    w = T.qlognei_diff(b=4, q=2, n=n)
+    gm, om = gpu_model(w), oracle_model(w)
+    assert rel(gm.L, om.L) < 1e-11
+    assert rel(gm.alpha, om.alpha) < 1e-10
+    Linv_ref = torch.linalg.solve_triangular(om.L, torch.eye(n, dtype=torch.float64), upper=False)
+    assert rel(gm.Linv, Linv_ref) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_posterior(cuda_lib, precision):
+    w = T.qlognei_diff(b=16, q=4, n=200)
+    gm, om = gpu_model(w), oracle_model(w)
+    post = gm.posterior(w.X.to(DEV), precision=precision)
+    mean, cov = om.posterior(w.X)
+    tol = 1e-10 if precision == "fp64" else 1e-5
+    assert rel(post.mean.squeeze(-1), mean) < tol
+    assert rel(post.covariance_matrix, cov) < tol * 10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_qei_small_config(cuda_lib, precision):
+    w = T.qei_small()
+    check_inputs(w, "qei_small_Xsum")
+    gm = gpu_model(w)
+    sampler = SobolQMCNormalSampler(torch.Size([w.n_samples]), seed=w.seed)
+    acqf = qExpectedImprovement(gm, best_f=w.best_f, sampler=sampler, precision=precision)
+    X = w.X.to(DEV).requires_grad_(True)
+    v = acqf(X)
+    v.sum().backward()
+    ov, og = fixture("qei_small_value"), fixture("qei_small_grad")
+    tv, tg = TOL[precision]
+    assert rel(v, ov) < tv, rel(v, ov)
+    assert rel(X.grad, og) < tg, rel(X.grad, og)
+
+
+def _qlognei_pair(w, precision, prune=True):
+    gm, om = gpu_model(w), oracle_model(w)
+    torch.manual_seed(0)
+    oa = OQLogNEI(om, w.train_X, w.n_samples, w.seed, prune_baseline=prune)
+    torch.manual_seed(0)
+    ga = qLogNoisyExpectedImprovement(gm, w.train_X, sampler=SobolQMCNormalSampler(
+        torch.Size([w.n_samples]), seed=w.seed), prune_baseline=prune, precision=precision)
+    return ga, oa
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_qlognei_differentiation_config(cuda_lib, precision):
+    w = T.qlognei_diff()          # d=12, n=1024, b=2048, q=4, 512 samples
+    check_inputs(w, "qlognei_diff_Xsum")
+    gm = gpu_model(w)
+    torch.manual_seed(0)
+    ga = qLogNoisyExpectedImprovement(gm, w.train_X, sampler=SobolQMCNormalSampler(
+        torch.Size([w.n_samples]), seed=w.seed), precision=precision)
+    assert torch.equal(ga.X_baseline.cpu(), fixture("qlognei_diff_Xb"))
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    idx = fixture("qlognei_diff_idx")
+    ov, og = fixture("qlognei_diff_value"), fixture("qlognei_diff_grad")
+    if precision == "fp64":
+        assert rel(v[idx], ov) < 1e-9, rel(v[idx], ov)
+        assert rel(X.grad[idx], og) < 1e-9, rel(X.grad[idx], og)
+    else:
+        # The float32 cross-covariance carries ~1e-6 absolute error in the mean
+        # and ~1e-8 in the covariance; t-batches whose dominant samples lie within
+        # ~100 tau_relu of the incumbent amplify it by up to 1 / tau_relu.
+        assert rel(v[idx], ov) < 1e-5, rel(v[idx], ov)
+        assert rel(X.grad[idx], og) < 1e-3, rel(X.grad[idx], og)
+
+
+def test_qlognei_gradient_central_differences(cuda_lib):
+    w = T.qlognei_diff(b=32)
+    ga, _ = _qlognei_pair(w, "fp64")
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    g = X.grad.cpu()
+    h = 1e-6
+    gen = torch.Generator().manual_seed(5)
+    for _ in range(24):
+        bi = int(torch.randint(0, 32, (1,), generator=gen))
+        qi = int(torch.randint(0, 4, (1,), generator=gen))
+        di = int(torch.randint(0, 12, (1,), generator=gen))
+        Xp, Xm = w.X.clone(), w.X.clone()
+        Xp[bi, qi, di] += h
+        Xm[bi, qi, di] -= h
+        with torch.no_grad():
+            fd = (ga(Xp.to(DEV))[bi] - ga(Xm.to(DEV))[bi]).item() / (2 * h)
+        assert abs(fd - g[bi, qi, di].item()) <= 1e-4 * max(1.0, abs(fd)), (bi, qi, di, fd, g[bi, qi, di])
+
+
+def test_prune_matches_oracle(cuda_lib):
+    w = T.qlognei_branin(n=512, b=4)
+    gm, om = gpu_model(w), oracle_model(w)
+    torch.manual_seed(3)
+    a = prune_inferior_points(gm, w.train_X)
+    torch.manual_seed(3)
+    b = oracle_prune(om, w.train_X)
+    assert torch.equal(a.cpu(), b)
+
+
+@pytest.mark.parametrize("kind", ["rbf", "matern32", "matern12"])
+def test_qlognei_other_kernels(cuda_lib, kind):
+    w = T.qlognei_diff(b=64, q=3, n=257)
+    w.kernel = kind
+    ga, oa = _qlognei_pair(w, "fp64")
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    ov, og = oa.value_and_grad(w.X)
+    assert rel(v, ov) < 1e-9 and rel(X.grad, og) < 1e-8
+
+
+@pytest.mark.parametrize("q", [1, 2, 5, 16])
+def test_qlognei_ragged_q(cuda_lib, q):
+    w = T.qlognei_diff(b=24, q=q, n=130)
+    ga, oa = _qlognei_pair(w, "fp64")
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    ov, og = oa.value_and_grad(w.X)
+    assert rel(v, ov) < 1e-9 and rel(X.grad, og) < 1e-8
+
+
+def test_qlognei_singular_q_batch_uses_jitter(cuda_lib):
+    # two identical points in a q-batch make Sigma_qq singular: psd_safe_cholesky adds jitter
+    w = T.qlognei_diff(b=8, q=3, n=100)
+    w.X[:, 1] = w.X[:, 0]
+    ga, oa = _qlognei_pair(w, "fp64")
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    ov, og = oa.value_and_grad(w.X)
+    # the jittered factor of a rank-deficient block amplifies rounding: looser bound
+    assert rel(v, ov) < 1e-5
+    assert torch.isfinite(X.grad).all()
+
+
+def test_candidates_on_training_points(cuda_lib):
+    w = T.qlognei_diff(b=8, q=2, n=100)
+    w.X[:, 0] = w.train_X[:8]
+    ga, oa = _qlognei_pair(w, "fp64")
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    ov, og = oa.value_and_grad(w.X)
+    assert rel(v, ov) < 1e-8 and rel(X.grad, og) < 1e-6
+
+
+def test_nan_candidates_raise(cuda_lib):
+    w = T.qlognei_diff(b=4, q=2, n=100)
+    ga, _ = _qlognei_pair(w, "fp64")
+    X = w.X.clone()
+    X[1, 0, 0] = float("nan")
+    with pytest.raises(NanError):
+        ga(X.to(DEV))
+
+
+def test_batch_shapes_and_empty(cuda_lib):
+    w = T.qlognei_diff(b=12, q=2, n=100)
+    ga, oa = _qlognei_pair(w, "fp64")
+    X = w.X.reshape(3, 4, 2, 12).to(DEV)
+    v = ga(X)
+    assert v.shape == (3, 4)
+    assert rel(v.reshape(-1), oa(w.X)) < 1e-9
+    assert ga(w.X[0].to(DEV)).shape == (1,)
+    assert ga(w.X[:0].to(DEV)).shape == (0,)
+
+
+def test_headline_mixed_matches_oracle(cuda_lib):
+    w = T.qlognei_branin(n=4096, b=4096, q=8, d=20)
+    check_inputs(w, "qlognei_branin_Xsum")
+    gm = gpu_model(w)
+    torch.manual_seed(0)
+    ga = qLogNoisyExpectedImprovement(gm, w.train_X, sampler=SobolQMCNormalSampler(
+        torch.Size([w.n_samples]), seed=w.seed), precision="mixed")
+    assert torch.equal(ga.X_baseline.cpu(), fixture("qlognei_branin_Xb"))
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    idx = fixture("qlognei_branin_idx")
+    ov, og = fixture("qlognei_branin_value"), fixture("qlognei_branin_grad")
+    assert rel(v[idx], ov) < 1e-5, rel(v[idx], ov)
+    assert rel(X.grad[idx], og) < 3e-4, rel(X.grad[idx], og)
+
+
+def test_headline_fp64_matches_oracle(cuda_lib):
+    w = T.qlognei_branin(n=4096, b=128, q=8, d=20)
+    gm = gpu_model(w)
+    torch.manual_seed(0)
+    ga = qLogNoisyExpectedImprovement(gm, w.train_X, sampler=SobolQMCNormalSampler(
+        torch.Size([w.n_samples]), seed=w.seed), precision="fp64")
+    idx = fixture("qlognei_branin_idx")
+    sel = idx[idx < 128]
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    ov, og = fixture("qlognei_branin_value")[: len(sel)], fixture("qlognei_branin_grad")[: len(sel)]
+    assert rel(v[sel], ov) < 1e-9 and rel(X.grad[sel], og) < 1e-9

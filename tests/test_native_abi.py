@@ -1,0 +1,86 @@
+"""The C ABI library loads and exports every symbol include/botorch_gb300.h declares (no GPU calls)."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from botorch_gb300 import _native
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "botorch_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bgb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_bound_functions():
+    assert set(declared_functions()) == set(_native.exported_symbols())
+
+
+def test_library_exports_every_declared_symbol():
+    if not _native.lib_path().exists():
+        from botorch_gb300.build import build
+        build()
+    lib = _native.lib()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert lib.bgb_version() >= 100
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """ctypes mirrors of bgb_gp_t / bgb_acq_t have the C compiler's layout."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f for f, _ in _native.BgbAcq._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "botorch_gb300.h"\n'
+        "int main(void) {\n"
+        '  printf("%zu %zu\\n", sizeof(bgb_gp_t), sizeof(bgb_acq_t));\n'
+        + "".join(f'  printf("%zu\\n", offsetof(bgb_acq_t, {f}));\n' for f in fields)
+        + "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(HEADER.parent), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert int(out[0]) == ctypes.sizeof(_native.BgbGP)
+    assert int(out[1]) == ctypes.sizeof(_native.BgbAcq)
+    for f, off in zip(fields, out[2:]):
+        assert getattr(_native.BgbAcq, f).offset == int(off), f
+
+
+def test_workspace_queries_need_no_gpu():
+    lib = _native.lib()
+    n = 4096
+    assert lib.bgb_gp_fit_workspace_bytes(n) >= n * n * 8
+    gp = _native.BgbGP(n=n, d=20, kernel=0, outputscale=1.0, mean_constant=0.0, y_mean=0.0,
+                       y_std=1.0, train_X=1, inv_lengthscale=1)
+    acq = _native.BgbAcq(gp=gp, acqf=1, precision=1, q=8, r=2, n_samples=512, ldb=n + 8)
+    ws = lib.bgb_acq_workspace_bytes(ctypes.byref(acq), 4096)
+    assert ws >= 4096 * 8 * n * 4 * 2
+
+
+def test_invalid_arguments_are_rejected_without_touching_the_device():
+    lib = _native.lib()
+    assert lib.bgb_kernel_matrix(None, None, 0, None, 0, 0.0, None, 0, None) == _native.BGB_ERR_ARG
+    acq = _native.BgbAcq()
+    assert lib.bgb_acq_forward(ctypes.byref(acq), None, 1, None, None, None, 0, None) == _native.BGB_ERR_ARG
+
+
+def test_product_requires_cuda():
+    import torch
+
+    from botorch_gb300 import SingleTaskGP, UnsupportedError
+
+    if torch.cuda.is_available():
+        pytest.skip("CPU-only check")
+    with pytest.raises((UnsupportedError, RuntimeError, AssertionError)):
+        SingleTaskGP(torch.rand(4, 2, dtype=torch.float64), torch.rand(4, 1, dtype=torch.float64),
+                     device="cpu")
