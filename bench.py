@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--b", type=int, default=B)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile", action="store_true",
+                   help="only warm up and run --steps mixed-precision steps between "
+                        "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+    p.add_argument("--simt", action="store_true", help="FFMA GEMMs instead of tcgen05")
     return p.parse_args()
 
 
@@ -210,6 +214,7 @@ def run_ours(args) -> None:
     model = make_model(device, w)
     acqf = make_acqf(model, w, "mixed")
     acqf.check_status = False
+    acqf.use_tensor_cores = not args.simt
     Xd = w.X.to(device).contiguous()
     out = (torch.empty(b, dtype=torch.float64, device=device),
            torch.empty(b, Q, DIM, dtype=torch.float64, device=device),
@@ -219,6 +224,15 @@ def run_ours(args) -> None:
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize(device)
+    if args.profile:
+        torch.cuda.profiler.start()
+        for _ in range(args.steps):
+            flush.zero_()
+            step()
+        torch.cuda.synchronize(device)
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_steps": args.steps, "b": b, "status_ok": int(out[2].max().item()) == 0}))
+        return
     lib = nat.lib()
     if world > 1:
         torch.distributed.barrier()

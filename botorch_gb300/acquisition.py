@@ -159,11 +159,14 @@ class qExpectedImprovement(_MCAcquisition):
                  posterior_transform=None, X_pending: Tensor | None = None, constraints=None,
                  eta: float = 1e-3, precision: str = "mixed") -> None:
         super().__init__(model, sampler, objective, posterior_transform, constraints, precision)
-        bf = torch.as_tensor(best_f, dtype=torch.float64)
+        # torch.as_tensor without a dtype, as the reference's register_buffer
+        # (monte_carlo.py:420): a Python float becomes a tensor of the default
+        # dtype first, and that value is what the improvement is measured from.
+        bf = torch.as_tensor(best_f)
         if bf.numel() != 1:
             raise UnsupportedError("a scalar best_f is supported")
         self.best_f = bf.reshape(())
-        self._best_f_dev = bf.reshape(1).to(self.device)
+        self._best_f_dev = bf.reshape(1).to(self.device, torch.float64)
         self.set_X_pending(X_pending)
 
     def set_X_pending(self, X_pending: Tensor | None = None) -> None:

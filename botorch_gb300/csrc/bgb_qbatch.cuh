@@ -47,16 +47,17 @@ int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta,
 template <typename T>
 int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc,
                         cudaStream_t stream);
-int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream);
-size_t batch_step_smem_bytes(int q, int r, int S);
+// mixed: float32 evaluation of the per-sample smooth reductions (see qbatch.cu)
+int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bool mixed = false);
+size_t batch_step_smem_bytes(int q, int r, int S, bool mixed_backward);
 // H (b*q x n) = gmu beta^T - 2 Gqq V - Gqb Vb per t-batch
 // H_lo non-null (float32): write the tf32 hi/lo split (H = hi) with leading dimension ldh.
 template <typename T>
 int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, const T* beta, T* H,
                     cudaStream_t stream, T* H_lo = nullptr, int64_t ldh = 0);
-// d value / d X from D (b*q x n) = H L^-1
+// d value / d X from D (b*q x n) = H L^-1; Xs: training inputs scaled by 1 / lengthscale (n x d)
 template <typename T>
-int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, cudaStream_t stream);
+int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* Xs, cudaStream_t stream);
 int launch_posterior_out(const QBatchArgs& a, double* mean, double* covar, cudaStream_t stream);
 
 }  // namespace bgb

@@ -22,6 +22,18 @@ __global__ void sub_const_kernel(const double* x, double c, double* y, int64_t n
     if (i < n) y[i] = x[i] - c;
 }
 
+// XsT[k][c] = Xt[c][k] / l_k (k-major, for the adjoint's coalesced staging)
+__global__ void scale_inputs_kernel(const double* X, const double* il, int64_t n, int d,
+                                    double* Xs64, float* Xs32) {
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * d) return;
+    const int64_t c = idx / d;
+    const int k = (int)(idx % d);
+    const double v = X[idx] * il[k];
+    Xs64[(int64_t)k * n + c] = v;
+    if (Xs32 != nullptr) Xs32[(int64_t)k * n + c] = (float)v;
+}
+
 // B = [Linv^T | 0]: B[k][j] = Linv[j][k] for j < n
 __global__ void fill_b_kernel(const double* Linv, int64_t n, double* B, int64_t ldb) {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -118,10 +130,14 @@ int valid_acq(const bgb_acq_t* a) {
     if (a == nullptr || !valid_gp(&a->gp)) return 0;
     if (a->q <= 0 || a->r < 0 || a->ldb < a->gp.n) return 0;
     if (a->precision == BGB_PREC_FP64) {
-        if (a->B64 == nullptr || a->Linv64 == nullptr || a->beta64 == nullptr) return 0;
+        if (a->B64 == nullptr || a->Linv64 == nullptr || a->beta64 == nullptr ||
+            a->Xs64 == nullptr)
+            return 0;
         if (a->r > 0 && (a->Vb64 == nullptr || a->VbT64 == nullptr)) return 0;
     } else if (a->precision == BGB_PREC_MIXED) {
-        if (a->B32 == nullptr || a->Linv32 == nullptr || a->beta32 == nullptr) return 0;
+        if (a->B32 == nullptr || a->Linv32 == nullptr || a->beta32 == nullptr ||
+            a->Xs32 == nullptr)
+            return 0;
         if (a->r > 0 && (a->Vb32 == nullptr || a->VbT32 == nullptr)) return 0;
     } else {
         return 0;
@@ -138,6 +154,7 @@ template <> struct Ops<float> {
     static const float* Vb(const bgb_acq_t* a) { return a->Vb32; }
     static const float* VbT(const bgb_acq_t* a) { return a->VbT32; }
     static const float* beta(const bgb_acq_t* a) { return a->beta32; }
+    static const float* Xs(const bgb_acq_t* a) { return a->Xs32; }
     static int gemm(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,
                     int64_t ldb, float* C, int64_t ldc, int kmode, int64_t n_tri, cudaStream_t st) {
         return gemm_f32(M, N, K, A, lda, B, ldb, C, ldc, kmode, n_tri, st);
@@ -154,6 +171,7 @@ template <> struct Ops<double> {
     static const double* Vb(const bgb_acq_t* a) { return a->Vb64; }
     static const double* VbT(const bgb_acq_t* a) { return a->VbT64; }
     static const double* beta(const bgb_acq_t* a) { return a->beta64; }
+    static const double* Xs(const bgb_acq_t* a) { return a->Xs64; }
     static int gemm(int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
                     const double* B, int64_t ldb, double* C, int64_t ldc, int kmode, int64_t n_tri,
                     cudaStream_t st) {
@@ -217,7 +235,7 @@ int run_call(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs& qa, T* 
     const int64_t n = a->gp.n, rows = b * a->q;
     int rc = run_front<T>(a, X, b, &qa, Kc, C, P, st, ev);
     if (rc) return rc;
-    rc = launch_batch_step(qa, backward, st);
+    rc = launch_batch_step(qa, backward, st, sizeof(T) == 4);
     if (rc) return rc;
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[4], st));
     if (!backward) return BGB_OK;
@@ -243,7 +261,7 @@ int run_call(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs& qa, T* 
         if (rc) return rc;
     }
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[6], st));
-    rc = launch_adjoint<T>(qa, C, a->ldb, st);
+    rc = launch_adjoint<T>(qa, C, a->ldb, Ops<T>::Xs(a), st);
     if (rc) return rc;
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[7], st));
     return BGB_OK;
@@ -418,8 +436,10 @@ int bgb_gp_fit(const bgb_gp_t* gp, const double* y, double noise, int32_t max_tr
 }
 
 int bgb_gp_operands(const bgb_gp_t* gp, const double* Linv, const double* beta, double* B64,
-                    float* B32, int64_t ldb, float* Linv32, float* beta32, void* stream) {
-    if (!valid_gp(gp) || Linv == nullptr || beta == nullptr || B64 == nullptr) return BGB_ERR_ARG;
+                    float* B32, int64_t ldb, float* Linv32, float* beta32, double* Xs64,
+                    float* Xs32, void* stream) {
+    if (!valid_gp(gp) || Linv == nullptr || beta == nullptr || B64 == nullptr || Xs64 == nullptr)
+        return BGB_ERR_ARG;
     const int64_t n = gp->n;
     if (ldb < n) return BGB_ERR_ARG;
     cudaStream_t st = as_stream(stream);
@@ -429,6 +449,9 @@ int bgb_gp_operands(const bgb_gp_t* gp, const double* Linv, const double* beta, 
     if (B32 != nullptr && (rc = convert_f64_f32(B64, B32, n * ldb, st)) != BGB_OK) return rc;
     if (Linv32 != nullptr && (rc = convert_f64_f32(Linv, Linv32, n * n, st)) != BGB_OK) return rc;
     if (beta32 != nullptr && (rc = convert_f64_f32(beta, beta32, n, st)) != BGB_OK) return rc;
+    scale_inputs_kernel<<<(unsigned)ceil_div(n * gp->d, 256), 256, 0, st>>>(
+        gp->train_X, gp->inv_lengthscale, n, gp->d, Xs64, Xs32);
+    BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
 

@@ -8,8 +8,15 @@
 //
 // One CTA computes a 128 x 256 tile of C. Warp roles: warp 0 issues the TMA
 // loads (one elected lane), warp 1 owns the TMEM allocation and issues the
-// MMAs (one elected lane), warps 2-5 drain the accumulator (tcgen05.ld) and
-// store C. Two shared-memory stages of {A_hi, A_lo, B_hi, B_lo} (96 KB each).
+// MMAs (one elected lane), warps 2-9 drain the accumulators. Two shared-memory
+// stages of {A_hi, A_lo, B_hi, B_lo} (96 KB each).
+//
+// Accumulation: the K range is cut into chunks of TC_FLUSH k-blocks; each chunk
+// is accumulated in one of two TMEM accumulators (ping-pong, 2 x 256 columns)
+// while the epilogue warps add the previous chunk into float32 registers
+// (round-to-nearest). Keeping each tensor-core accumulation short holds the
+// 3xTF32 product to float32 accuracy over long K.
+//
 // Every mbarrier wait is bounded in time; on expiry the CTA records an error
 // code, stops issuing work, waits (bounded) for its copies in flight, frees
 // its TMEM and returns.
@@ -28,8 +35,9 @@ constexpr int TC_UMMA_K = 8;                          // tf32 K per tcgen05.mma
 constexpr uint32_t A_TILE = TC_BM * TC_BK * 4;        // 16 KB
 constexpr uint32_t B_TILE = TC_BN * TC_BK * 4;        // 32 KB
 constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
-constexpr int TC_THREADS = 192;
-constexpr uint32_t TMEM_COLS = 256;
+constexpr int TC_THREADS = 320;                       // 10 warps
+constexpr int TC_FLUSH = 1;                           // k-blocks per TMEM accumulation chunk
+constexpr uint32_t TMEM_COLS = 512;                   // two 128 x 256 float32 accumulators
 constexpr size_t TC_SMEM = TC_STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
@@ -57,8 +65,14 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                  : "memory");
 }
 
-// Wait for the phase with parity `phase` to complete; false after kWaitNs.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Wait for the phase with parity `phase` to complete; false after kWaitNs or
+// as soon as another role of the CTA has recorded a failure in *fail.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase,
+                                          const int* fail = nullptr) {
     const uint32_t addr = smem_u32(bar);
     const unsigned long long t0 = global_ns();
     while (true) {
@@ -71,6 +85,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
             : "r"(addr), "r"(phase)
             : "memory");
         if (done) return true;
+        if (fail != nullptr && *(volatile const int*)fail != 0) return false;
         if (global_ns() - t0 > kWaitNs) return false;
     }
 }
@@ -138,8 +153,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                                ~(uintptr_t)1023);
     uint64_t* full = reinterpret_cast<uint64_t*>(base + TC_STAGES * STAGE_BYTES);
     uint64_t* empty = full + TC_STAGES;
-    uint64_t* accum = empty + TC_STAGES;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+    uint64_t* accf = empty + TC_STAGES;  // accumulator a holds a finished chunk
+    uint64_t* acce = accf + 2;           // accumulator a has been drained
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
     int* fail = reinterpret_cast<int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -156,7 +172,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accum, 1);
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(&accf[a], 1);
+            mbar_init(&acce[a], 8);  // one arrival per epilogue warp
+        }
         *fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -176,7 +195,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         int issued = 0;
         for (int kb = 0; kb < nkb; ++kb) {
             const int s = kb % TC_STAGES;
-            if (kb >= TC_STAGES && !mbar_wait(&empty[s], ((kb / TC_STAGES) - 1) & 1)) {
+            if (kb >= TC_STAGES && !mbar_wait(&empty[s], ((kb / TC_STAGES) - 1) & 1, fail)) {
                 atomicExch(fail, 1);
                 break;
             }
@@ -198,58 +217,88 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % TC_STAGES;
-            if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1)) {
-                atomicExch(fail, 2);
+        const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
+        for (int c = 0; c < nch; ++c) {
+            const int a = c & 1;
+            if (c >= 2 && !mbar_wait(&acce[a], ((c >> 1) - 1) & 1, fail)) {
+                atomicCAS(fail, 0, 4);
                 break;
             }
-            if (*(volatile int*)fail) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
-            const uint32_t a_hi = sa, a_lo = sa + A_TILE, b_hi = sa + 2 * A_TILE,
-                           b_lo = sa + 2 * A_TILE + B_TILE;
-#pragma unroll
-            for (int kk = 0; kk < TC_BK / TC_UMMA_K; ++kk) {
-                const uint32_t off = kk * TC_UMMA_K * 4;  // bytes along K inside the 128-B row
-                const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
-                umma_tf32(tmem, sdesc(a_lo + off), sdesc(b_hi + off), acc);
-                umma_tf32(tmem, sdesc(a_hi + off), sdesc(b_lo + off), 1u);
-                umma_tf32(tmem, sdesc(a_hi + off), sdesc(b_hi + off), 1u);
-            }
-            umma_commit(&empty[s]);
-        }
-        umma_commit(accum);
-    } else if (warp >= 2) {
-        // ---------------- epilogue: TMEM -> registers -> C
-        const bool ok = mbar_wait(accum, 0);
-        if (!ok) atomicExch(fail, 3);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int quarter = warp % 4;  // TMEM lanes 32*quarter .. +31
-        const int row = m0 + quarter * 32 + lane;
-        // warp-uniform decision: tcgen05.ld is a .sync.aligned warp instruction
-        const int drain = __shfl_sync(0xffffffffu, (ok && *(volatile int*)fail == 0) ? 1 : 0, 0);
-        if (drain && nkb > 0) {
-            for (int c0 = 0; c0 < TC_BN; c0 += 32) {
-                uint32_t r[32];
-                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, r);
-                if (row < M) {
-                    float* dst = C + (int64_t)row * ldc + n0 + c0;
-                    const int cols = min(32, N - (n0 + c0));
-                    if (cols == 32 && (ldc % 4) == 0) {
-#pragma unroll
-                        for (int v = 0; v < 8; ++v)
-                            reinterpret_cast<float4*>(dst)[v] =
-                                make_float4(__uint_as_float(r[4 * v]), __uint_as_float(r[4 * v + 1]),
-                                            __uint_as_float(r[4 * v + 2]),
-                                            __uint_as_float(r[4 * v + 3]));
-                    } else {
-                        for (int v = 0; v < cols; ++v) dst[v] = __uint_as_float(r[v]);
-                    }
+            const uint32_t tacc = tmem + (uint32_t)(a * TC_BN);
+            const int kb_end = min(nkb, (c + 1) * TC_FLUSH);
+            bool ok = true;
+            for (int kb = c * TC_FLUSH; kb < kb_end; ++kb) {
+                const int s = kb % TC_STAGES;
+                if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, fail)) {
+                    atomicCAS(fail, 0, 2);
+                    ok = false;
+                    break;
                 }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
+                const uint32_t a_hi = sa, a_lo = sa + A_TILE, b_hi = sa + 2 * A_TILE,
+                               b_lo = sa + 2 * A_TILE + B_TILE;
+#pragma unroll
+                for (int kk = 0; kk < TC_BK / TC_UMMA_K; ++kk) {
+                    const uint32_t off = kk * TC_UMMA_K * 4;  // bytes along K in the 128-B row
+                    const uint32_t acc = (kb > c * TC_FLUSH || kk > 0) ? 1u : 0u;
+                    umma_tf32(tacc, sdesc(a_lo + off), sdesc(b_hi + off), acc);
+                    umma_tf32(tacc, sdesc(a_hi + off), sdesc(b_lo + off), 1u);
+                    umma_tf32(tacc, sdesc(a_hi + off), sdesc(b_hi + off), 1u);
+                }
+                umma_commit(&empty[s]);
             }
-        } else if (nkb == 0 && row < M) {
-            for (int c = 0; c < TC_BN && n0 + c < N; ++c) C[(int64_t)row * ldc + n0 + c] = 0.f;
+            umma_commit(&accf[a]);
+            if (!ok) break;
+        }
+    } else if (warp >= 2) {
+        // ---------------- epilogue: drain chunks into float32 registers, then store C
+        const int quarter = warp % 4;          // TMEM lanes 32*quarter .. +31
+        const int half = (warp - 2) / 4;       // columns 128*half .. +127
+        const int row = m0 + quarter * 32 + lane;
+        const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
+        float tot[TC_BN / 2];
+#pragma unroll
+        for (int j = 0; j < TC_BN / 2; ++j) tot[j] = 0.f;
+        bool good = true;
+        for (int c = 0; c < nch; ++c) {
+            const int a = c & 1;
+            const bool ok = mbar_wait(&accf[a], (c >> 1) & 1, fail);
+            // warp-uniform decision: tcgen05.ld is a .sync.aligned warp instruction
+            const int drain = __shfl_sync(0xffffffffu, (ok && *(volatile int*)fail == 0) ? 1 : 0, 0);
+            if (!drain) {
+                if (lane == 0) atomicCAS(fail, 0, 3);
+                good = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) +
+                                   (uint32_t)(a * TC_BN + half * (TC_BN / 2));
+#pragma unroll
+            for (int j = 0; j < TC_BN / 2 / 32; ++j) {
+                uint32_t r[32];
+                tmem_ld32(tbase + (uint32_t)(j * 32), r);
+#pragma unroll
+                for (int v = 0; v < 32; ++v) tot[j * 32 + v] += __uint_as_float(r[v]);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[a]);
+        }
+        if (good && row < M) {
+            const int c0 = n0 + half * (TC_BN / 2);
+            float* dst = C + (int64_t)row * ldc + c0;
+            if (c0 + TC_BN / 2 <= N && (ldc % 4) == 0) {
+#pragma unroll
+                for (int v = 0; v < TC_BN / 2 / 4; ++v)
+                    reinterpret_cast<float4*>(dst)[v] =
+                        make_float4(tot[4 * v], tot[4 * v + 1], tot[4 * v + 2], tot[4 * v + 3]);
+            } else {
+#pragma unroll
+                for (int v = 0; v < TC_BN / 2; ++v)
+                    if (c0 + v < N) dst[v] = tot[v];
+            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -237,6 +237,28 @@ __device__ __forceinline__ double dpareto2(double x) {
     return -4.0 * (1.0 + x) / (den * den);
 }
 
+// float32 forms for the mixed path (the argument v = u / tau is formed in float64)
+__device__ __forceinline__ float softplus_f(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+__device__ __forceinline__ float softplus_grad_f(float x) {
+    if (x > 20.f) return 1.f;
+    const float z = expf(x);
+    return z / (z + 1.f);
+}
+// log_fatplus(u) = log(tau) + log(h(v)), d/du = h'(v) / (tau h(v)), v = u / tau
+__device__ __forceinline__ void log_fatplus_f(float v, float log_tau, float inv_tau, float& li,
+                                              float& dli) {
+    const float c = 1.f / (1.f + v * v);
+    const float h = softplus_f(v) + 0.1f * c;
+    const float hp = softplus_grad_f(v) - 0.2f * v * c * c;
+    li = log_tau + logf(h);
+    dli = hp * inv_tau / h;
+}
+__device__ __forceinline__ float pareto2_f(float x) { return 2.f / (2.f + 2.f * x + x * x); }
+__device__ __forceinline__ float dpareto2_f(float x) {
+    const float den = 2.f + 2.f * x + x * x;
+    return -4.f * (1.f + x) / (den * den);
+}
+
 // In-place Cholesky of a q x q row-major matrix (lower). Returns 0 or pivot+1.
 __device__ int chol_small(double* A, int q) {
     for (int j = 0; j < q; ++j) {
@@ -260,6 +282,11 @@ __device__ int chol_small(double* A, int q) {
 //                          t S | dY SC*q | scratch q*q
 constexpr int kSampleChunk = 128;
 
+// MIXED: the per-sample log_fatplus / fatmax (and their derivatives, kept in
+// shared memory for the reverse pass) are evaluated in float32 from the
+// float64 improvement u = Y - best_f; Y, the Cholesky, log-mean-exp and every
+// accumulation stay float64.
+template <bool MIXED>
 __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backward) {
     extern __shared__ double sm[];
     const int q = a.q, r = a.r, S = a.S, D = r + q;
@@ -273,6 +300,9 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     double* tS = dmu + q;
     double* dY = tS + S;
     double* scr = dY + kSampleChunk * q;
+    // MIXED + backward: float li and d li / du per (sample, point) after scr
+    float* Lf = reinterpret_cast<float*>(scr + (q * q > q * r ? q * q : q * r));
+    float* Df = Lf + S * q;
     __shared__ int s_status;
     __shared__ double s_red[4];
     __shared__ double s_lse;
@@ -348,11 +378,40 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     }
     const bool qei = (a.acqf == BGB_ACQF_QEI);
     const double tau = a.tau_relu, taum = a.tau_max;
+    const double inv_tau = 1.0 / tau;
+    const float log_tau = (float)log(tau);
+    const float inv_taum = (float)(1.0 / taum);
     // (5) forward over samples: t_s (per-sample reduced utility)
     int local_bad = 0;
     for (int s = tid; s < S; s += blockDim.x) {
         const double* z = a.Z + (int64_t)s * D;
         const double bf = qei ? a.best_f[0] : a.best_f[s];
+        if (MIXED && !qei) {
+            float lf[kMaxQ];
+            float Mf = -INFINITY;
+            for (int i = 0; i < q; ++i) {
+                double y = mu[i];
+                for (int k = 0; k < r + i + 1; ++k) y += Lq[i * D + k] * z[k];
+                if (!isfinite(y)) local_bad = 1;
+                float dl;
+                log_fatplus_f((float)((y - bf) * inv_tau), log_tau, (float)inv_tau, lf[i], dl);
+                if (backward) {
+                    Lf[s * q + i] = lf[i];
+                    Df[s * q + i] = dl;
+                }
+                Mf = fmaxf(Mf, lf[i]);
+            }
+            float t;
+            if (isinf(Mf)) {
+                t = Mf;
+            } else {
+                float P = 0.f;
+                for (int i = 0; i < q; ++i) P += pareto2_f((Mf - lf[i]) * inv_taum);
+                t = Mf + (float)taum * logf(P);
+            }
+            tS[s] = (double)t;
+            continue;
+        }
         double li[kMaxQ];
         double Mx = -INFINITY;
         for (int i = 0; i < q; ++i) {
@@ -436,6 +495,32 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
         const int sc = min(kSampleChunk, S - s0);
         for (int ls = tid; ls < sc; ls += blockDim.x) {
             const int s = s0 + ls;
+            if (MIXED && !qei) {
+                const float* lf = Lf + s * q;
+                const float* df = Df + s * q;
+                float Mf = -INFINITY;
+                for (int i = 0; i < q; ++i) Mf = fmaxf(Mf, lf[i]);
+                int nt = 0;
+                for (int i = 0; i < q; ++i) nt += (lf[i] == Mf);
+                const double ws = isinf(mx) ? (tS[s] == mx ? 1.0 : 0.0) : exp(tS[s] - lse);
+                if (isinf(Mf)) {
+                    for (int i = 0; i < q; ++i) dY[ls * q + i] = (lf[i] == Mf) ? ws : 0.0;
+                } else {
+                    float P = 0.f, Pd = 0.f;
+                    for (int i = 0; i < q; ++i) {
+                        const float x = (Mf - lf[i]) * inv_taum;
+                        P += pareto2_f(x);
+                        Pd += dpareto2_f(x);
+                    }
+                    const float top = (1.f + Pd / P) / (float)nt;
+                    for (int i = 0; i < q; ++i) {
+                        const float x = (Mf - lf[i]) * inv_taum;
+                        const float dt = -dpareto2_f(x) / P + (lf[i] == Mf ? top : 0.f);
+                        dY[ls * q + i] = ws * (double)(dt * df[i]);
+                    }
+                }
+                continue;
+            }
             const double* z = a.Z + (int64_t)s * D;
             const double bf = qei ? a.best_f[0] : a.best_f[s];
             double u[kMaxQ], li[kMaxQ], g[kMaxQ];
@@ -545,32 +630,38 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
 
 // ---------------------------------------------------------------- mix_rows
 // H[row i of t-batch] = gmu_i beta - 2 sum_j Gqq[i,j] V[j,:] - sum_k Gqb[i,k] Vb[k,:]
-// (d value / d V through mu = V beta, Sigma_qq and Sigma_qb)
-template <typename T>
+// (d value / d V through mu = V beta, Sigma_qq and Sigma_qb). One thread per
+// column of one t-batch; QM >= q bounds the register arrays.
+template <typename T, int QM>
 __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __restrict__ V,
                                                        int64_t ldv, const T* __restrict__ Vb,
                                                        const T* __restrict__ beta,
                                                        T* __restrict__ H, T* __restrict__ H_lo,
                                                        int64_t ldh) {
-    extern __shared__ double gs[];  // q*q + q*r + q seeds
+    extern __shared__ __align__(16) unsigned char gsraw[];  // q*q + q*r + q seeds (as T)
+    T* gq = reinterpret_cast<T*>(gsraw);
     const int q = a.q, r = a.r;
     const int64_t n = a.n, bidx = blockIdx.y, rbase = bidx * q;
-    double* gq = gs;
-    double* gqb = gs + q * q;
-    double* gm = gqb + q * r;
-    for (int p = threadIdx.x; p < q * q; p += blockDim.x) gq[p] = a.gqq[bidx * q * q + p];
-    for (int p = threadIdx.x; p < q * r; p += blockDim.x) gqb[p] = a.gqb[bidx * q * r + p];
-    for (int p = threadIdx.x; p < q; p += blockDim.x) gm[p] = a.gmu[bidx * q + p];
+    T* gqb = gq + q * q;
+    T* gm = gqb + q * r;
+    for (int p = threadIdx.x; p < q * q; p += blockDim.x) gq[p] = (T)(-2.0 * a.gqq[bidx * q * q + p]);
+    for (int p = threadIdx.x; p < q * r; p += blockDim.x) gqb[p] = (T)(-a.gqb[bidx * q * r + p]);
+    for (int p = threadIdx.x; p < q; p += blockDim.x) gm[p] = (T)a.gmu[bidx * q + p];
     __syncthreads();
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    T v[kMaxQ];
-    for (int j = 0; j < q; ++j) v[j] = V[(rbase + j) * ldv + c];
+    T v[QM];
+#pragma unroll
+    for (int j = 0; j < QM; ++j) v[j] = (j < q) ? V[(rbase + j) * ldv + c] : T(0);
     const T bc = beta[c];
-    for (int i = 0; i < q; ++i) {
-        T h = (T)gm[i] * bc;
-        for (int j = 0; j < q; ++j) h -= T(2) * (T)gq[i * q + j] * v[j];
-        for (int k = 0; k < r; ++k) h -= (T)gqb[i * r + k] * Vb[(int64_t)k * n + c];
+#pragma unroll
+    for (int i = 0; i < QM; ++i) {
+        if (i >= q) break;
+        T h = gm[i] * bc;
+#pragma unroll
+        for (int j = 0; j < QM; ++j)
+            if (j < q) h = fma(gq[i * q + j], v[j], h);
+        for (int k = 0; k < r; ++k) h = fma(gqb[i * r + k], Vb[(int64_t)k * n + c], h);
         if constexpr (sizeof(T) == 4) {
             if (H_lo != nullptr) {  // tf32 split for the tensor-core adjoint GEMM
                 uint32_t hb, lb;
@@ -587,94 +678,91 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
 }
 
 // ---------------------------------------------------------------- adjoint
+// d value / d X: one thread per row of X (64 rows per CTA). Per chunk of 64
+// training points the CTA stages, in shared memory, the D tile of its rows
+// (coalesced row segments) and the k-major scaled training inputs XsT (read
+// by all threads as broadcasts); each thread then sweeps the chunk with its
+// row's scaled coordinates and gradient accumulator in registers:
+//   g += D[i,c] kappa'(r2_ic) (z_i - zt_c),   r2_ic = |z_i - zt_c|^2.
+constexpr int kAdjRows = 64;
 constexpr int kAdjChunk = 64;
 
 template <typename T, int DMAX>
-__global__ void __launch_bounds__(256) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
-                                                      int64_t ldd) {
-    // smem: D chunk [q][CH] (T), scaled Xt chunk [CH][d] (T)
+__global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
+                                                           int64_t ldd, const T* __restrict__ XsT) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int q = a.q, r = a.r, d = a.d;
-    const int64_t n = a.n;
-    const int64_t bidx = blockIdx.x;
-    const int64_t rbase = bidx * q;
-    T* Dc = reinterpret_cast<T*>(smraw);
-    T* Xc = Dc + q * kAdjChunk;
-    double* gq = reinterpret_cast<double*>(Xc + kAdjChunk * d + 8);  // q*q + q*r + q seeds
-    double* gqb = gq + q * q;
-    double* gmu = gqb + q * r;
-    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32, nwarps = blockDim.x / 32;
-    for (int p = threadIdx.x; p < q * q; p += blockDim.x) gq[p] = a.gqq[bidx * q * q + p];
-    for (int p = threadIdx.x; p < q * r; p += blockDim.x) gqb[p] = a.gqb[bidx * q * r + p];
-    for (int p = threadIdx.x; p < q; p += blockDim.x) gmu[p] = a.gmu[bidx * q + p];
-    if (threadIdx.x == 0 && a.dev_err != nullptr && *a.dev_err != 0) a.status[bidx] = BGB_DEVICE_TIMEOUT;
-    const T os = (T)a.outputscale;
-    for (int i0 = 0; i0 < q; i0 += nwarps) {
-        const int i = i0 + warp;
-        const bool active = i < q;
-        T zx[DMAX], g[DMAX];
+    T* Xc = reinterpret_cast<T*>(smraw);              // [d][kAdjChunk]
+    T* Dc = Xc + (size_t)a.d * kAdjChunk;             // [kAdjRows][kAdjChunk + 1]
+    constexpr int LDD = kAdjChunk + 1;
+    const int q = a.q, r = a.r, d = a.d, kind = a.kernel;
+    const int64_t n = a.n, rows = a.b * a.q;
+    const int tid = threadIdx.x;
+    const int64_t row0 = (int64_t)blockIdx.x * kAdjRows;
+    const int64_t row = row0 + tid;
+    const bool active = row < rows;
+    T zx[DMAX], g[DMAX];
 #pragma unroll
-        for (int k = 0; k < DMAX; ++k) {
-            zx[k] = (active && k < d) ? (T)(a.X[(rbase + i) * d + k] * a.inv_ls[k]) : T(0);
-            g[k] = T(0);
+    for (int k = 0; k < DMAX; ++k) {
+        zx[k] = (active && k < d) ? (T)(a.X[row * d + k] * a.inv_ls[k]) : T(0);
+        g[k] = T(0);
+    }
+    for (int64_t c0 = 0; c0 < n; c0 += kAdjChunk) {
+        const int cc = (int)((n - c0) < kAdjChunk ? (n - c0) : kAdjChunk);
+        __syncthreads();
+        for (int p = tid; p < kAdjRows * kAdjChunk; p += kAdjRows) {
+            const int rr = p / kAdjChunk, c = p % kAdjChunk;
+            Dc[rr * LDD + c] = (row0 + rr < rows && c < cc) ? Dm[(row0 + rr) * ldd + c0 + c] : T(0);
         }
-        for (int64_t c0 = 0; c0 < n; c0 += kAdjChunk) {
-            const int cc = (int)((n - c0) < kAdjChunk ? (n - c0) : kAdjChunk);
-            __syncthreads();
-            for (int p = threadIdx.x; p < q * kAdjChunk; p += blockDim.x) {
-                int j = p / kAdjChunk, c = p % kAdjChunk;
-                Dc[p] = (c < cc) ? Dm[(rbase + j) * ldd + c0 + c] : T(0);
-            }
-            for (int p = threadIdx.x; p < kAdjChunk * d; p += blockDim.x) {
-                int c = p / d, k = p % d;
-                Xc[p] = (c < cc) ? (T)(a.Xt[(c0 + c) * d + k] * a.inv_ls[k]) : T(0);
-            }
-            __syncthreads();
-            if (!active) continue;
-            for (int c = lane; c < cc; c += 32) {
-                // dKc[i, c] = D[i, c] = (d value / d V  L^-1)[i, c]
-                const T dk = Dc[i * kAdjChunk + c];
-                T r2 = T(0);
-                T df[DMAX];
-#pragma unroll
-                for (int k = 0; k < DMAX; ++k) {
-                    df[k] = (k < d) ? zx[k] - Xc[c * d + k] : T(0);
-                    r2 += df[k] * df[k];
-                }
-                const T coef = dk * dkappa_dr2<T>(a.kernel, r2);
-#pragma unroll
-                for (int k = 0; k < DMAX; ++k) g[k] += coef * df[k];
-            }
+        for (int p = tid; p < d * kAdjChunk; p += kAdjRows) {
+            const int k = p / kAdjChunk, c = p % kAdjChunk;
+            Xc[k * kAdjChunk + c] = (c < cc) ? XsT[(int64_t)k * n + c0 + c] : T(0);
         }
-        if (active) {
-            // K(X, X) and K(X, Xb) terms, float64
-            double gx[DMAX];
+        __syncthreads();
+        for (int c = 0; c < cc; ++c) {
+            const T dk = Dc[tid * LDD + c];
+            T df[DMAX];
+            T r2a = T(0), r2b = T(0);
 #pragma unroll
-            for (int k = 0; k < DMAX; ++k) gx[k] = (double)g[k];
-            for (int j = lane; j < q + r; j += 32) {
-                const double* y = (j < q) ? a.X + (rbase + j) * d : a.Xb + (int64_t)(j - q) * d;
-                const double w = (j < q) ? 2.0 * gq[i * q + j] : gqb[i * r + (j - q)];
-                double dfx[DMAX];
-                double r2 = 0.0;
-#pragma unroll
-                for (int k = 0; k < DMAX; ++k) {
-                    dfx[k] = (k < d) ? (a.X[(rbase + i) * d + k] - y[k]) * a.inv_ls[k] : 0.0;
-                    r2 += dfx[k] * dfx[k];
+            for (int k = 0; k < DMAX; k += 2) {
+                df[k] = (k < d) ? zx[k] - Xc[k * kAdjChunk + c] : T(0);
+                r2a = fma(df[k], df[k], r2a);
+                if (k + 1 < DMAX) {
+                    df[k + 1] = (k + 1 < d) ? zx[k + 1] - Xc[(k + 1) * kAdjChunk + c] : T(0);
+                    r2b = fma(df[k + 1], df[k + 1], r2b);
                 }
-                const double coef = w * dkappa_dr2<double>(a.kernel, r2);
-#pragma unroll
-                for (int k = 0; k < DMAX; ++k) gx[k] += coef * dfx[k];
             }
+            const T coef = dk * dkappa_dr2<T>(kind, r2a + r2b);
 #pragma unroll
-            for (int k = 0; k < DMAX; ++k) {
-                double v = gx[k];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                if (lane == 0 && k < d)
-                    a.grad[(rbase + i) * d + k] = 2.0 * (double)os * a.inv_ls[k] * v;
-            }
+            for (int k = 0; k < DMAX; ++k) g[k] = fma(coef, df[k], g[k]);
         }
     }
+    if (!active) return;
+    const int64_t bidx = row / q;
+    const int i = (int)(row % q);
+    if (a.dev_err != nullptr && *a.dev_err != 0 && i == 0) a.status[bidx] = BGB_DEVICE_TIMEOUT;
+    // K(X, X) and K(X, Xb) terms, float64
+    double gx[DMAX];
+#pragma unroll
+    for (int k = 0; k < DMAX; ++k) gx[k] = (double)g[k];
+    const int64_t rbase = bidx * q;
+    for (int j = 0; j < q + r; ++j) {
+        if (j == i) continue;
+        const double* y = (j < q) ? a.X + (rbase + j) * d : a.Xb + (int64_t)(j - q) * d;
+        const double w = (j < q) ? 2.0 * a.gqq[(bidx * q + i) * q + j] : a.gqb[(bidx * q + i) * r + (j - q)];
+        double dfx[DMAX];
+        double r2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k) {
+            dfx[k] = (k < d) ? (a.X[row * d + k] - y[k]) * a.inv_ls[k] : 0.0;
+            r2 += dfx[k] * dfx[k];
+        }
+        const double coef = w * dkappa_dr2<double>(kind, r2);
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k) gx[k] += coef * dfx[k];
+    }
+#pragma unroll
+    for (int k = 0; k < DMAX; ++k)
+        if (k < d) a.grad[row * d + k] = 2.0 * a.outputscale * a.inv_ls[k] * gx[k];
 }
 
 __global__ void posterior_out_kernel(QBatchArgs a, double* mean, double* covar) {
@@ -701,21 +789,31 @@ int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc
     return BGB_OK;
 }
 
-size_t batch_step_smem_bytes(int q, int r, int S) {
+size_t batch_step_smem_bytes(int q, int r, int S, bool mixed_backward) {
     const int D = r + q;
-    return sizeof(double) * (size_t)(2 * q * D + 3 * q * q + 2 * q + S + kSampleChunk * q +
-                                     (q * r > q * q ? q * r : 0));
+    size_t bytes = sizeof(double) * (size_t)(2 * q * D + 2 * q * q + 2 * q + S + kSampleChunk * q +
+                                             (q * q > q * r ? q * q : q * r));
+    if (mixed_backward) bytes += 2 * sizeof(float) * (size_t)S * q;
+    return bytes;
 }
 
-int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream) {
+int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bool mixed) {
     if (a.b <= 0) return BGB_OK;
     if (a.q > kMaxQ) return BGB_ERR_UNSUPPORTED;
-    size_t smem = batch_step_smem_bytes(a.q, a.r, a.S);
+    const bool mb = mixed && backward && a.acqf != BGB_ACQF_QEI;
+    size_t smem = batch_step_smem_bytes(a.q, a.r, a.S, mb);
     if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
-    if (smem > 48 * 1024)
-        BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    batch_step_kernel<<<(unsigned)a.b, 128, smem, stream>>>(a, backward);
+    if (mixed) {
+        if (smem > 48 * 1024)
+            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_kernel<true>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        batch_step_kernel<true><<<(unsigned)a.b, 128, smem, stream>>>(a, backward);
+    } else {
+        if (smem > 48 * 1024)
+            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_kernel<false>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        batch_step_kernel<false><<<(unsigned)a.b, 128, smem, stream>>>(a, backward);
+    }
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
@@ -735,36 +833,41 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
                     cudaStream_t stream, T* H_lo, int64_t ldh) {
     if (a.b <= 0) return BGB_OK;
     if (a.q > kMaxQ) return BGB_ERR_UNSUPPORTED;
-    const size_t smem = sizeof(double) * (size_t)(a.q * a.q + a.q * a.r + a.q);
+    const size_t smem = sizeof(T) * (size_t)(a.q * a.q + a.q * a.r + a.q);
     if (smem > 48 * 1024) return BGB_ERR_UNSUPPORTED;
     dim3 grid((unsigned)ceil_div(a.n, 256), (unsigned)a.b);
-    mix_rows_kernel<T><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ldh > 0 ? ldh : a.n);
+    const int64_t ld = ldh > 0 ? ldh : a.n;
+    if (a.q <= 4) mix_rows_kernel<T, 4><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld);
+    else if (a.q <= 8) mix_rows_kernel<T, 8><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld);
+    else if (a.q <= 16) mix_rows_kernel<T, 16><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld);
+    else mix_rows_kernel<T, 32><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
 
 template <typename T>
-size_t adjoint_smem_bytes(int q, int r, int d) {
-    return sizeof(T) * (size_t)(q * kAdjChunk + kAdjChunk * d + 8) +
-           sizeof(double) * (size_t)(q * q + q * r + q) + 16;
+size_t adjoint_smem_bytes(int d) {
+    return sizeof(T) * ((size_t)d * kAdjChunk + (size_t)kAdjRows * (kAdjChunk + 1));
 }
 
 template <typename T>
-int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, cudaStream_t stream) {
-    if (a.b <= 0) return BGB_OK;
-    size_t smem = adjoint_smem_bytes<T>(a.q, a.r, a.d);
+int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, cudaStream_t stream) {
+    const int64_t rows = a.b * a.q;
+    if (rows <= 0) return BGB_OK;
+    const size_t smem = adjoint_smem_bytes<T>(a.d);
     if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
-    const unsigned grid = (unsigned)a.b;
+    const unsigned grid = (unsigned)ceil_div(rows, kAdjRows);
 #define BGB_ADJ(DM)                                                                              \
     do {                                                                                        \
         if (smem > 48 * 1024)                                                                   \
             BGB_CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel<T, DM>,                            \
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                               (int)smem));                                      \
-        adjoint_kernel<T, DM><<<grid, 256, smem, stream>>>(a, D, ldd);                          \
+        adjoint_kernel<T, DM><<<grid, kAdjRows, smem, stream>>>(a, D, ldd, XsT);                \
     } while (0)
     if (a.d <= 8) BGB_ADJ(8);
     else if (a.d <= 16) BGB_ADJ(16);
+    else if (a.d <= 24) BGB_ADJ(24);
     else if (a.d <= 32) BGB_ADJ(32);
     else if (a.d <= 64) BGB_ADJ(64);
     else return BGB_ERR_UNSUPPORTED;
@@ -793,7 +896,9 @@ template int launch_mix_rows<double>(const QBatchArgs&, const double*, int64_t, 
                                      const double*, double*, cudaStream_t, double*, int64_t);
 template int launch_mix_rows<float>(const QBatchArgs&, const float*, int64_t, const float*,
                                     const float*, float*, cudaStream_t, float*, int64_t);
-template int launch_adjoint<double>(const QBatchArgs&, const double*, int64_t, cudaStream_t);
-template int launch_adjoint<float>(const QBatchArgs&, const float*, int64_t, cudaStream_t);
+template int launch_adjoint<double>(const QBatchArgs&, const double*, int64_t, const double*,
+                                    cudaStream_t);
+template int launch_adjoint<float>(const QBatchArgs&, const float*, int64_t, const float*,
+                                   cudaStream_t);
 
 }  // namespace bgb

@@ -165,10 +165,10 @@ class SingleTaskGP:
     def operands(self, precision: str):
         """Model-level operands of the C ABI, built once per precision.
 
-        Returns (B64, B32, ldb, Linv32, beta32, tc) with B = L^-T, float32
-        copies of L^-1 and beta, and for the mixed path ``tc`` = (Lhi, Llo,
+        Returns (B64, B32, ldb, Linv32, beta32, tc, Xs64, Xs32) with B = L^-T,
+        float32 copies of L^-1 and beta, for the mixed path ``tc`` = (Lhi, Llo,
         LThi, LTlo, ldl): the tf32 hi/lo split of L^-1 and L^-T used by the
-        tensor-core GEMMs.
+        tensor-core GEMMs, and the training inputs scaled by 1 / lengthscale.
         """
         if precision in self._operands:
             return self._operands[precision]
@@ -181,11 +181,13 @@ class SingleTaskGP:
         B32 = torch.empty(n, ldb, dtype=torch.float32, device=dev) if mixed else None
         L32 = torch.empty(n, n, dtype=torch.float32, device=dev) if mixed else None
         b32 = torch.empty(n, dtype=torch.float32, device=dev) if mixed else None
+        Xs64 = torch.empty(self.d, n, dtype=torch.float64, device=dev)
+        Xs32 = torch.empty(self.d, n, dtype=torch.float32, device=dev) if mixed else None
         gp = self.gp_struct()
         with torch.cuda.device(dev):
             rc = lib.bgb_gp_operands(ctypes.byref(gp), nat.ptr(self.Linv), nat.ptr(self.beta),
                                      nat.ptr(B64), nat.ptr(B32), ldb, nat.ptr(L32), nat.ptr(b32),
-                                     nat.stream_handle(dev))
+                                     nat.ptr(Xs64), nat.ptr(Xs32), nat.stream_handle(dev))
             nat.check(rc, "model operands")
             tc = None
             if mixed:
@@ -193,15 +195,16 @@ class SingleTaskGP:
                 rc = lib.bgb_gp_tc_operands(ctypes.byref(gp), nat.ptr(self.Linv), ldb,
                                             *(nat.ptr(t) for t in tc[:4]), nat.stream_handle(dev))
                 nat.check(rc, "tensor-core operands")
-        self._operands[precision] = (B64, B32, ldb, L32, b32, tc)
+        self._operands[precision] = (B64, B32, ldb, L32, b32, tc, Xs64, Xs32)
         return self._operands[precision]
 
     def acq_struct_base(self, precision: str, tensor_cores: bool = True) -> dict:
         """Keyword arguments of BgbAcq shared by every acquisition call on this model."""
-        B64, B32, ldb, L32, b32, tc = self.operands(precision)
+        B64, B32, ldb, L32, b32, tc, Xs64, Xs32 = self.operands(precision)
         kw = dict(gp=self.gp_struct(), precision=nat.PRECISIONS[precision], ldb=ldb,
                   B64=nat.ptr(B64), B32=nat.ptr(B32), Linv64=nat.ptr(self.Linv),
-                  Linv32=nat.ptr(L32), beta64=nat.ptr(self.beta), beta32=nat.ptr(b32))
+                  Linv32=nat.ptr(L32), beta64=nat.ptr(self.beta), beta32=nat.ptr(b32),
+                  Xs64=nat.ptr(Xs64), Xs32=nat.ptr(Xs32))
         if tc is not None:
             kw.update(Lhi=nat.ptr(tc[0]), Llo=nat.ptr(tc[1]), LThi=nat.ptr(tc[2]),
                       LTlo=nat.ptr(tc[3]), ldl=tc[4])

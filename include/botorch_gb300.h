@@ -97,6 +97,8 @@ typedef struct bgb_acq {
     const float* VbT32;
     const double* beta64;
     const float* beta32;
+    const double* Xs64;      /* d x n (k-major): training inputs / lengthscale (adjoint) */
+    const float* Xs32;
     /* tensor-core operands of MIXED (tf32 hi/lo, n x ldl, ldl >= n, ldl % 8 == 0):
      * L^-1 for the forward GEMM and L^-T for the adjoint GEMM; NULL: FFMA GEMM */
     const float* Lhi;
@@ -158,9 +160,12 @@ int bgb_gp_fit(const bgb_gp_t* gp, const double* y, double noise, int32_t max_tr
 size_t bgb_gp_fit_workspace_bytes(int64_t n);
 
 /* (c) Model-level operands: B = Linv^T (n x ldb, ldb >= n) in float64 and
- * float32 (B32 may be NULL), and float32 copies of Linv and beta (may be NULL). */
+ * float32 (B32 may be NULL), float32 copies of Linv and beta (may be NULL), and
+ * the training inputs scaled by 1 / lengthscale, Xs (d x n, k-major) in
+ * float64 and float32 (Xs32 may be NULL). */
 int bgb_gp_operands(const bgb_gp_t* gp, const double* Linv, const double* beta, double* B64,
-                    float* B32, int64_t ldb, float* Linv32, float* beta32, void* stream);
+                    float* B32, int64_t ldb, float* Linv32, float* beta32, double* Xs64,
+                    float* Xs32, void* stream);
 
 /* (c) Tensor-core operands of the mixed path: the tf32 hi/lo split of L^-1
  * (Lhi, Llo) and of L^-T (LThi, LTlo), n x ldl each (ldl >= n, ldl % 8 == 0). */

@@ -57,23 +57,30 @@ def test_tc_gemm_matches_float64(cuda_lib, M, N, K, kmode):
     assert float((out - ref).norm() / ref.norm()) < 5e-6
 
 
-def test_mixed_tensor_core_and_ffma_paths_agree(cuda_lib):
+def test_mixed_tensor_core_and_ffma_paths_against_fp64(cuda_lib):
+    """Both float32 GEMM forms of the mixed path against the float64 GPU path on a
+    Branin-sum workload (n=1024, d=20, q=8, y_std ~ 160). Values hold 2e-5; the
+    gradient is dominated by t-batches within ~100 tau_relu of the incumbent
+    (see test_qlognei_differentiation_config), so its bound is 1e-2."""
     from botorch_gb300 import testing as T
     from tests.test_gpu_parity import gpu_model
     from botorch_gb300 import SobolQMCNormalSampler, qLogNoisyExpectedImprovement
 
     w = T.qlognei_branin(n=1024, b=256, q=8, d=20)
     gm = gpu_model(w)
-    vals = {}
-    for tc in (True, False):
+    out = {}
+    for name, precision, tc in (("fp64", "fp64", False), ("tc", "mixed", True), ("ffma", "mixed", False)):
         torch.manual_seed(0)
         a = qLogNoisyExpectedImprovement(gm, w.train_X, sampler=SobolQMCNormalSampler(
-            torch.Size([512]), seed=0), precision="mixed")
+            torch.Size([512]), seed=0), precision=precision)
         a.use_tensor_cores = tc
         X = w.X.to(DEV).requires_grad_(True)
         v = a(X)
         v.sum().backward()
-        vals[tc] = (v.detach().cpu(), X.grad.cpu())
-    (v1, g1), (v0, g0) = vals[True], vals[False]
-    assert float((v1 - v0).norm() / v0.norm()) < 1e-5
-    assert float((g1 - g0).norm() / g0.norm()) < 1e-3
+        out[name] = (v.detach().cpu(), X.grad.cpu())
+    v64, g64 = out["fp64"]
+    for name in ("tc", "ffma"):
+        v, g = out[name]
+        ev = float((v - v64).norm() / v64.norm())
+        eg = float((g - g64).norm() / g64.norm())
+        assert ev < 2e-5 and eg < 1e-2, (name, ev, eg)
