@@ -23,6 +23,8 @@ BGB_ERR_ARG = -1
 BGB_ERR_WORKSPACE = -2
 BGB_ERR_CUDA = -3
 BGB_ERR_UNSUPPORTED = -4
+BGB_ERR_SCRATCH_LIMIT = -5
+BGB_NOALLOC_SCRATCH_BYTES = 32 << 20   # fixed scratch of bgb_acq_forward_backward_noalloc
 
 KERNELS = {"matern52": 0, "matern32": 1, "matern12": 2, "rbf": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1}
@@ -102,6 +104,8 @@ _SIGNATURES = {
     "bgb_acq_forward_backward_timed": (c_i32, [ctypes.POINTER(BgbAcq), c_vp, c_i64, c_vp, c_vp,
                                                c_vp, c_vp, c_size, ctypes.POINTER(ctypes.c_float),
                                                c_vp]),
+    "bgb_acq_forward_backward_noalloc": (c_i32, [ctypes.POINTER(BgbAcq), c_vp, c_i64, c_vp, c_vp,
+                                                 c_vp, c_vp]),
     "bgb_launch_count": (ctypes.c_ulonglong, []),
 }
 
@@ -154,7 +158,8 @@ def check(rc: int, what: str) -> None:
     if rc == BGB_NAN:
         raise NanError(f"{what}: NaN encountered")
     names = {BGB_ERR_ARG: "invalid argument", BGB_ERR_WORKSPACE: "workspace too small",
-             BGB_ERR_CUDA: "CUDA error", BGB_ERR_UNSUPPORTED: "unsupported size"}
+             BGB_ERR_CUDA: "CUDA error", BGB_ERR_UNSUPPORTED: "unsupported size",
+             BGB_ERR_SCRATCH_LIMIT: "needs more than the fixed no-allocation scratch"}
     raise RuntimeError(f"{what}: {names.get(rc, rc)} (code {rc})")
 
 

@@ -3,6 +3,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <mutex>
 
 #include "bgb_common.cuh"
 #include "bgb_kernels.cuh"
@@ -14,6 +15,11 @@ namespace bgb {
 static std::atomic<unsigned long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 }  // namespace bgb
+
+// Scratch of bgb_acq_forward_backward_noalloc: one fixed array per device,
+// shared by every call of that entry point on the device. Part of the module's
+// static device memory, so using it allocates nothing at call time.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[BGB_NOALLOC_SCRATCH_BYTES];
 
 namespace {
 
@@ -294,6 +300,27 @@ int acq_call(const bgb_acq_t* a, const double* X, int64_t b, double* value, doub
                             static_cast<double*>(P), grad != nullptr, st, ev);
 }
 
+// Device address of g_noalloc_scratch on the current device, looked up once per
+// device (cudaGetSymbolAddress with that device current) and cached.
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+int noalloc_scratch(void** out) {
+    int dev = -1;
+    BGB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return BGB_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr)
+            return BGB_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return BGB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -556,6 +583,24 @@ int bgb_acq_forward_backward(const bgb_acq_t* acq, const double* X, int64_t b, d
                              size_t workspace_bytes, void* stream) {
     if (grad == nullptr) return BGB_ERR_ARG;
     return acq_call(acq, X, b, value, grad, status, workspace, workspace_bytes,
+                    as_stream(stream));
+}
+
+int bgb_acq_forward_backward_noalloc(const bgb_acq_t* acq, const double* X, int64_t b,
+                                     double* value, double* grad, int32_t* status, void* stream) {
+    if (!valid_acq(acq) || X == nullptr || value == nullptr || grad == nullptr ||
+        status == nullptr || b < 0)
+        return BGB_ERR_ARG;
+    if (b == 0) return BGB_OK;
+    // size check first: an oversized call launches nothing and touches no device
+    if (acq_ws_layout(acq, b, nullptr, nullptr, nullptr, nullptr, nullptr) >
+        BGB_NOALLOC_SCRATCH_BYTES)
+        return BGB_ERR_SCRATCH_LIMIT;
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    // acq_call clears the device error word on `stream` before its first launch
+    return acq_call(acq, X, b, value, grad, status, scratch, BGB_NOALLOC_SCRATCH_BYTES,
                     as_stream(stream));
 }
 

@@ -33,6 +33,7 @@ extern "C" {
 #define BGB_ERR_WORKSPACE (-2) /* workspace smaller than the *_bytes query */
 #define BGB_ERR_CUDA (-3)      /* a CUDA launch or runtime call failed */
 #define BGB_ERR_UNSUPPORTED (-4)
+#define BGB_ERR_SCRATCH_LIMIT (-5) /* call needs more than BGB_NOALLOC_SCRATCH_BYTES of scratch */
 
 /* Stationary kernels (gpytorch ScaleKernel over MaternKernel(nu) / RBFKernel, ARD). */
 #define BGB_KERNEL_MATERN52 0
@@ -256,6 +257,38 @@ int bgb_acq_forward_backward(const bgb_acq_t* acq, const double* X, int64_t b, d
 int bgb_acq_forward_backward_timed(const bgb_acq_t* acq, const double* X, int64_t b,
                                    double* value, double* grad, int32_t* status, void* workspace,
                                    size_t workspace_bytes, float* stage_ms_host, void* stream);
+
+/* ---- No-allocation variant. No counterpart in the reference: there, PyTorch's
+ * caching allocator always supplies the scratch memory.
+ *
+ * Computes what bgb_acq_forward_backward computes, but takes no workspace. Its
+ * scratch is one fixed array of BGB_NOALLOC_SCRATCH_BYTES (32 MiB) that the
+ * library keeps in device memory. The call itself allocates and frees nothing,
+ * on the device or the host. It is for callers that cannot allocate at the
+ * point of the call:
+ *   - C, C++ or FFI hosts without a device allocator of their own (no PyTorch);
+ *   - services that fix their device memory at start-up and must not grow it
+ *     inside an optimisation loop;
+ *   - latency-bound loops, where cudaMalloc / cudaFree may synchronise the
+ *     device and stall work queued on other streams.
+ * Limits:
+ *   - The array holds about 48 KB per candidate point at n = 4096 in the mixed
+ *     tensor-core form (b * q up to ~680 at n = 4096, ~2700 at n = 1024). A call
+ *     that needs more (bgb_acq_workspace_bytes(acq, b) > BGB_NOALLOC_SCRATCH_BYTES)
+ *     returns BGB_ERR_SCRATCH_LIMIT and launches nothing. Split the t-batches
+ *     over several calls instead.
+ *   - The first call on each device looks up the array's address on that device
+ *     (with that device current), which may load the library's device code
+ *     there. Make that first call before any stream capture on the device.
+ *   - All calls on a device share the one array. Calls that overlap on the GPU
+ *     (two streams, or two host threads with their own streams) race and
+ *     corrupt each other's results: issue them on one stream, or serialise them.
+ *   - Each call clears, on its own stream, the one part of the array that must
+ *     start at zero (the device error word); nothing else is read before it is
+ *     written. */
+#define BGB_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
+int bgb_acq_forward_backward_noalloc(const bgb_acq_t* acq, const double* X, int64_t b,
+                                     double* value, double* grad, int32_t* status, void* stream);
 
 /* Number of kernel launches this library has issued in the process so far.
  * Measurement aid; no reference counterpart. */
