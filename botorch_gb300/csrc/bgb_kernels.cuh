@@ -13,6 +13,12 @@ int launch_kernel_matrix(const TIn* X1, int64_t m, const TIn* X2, int64_t n2, in
                          const double* inv_ls, double outputscale, int kind, double diag_add,
                          int same, TOut* K, int64_t ldk, cudaStream_t stream,
                          TOut* K_lo = nullptr);
+// Float32 form over coordinates already scaled by 1 / lengthscale, both k-major
+// (Z1T: d x m with leading dimension ldz1, Z2T: d x n2 with ldz2). Same tile
+// arithmetic as the float instantiation above, without rescaling per tile.
+int launch_kernel_matrix_zt(const float* Z1T, int64_t ldz1, int64_t m, const float* Z2T,
+                            int64_t ldz2, int64_t n2, int d, double outputscale, int kind,
+                            float* K, int64_t ldk, cudaStream_t stream, float* K_lo = nullptr);
 
 // dense_f64.cu ------------------------------------------------------------
 // k-range modes of the GEMMs (structure of triangular operands):

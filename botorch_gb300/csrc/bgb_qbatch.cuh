@@ -37,8 +37,14 @@ struct QBatchArgs {
     double* grad;           // b x q x d
     int32_t* status;        // b
     const int* dev_err;     // non-zero: a bounded wait in a tensor-core GEMM expired
+    float* zt;              // mixed: candidates scaled by 1 / lengthscale, d x (b*q), k-major
 };
 
+// mu, Sigma_qq and Sigma_qb in one pass over V (q <= 8, r <= 4); returns
+// BGB_ERR_UNSUPPORTED (nothing launched) outside those sizes.
+template <typename T>
+int launch_qstats(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb,
+                  cudaStream_t stream);
 // mu (into a.mu) = m + V beta and P (b*q x r) = V Vb^T
 template <typename T>
 int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb, T* P,
@@ -55,9 +61,12 @@ size_t batch_step_smem_bytes(int q, int r, int S, bool mixed_backward);
 template <typename T>
 int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, const T* beta, T* H,
                     cudaStream_t stream, T* H_lo = nullptr, int64_t ldh = 0);
-// d value / d X from D (b*q x n) = H L^-1; Xs: training inputs scaled by 1 / lengthscale (n x d)
+// d value / d X from D (b*q x n) = H L^-1; XsT: training inputs scaled by 1 / lengthscale,
+// d x n (k-major). part: scratch of part_cap elements for per-slab partial
+// gradients (nullptr / 0: a single slab, no finalize pass).
 template <typename T>
-int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* Xs, cudaStream_t stream);
+int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T* part,
+                   int64_t part_cap, cudaStream_t stream);
 int launch_posterior_out(const QBatchArgs& a, double* mean, double* covar, cudaStream_t stream);
 
 }  // namespace bgb

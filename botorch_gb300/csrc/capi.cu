@@ -28,6 +28,17 @@ __global__ void sub_const_kernel(const double* x, double c, double* y, int64_t n
     if (i < n) y[i] = x[i] - c;
 }
 
+// ZT[k][i] = X[i][k] / l_k in float32 (k-major): the candidates' scaled
+// coordinates for the float32 kernel build, scaled once per call.
+__global__ void scale_rows_t_kernel(const double* X, int64_t rows, int d, const double* il,
+                                    float* ZT) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= rows * d) return;
+    const int64_t i = idx / d;
+    const int k = (int)(idx % d);
+    ZT[(int64_t)k * rows + i] = (float)(X[idx] * il[k]);
+}
+
 // XsT[k][c] = Xt[c][k] / l_k (k-major, for the adjoint's coalesced staging)
 __global__ void scale_inputs_kernel(const double* X, const double* il, int64_t n, int d,
                                     double* Xs64, float* Xs32) {
@@ -84,6 +95,7 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
     total += align_up(sizeof(double) * b * a->q * rr) * 2;
     total += align_up(sizeof(double) * b * a->q) * 2;
     total += align_up(sizeof(int));
+    if (es == sizeof(float)) total += align_up(sizeof(float) * rows * a->gp.d);
     if (ar == nullptr) return total;
     if (ar->cap < total) return 0;
     if (es == sizeof(float)) {
@@ -103,6 +115,7 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
     qa->gmu = ar->take<double>(b * a->q);
     int* e = ar->take<int>(1);
     if (err != nullptr) *err = e;
+    if (es == sizeof(float)) qa->zt = ar->take<float>(rows * a->gp.d);
     return total;
 }
 
@@ -165,10 +178,16 @@ template <> struct Ops<float> {
                     int64_t ldb, float* C, int64_t ldc, int kmode, int64_t n_tri, cudaStream_t st) {
         return gemm_f32(M, N, K, A, lda, B, ldb, C, ldc, kmode, n_tri, st);
     }
-    static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, float* K, cudaStream_t st) {
-        return launch_kernel_matrix<double, float, float>(X, rows, a->gp.train_X, a->gp.n, a->gp.d,
-                                                          a->gp.inv_lengthscale, a->gp.outputscale,
-                                                          a->gp.kernel, 0.0, 0, K, a->gp.n, st);
+    // K(X, Xt) in float32 from the scaled coordinates (zt: d x rows, Xs32: d x n);
+    // K_lo non-null: the tf32 hi / lo split with leading dimension ldk
+    static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, float* zt, float* K,
+                    int64_t ldk, float* K_lo, cudaStream_t st) {
+        const int64_t tot = rows * a->gp.d;
+        scale_rows_t_kernel<<<(unsigned)ceil_div(tot, 256), 256, 0, st>>>(
+            X, rows, a->gp.d, a->gp.inv_lengthscale, zt);
+        BGB_CHECK_LAUNCH();
+        return launch_kernel_matrix_zt(zt, rows, rows, a->Xs32, a->gp.n, a->gp.n, a->gp.d,
+                                       a->gp.outputscale, a->gp.kernel, K, ldk, st, K_lo);
     }
 };
 template <> struct Ops<double> {
@@ -184,11 +203,11 @@ template <> struct Ops<double> {
         return gemm_f64(M, N, K, 1.0, A, lda, 0, B, ldb, 0, 0.0, C, ldc, kmode, 0, nullptr, st,
                         n_tri);
     }
-    static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, double* K,
-                    cudaStream_t st) {
+    static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, float* /*zt*/, double* K,
+                    int64_t ldk, double* /*K_lo*/, cudaStream_t st) {
         return launch_kernel_matrix<double, double, double>(
             X, rows, a->gp.train_X, a->gp.n, a->gp.d, a->gp.inv_lengthscale, a->gp.outputscale,
-            a->gp.kernel, 0.0, 0, K, a->gp.n, st);
+            a->gp.kernel, 0.0, 0, K, ldk, st);
     }
 };
 
@@ -204,9 +223,7 @@ int run_front(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa, T*
             // tensor cores: K(X, Xt) as its tf32 split, then V = K L^-T
             float* Khi = Kc;
             float* Klo = Kc + rows * a->ldl;
-            rc = launch_kernel_matrix<double, float, float>(
-                X, rows, a->gp.train_X, n, a->gp.d, a->gp.inv_lengthscale, a->gp.outputscale,
-                a->gp.kernel, 0.0, 0, Khi, a->ldl, st, Klo);
+            rc = Ops<float>::kmat(a, X, rows, qa->zt, Khi, a->ldl, Klo, st);
             if (rc) return rc;
             if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[1], st));
             rc = tc_gemm_tf32x3(rows, n, n, Khi, Klo, a->ldl, a->Lhi, a->Llo, a->ldl, C, a->ldb,
@@ -215,16 +232,19 @@ int run_front(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa, T*
             goto after_gemm;
         }
     }
-    rc = Ops<T>::kmat(a, X, rows, Kc, st);
+    rc = Ops<T>::kmat(a, X, rows, qa->zt, Kc, n, nullptr, st);
     if (rc) return rc;
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[1], st));
     rc = Ops<T>::gemm(rows, n, n, Kc, n, Ops<T>::B(a), a->ldb, C, a->ldb, KB_UPPER, n, st);
     if (rc) return rc;
 after_gemm:
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[2], st));
-    rc = launch_row_dots<T>(*qa, C, a->ldb, Ops<T>::beta(a), Ops<T>::Vb(a), P, st);
-    if (rc) return rc;
-    rc = launch_sigma_reduce<T>(*qa, P, C, a->ldb, st);
+    rc = launch_qstats<T>(*qa, C, a->ldb, Ops<T>::beta(a), Ops<T>::Vb(a), st);
+    if (rc == BGB_ERR_UNSUPPORTED) {  // q > 8 or r > 4: separate row and pair passes
+        rc = launch_row_dots<T>(*qa, C, a->ldb, Ops<T>::beta(a), Ops<T>::Vb(a), P, st);
+        if (rc) return rc;
+        rc = launch_sigma_reduce<T>(*qa, P, C, a->ldb, st);
+    }
     if (rc) return rc;
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[3], st));
     return BGB_OK;
@@ -267,7 +287,9 @@ int run_call(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs& qa, T* 
         if (rc) return rc;
     }
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[6], st));
-    rc = launch_adjoint<T>(qa, C, a->ldb, Ops<T>::Xs(a), st);
+    // the Kc / H region is free once the adjoint GEMM has read H: slab partials go there
+    const int64_t kc_elems = tc ? 2 * rows * a->ldl : rows * n;
+    rc = launch_adjoint<T>(qa, C, a->ldb, Ops<T>::Xs(a), Kc, kc_elems, st);
     if (rc) return rc;
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[7], st));
     return BGB_OK;

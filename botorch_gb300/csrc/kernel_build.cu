@@ -29,7 +29,8 @@ template <typename TIn, typename TAcc, typename TOut>
 __global__ void __launch_bounds__(256) kernel_matrix_kernel(
     const TIn* __restrict__ X1, int64_t m, const TIn* __restrict__ X2, int64_t n2, int d,
     const double* __restrict__ inv_ls, double outputscale, int kind, double diag_add,
-    int same, TOut* __restrict__ K, int64_t ldk, TOut* __restrict__ K_lo) {
+    int same, TOut* __restrict__ K, int64_t ldk, TOut* __restrict__ K_lo,
+    const float* __restrict__ Z1T, int64_t ldz1, const float* __restrict__ Z2T, int64_t ldz2) {
     __shared__ TAcc s1[KB_DCHUNK][KB_TILE + 1];
     __shared__ TAcc s2[KB_DCHUNK][KB_TILE + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -44,7 +45,10 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
         for (int idx = threadIdx.x; idx < KB_DCHUNK * KB_TILE; idx += blockDim.x) {
             int kk = idx / KB_TILE, rr = idx % KB_TILE;
             TAcc v1 = 0, v2 = 0;
-            if (kk < kc) {
+            if (kk < kc && Z1T != nullptr) {  // pre-scaled float32, k-major
+                if (row0 + rr < m) v1 = (TAcc)Z1T[(int64_t)(k0 + kk) * ldz1 + row0 + rr];
+                if (col0 + rr < n2) v2 = (TAcc)Z2T[(int64_t)(k0 + kk) * ldz2 + col0 + rr];
+            } else if (kk < kc) {
                 const double il = inv_ls[k0 + kk];
                 if (row0 + rr < m) v1 = (TAcc)((double)X1[(row0 + rr) * d + k0 + kk] * il);
                 if (col0 + rr < n2) v2 = (TAcc)((double)X2[(col0 + rr) * d + k0 + kk] * il);
@@ -102,7 +106,21 @@ int launch_kernel_matrix(const TIn* X1, int64_t m, const TIn* X2, int64_t n2, in
     if (m <= 0 || n2 <= 0) return BGB_OK;
     dim3 grid((unsigned)ceil_div(n2, KB_TILE), (unsigned)ceil_div(m, KB_TILE));
     kernel_matrix_kernel<TIn, TAcc, TOut><<<grid, 256, 0, stream>>>(
-        X1, m, X2, n2, d, inv_ls, outputscale, kind, diag_add, same, K, ldk, K_lo);
+        X1, m, X2, n2, d, inv_ls, outputscale, kind, diag_add, same, K, ldk, K_lo, nullptr, 0,
+        nullptr, 0);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+int launch_kernel_matrix_zt(const float* Z1T, int64_t ldz1, int64_t m, const float* Z2T,
+                            int64_t ldz2, int64_t n2, int d, double outputscale, int kind,
+                            float* K, int64_t ldk, cudaStream_t stream, float* K_lo) {
+    if (m <= 0 || n2 <= 0) return BGB_OK;
+    if (Z1T == nullptr || Z2T == nullptr || ldz1 < m || ldz2 < n2) return BGB_ERR_ARG;
+    dim3 grid((unsigned)ceil_div(n2, KB_TILE), (unsigned)ceil_div(m, KB_TILE));
+    kernel_matrix_kernel<float, float, float><<<grid, 256, 0, stream>>>(
+        nullptr, m, nullptr, n2, d, nullptr, outputscale, kind, 0.0, 0, K, ldk, K_lo, Z1T, ldz1,
+        Z2T, ldz2);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }

@@ -210,6 +210,177 @@ __global__ void __launch_bounds__(256) row_dots_kernel(QBatchArgs a, const T* __
     }
 }
 
+// ---------------------------------------------------------------- qstats
+// row_dots + sigma_reduce in one pass over V for q <= 8, r <= 4: one CTA of 256
+// threads per t-batch reads its q rows of V once with 16-byte loads and forms
+//   G = V V^T (lower triangle), mu = m + V beta, P = V Vb^T,
+//   Sigma_qq = K(X,X) - G, Sigma_qb = K(X,Xb) - P.
+// Per thread: T sums over n / 256 columns (mu compensated). Across the 32 lanes
+// of a warp: a butterfly reduce-scatter of (hi, lo) pairs with error-free
+// two-sums, so each lane ends with NPAD / 32 totals and moves only about twice
+// that many values. Across the 8 warps: float64.
+template <typename T> struct Vec16;
+template <> struct Vec16<float> {
+    using type = float4;
+    static constexpr int E = 4;
+    static __device__ __forceinline__ float at(const float4& v, int e) {
+        return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+    }
+};
+template <> struct Vec16<double> {
+    using type = double2;
+    static constexpr int E = 2;
+    static __device__ __forceinline__ double at(const double2& v, int e) { return e == 0 ? v.x : v.y; }
+};
+
+// (h, l) += (bh, bl), with the rounding error of h + bh kept in l (Knuth two-sum)
+template <typename T>
+__device__ __forceinline__ void add_pair(T& h, T& l, T bh, T bl) {
+    const T s = h + bh;
+    const T bb = s - h;
+    const T e = (h - (s - bb)) + (bh - bb);
+    h = s;
+    l = l + bl + e;
+}
+
+constexpr int kQstatsThreads = 256;
+
+template <int NV>
+struct PadPow2 {
+    static constexpr int value = NV <= 32 ? 32 : NV <= 64 ? 64 : 128;
+};
+
+template <typename T, int QMAX, int RM>
+__global__ void __launch_bounds__(kQstatsThreads) qstats_kernel(QBatchArgs a, const T* __restrict__ V,
+                                                                int64_t ldv, const T* __restrict__ beta,
+                                                                const T* __restrict__ Vb, int vec_ok) {
+    using VT = typename Vec16<T>::type;
+    constexpr int E = Vec16<T>::E;
+    constexpr int NG = QMAX * (QMAX + 1) / 2;
+    constexpr int NV = NG + QMAX + QMAX * RM;
+    constexpr int NPAD = PadPow2<NV>::value;
+    constexpr int NPL = NPAD / 32;  // totals per lane after the butterfly
+    const int q = a.q, r = a.r, tid = threadIdx.x;
+    const int64_t n = a.n, bidx = blockIdx.x, rbase = bidx * q;
+    T g[NG], ms[QMAX], mc[QMAX], pv[QMAX * RM];
+#pragma unroll
+    for (int p = 0; p < NG; ++p) g[p] = T(0);
+#pragma unroll
+    for (int i = 0; i < QMAX; ++i) { ms[i] = T(0); mc[i] = T(0); }
+#pragma unroll
+    for (int p = 0; p < QMAX * RM; ++p) pv[p] = T(0);
+    // one column's contribution
+    auto consume = [&](const T* w, T bt, const T* vb) {
+        int p = 0;
+#pragma unroll
+        for (int i = 0; i < QMAX; ++i) {
+#pragma unroll
+            for (int j = 0; j <= i; ++j) {
+                g[p] = fma(w[i], w[j], g[p]);
+                ++p;
+            }
+            comp_add<T>(ms[i], mc[i], w[i] * bt);
+#pragma unroll
+            for (int k = 0; k < RM; ++k) pv[i * RM + k] = fma(w[i], vb[k], pv[i * RM + k]);
+        }
+    };
+    const int64_t nvec = vec_ok ? n / E : 0;
+    for (int64_t u = tid; u < nvec; u += kQstatsThreads) {
+        VT wv[QMAX], bv[RM];
+#pragma unroll
+        for (int i = 0; i < QMAX; ++i)
+            if (i < q) wv[i] = *reinterpret_cast<const VT*>(V + (rbase + i) * ldv + u * E);
+        const VT btv = *reinterpret_cast<const VT*>(beta + u * E);
+#pragma unroll
+        for (int k = 0; k < RM; ++k)
+            if (k < r) bv[k] = *reinterpret_cast<const VT*>(Vb + (int64_t)k * n + u * E);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            T w[QMAX], vb[RM];
+#pragma unroll
+            for (int i = 0; i < QMAX; ++i) w[i] = (i < q) ? Vec16<T>::at(wv[i], e) : T(0);
+#pragma unroll
+            for (int k = 0; k < RM; ++k) vb[k] = (k < r) ? Vec16<T>::at(bv[k], e) : T(0);
+            consume(w, Vec16<T>::at(btv, e), vb);
+        }
+    }
+    for (int64_t c = nvec * E + tid; c < n; c += kQstatsThreads) {
+        T w[QMAX], vb[RM];
+#pragma unroll
+        for (int i = 0; i < QMAX; ++i) w[i] = (i < q) ? V[(rbase + i) * ldv + c] : T(0);
+#pragma unroll
+        for (int k = 0; k < RM; ++k) vb[k] = (k < r) ? Vb[(int64_t)k * n + c] : T(0);
+        consume(w, beta[c], vb);
+    }
+    // butterfly reduce-scatter over the lanes
+    T h[NPAD], l[NPAD];
+#pragma unroll
+    for (int p = 0; p < NPAD; ++p) {
+        if (p < NG) { h[p] = g[p]; l[p] = T(0); }
+        else if (p < NG + QMAX) { h[p] = ms[p - NG]; l[p] = -mc[p - NG]; }
+        else if (p < NV) { h[p] = pv[p - NG - QMAX]; l[p] = T(0); }
+        else { h[p] = T(0); l[p] = T(0); }
+    }
+    const int lane = tid % 32, warp = tid / 32;
+    int base = 0;
+#pragma unroll
+    for (int lvl = 0; lvl < 5; ++lvl) {
+        const int half = NPAD >> (lvl + 1);
+        const bool up = (lane >> lvl) & 1;
+        if (up) base += half;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const T sh = up ? h[i] : h[i + half], sl = up ? l[i] : l[i + half];
+            T kh = up ? h[i + half] : h[i], kl = up ? l[i + half] : l[i];
+            const T rh = __shfl_xor_sync(0xffffffffu, sh, 1 << lvl);
+            const T rl = __shfl_xor_sync(0xffffffffu, sl, 1 << lvl);
+            add_pair<T>(kh, kl, rh, rl);
+            h[i] = kh;
+            l[i] = kl;
+        }
+    }
+    __shared__ double red[kQstatsThreads / 32][NPAD];
+#pragma unroll
+    for (int i = 0; i < NPL; ++i) red[warp][base + i] = (double)h[i] + (double)l[i];
+    __syncthreads();
+    if (tid >= NV) return;
+    double tot = 0.0;
+#pragma unroll
+    for (int w = 0; w < kQstatsThreads / 32; ++w) tot += red[w][tid];
+    const int d = a.d;
+    if (tid < NG) {
+        int i = 0;
+        while ((i + 1) * (i + 2) / 2 <= tid) ++i;
+        const int j = tid - i * (i + 1) / 2;
+        if (i >= q) return;
+        const double* xi = a.X + (rbase + i) * d;
+        const double* xj = a.X + (rbase + j) * d;
+        double r2 = 0.0;
+        for (int k = 0; k < d; ++k) {
+            const double df = (xi[k] - xj[k]) * a.inv_ls[k];
+            r2 = fma(df, df, r2);
+        }
+        const double v = a.outputscale * kappa<double>(a.kernel, r2) - tot;
+        a.sig[(bidx * q + i) * q + j] = v;
+        a.sig[(bidx * q + j) * q + i] = v;
+    } else if (tid < NG + QMAX) {
+        const int i = tid - NG;
+        if (i < q) a.mu[rbase + i] = a.mean_constant + tot;
+    } else {
+        const int i = (tid - NG - QMAX) / RM, kb = (tid - NG - QMAX) % RM;
+        if (i >= q || kb >= r) return;
+        const double* xi = a.X + (rbase + i) * d;
+        const double* xb = a.Xb + (int64_t)kb * d;
+        double r2 = 0.0;
+        for (int k = 0; k < d; ++k) {
+            const double df = (xi[k] - xb[k]) * a.inv_ls[k];
+            r2 = fma(df, df, r2);
+        }
+        // P rounded to T as the two-kernel path stores it
+        a.sqb[(bidx * q + i) * r + kb] = a.outputscale * kappa<double>(a.kernel, r2) - (double)(T)tot;
+    }
+}
+
 // ---------------------------------------------------------------- smooth pieces
 // softplus with torch's threshold 20 (beta = 1)
 __device__ __forceinline__ double softplus_t(double x) { return x > 20.0 ? x : log1p(exp(x)); }
@@ -678,72 +849,27 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
 }
 
 // ---------------------------------------------------------------- adjoint
-// d value / d X: one thread per row of X (64 rows per CTA). Per chunk of 64
-// training points the CTA stages, in shared memory, the D tile of its rows
-// (coalesced row segments) and the k-major scaled training inputs XsT (read
-// by all threads as broadcasts); each thread then sweeps the chunk with its
-// row's scaled coordinates and gradient accumulator in registers:
+// d value / d X through K(X, Xt): one thread per row of X, kAdjRows rows per CTA.
+// The training points are split into grid.y slabs, since the rows alone give
+// too few threads to hide latency. Per chunk of kAdjChunk points the CTA stages
+// the D tile of its rows (coalesced row segments) and the points' scaled
+// coordinates point-major (16-byte broadcast reads); each thread then sweeps the
+// chunk with its row's coordinates and gradient accumulator in registers:
 //   g += D[i,c] kappa'(r2_ic) (z_i - zt_c),   r2_ic = |z_i - zt_c|^2.
-constexpr int kAdjRows = 64;
+// One slab: the CTA finishes its rows (adjoint_finish_row). Several: each slab
+// writes its partial g to part[slab][k][row] and adjoint_finalize_kernel adds
+// the slabs in float64 and finishes the rows.
+constexpr int kAdjRows = 128;
 constexpr int kAdjChunk = 64;
 
-template <typename T, int DMAX>
-__global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
-                                                           int64_t ldd, const T* __restrict__ XsT) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    T* Xc = reinterpret_cast<T*>(smraw);              // [d][kAdjChunk]
-    T* Dc = Xc + (size_t)a.d * kAdjChunk;             // [kAdjRows][kAdjChunk + 1]
-    constexpr int LDD = kAdjChunk + 1;
+// K(X, X) and K(X, Xb) terms of the gradient (float64), then the chain rule
+// through the scaled coordinates; writes grad[row, :].
+template <int DMAX>
+__device__ __forceinline__ void adjoint_finish_row(const QBatchArgs& a, int64_t row, double* gx) {
     const int q = a.q, r = a.r, d = a.d, kind = a.kernel;
-    const int64_t n = a.n, rows = a.b * a.q;
-    const int tid = threadIdx.x;
-    const int64_t row0 = (int64_t)blockIdx.x * kAdjRows;
-    const int64_t row = row0 + tid;
-    const bool active = row < rows;
-    T zx[DMAX], g[DMAX];
-#pragma unroll
-    for (int k = 0; k < DMAX; ++k) {
-        zx[k] = (active && k < d) ? (T)(a.X[row * d + k] * a.inv_ls[k]) : T(0);
-        g[k] = T(0);
-    }
-    for (int64_t c0 = 0; c0 < n; c0 += kAdjChunk) {
-        const int cc = (int)((n - c0) < kAdjChunk ? (n - c0) : kAdjChunk);
-        __syncthreads();
-        for (int p = tid; p < kAdjRows * kAdjChunk; p += kAdjRows) {
-            const int rr = p / kAdjChunk, c = p % kAdjChunk;
-            Dc[rr * LDD + c] = (row0 + rr < rows && c < cc) ? Dm[(row0 + rr) * ldd + c0 + c] : T(0);
-        }
-        for (int p = tid; p < d * kAdjChunk; p += kAdjRows) {
-            const int k = p / kAdjChunk, c = p % kAdjChunk;
-            Xc[k * kAdjChunk + c] = (c < cc) ? XsT[(int64_t)k * n + c0 + c] : T(0);
-        }
-        __syncthreads();
-        for (int c = 0; c < cc; ++c) {
-            const T dk = Dc[tid * LDD + c];
-            T df[DMAX];
-            T r2a = T(0), r2b = T(0);
-#pragma unroll
-            for (int k = 0; k < DMAX; k += 2) {
-                df[k] = (k < d) ? zx[k] - Xc[k * kAdjChunk + c] : T(0);
-                r2a = fma(df[k], df[k], r2a);
-                if (k + 1 < DMAX) {
-                    df[k + 1] = (k + 1 < d) ? zx[k + 1] - Xc[(k + 1) * kAdjChunk + c] : T(0);
-                    r2b = fma(df[k + 1], df[k + 1], r2b);
-                }
-            }
-            const T coef = dk * dkappa_dr2<T>(kind, r2a + r2b);
-#pragma unroll
-            for (int k = 0; k < DMAX; ++k) g[k] = fma(coef, df[k], g[k]);
-        }
-    }
-    if (!active) return;
     const int64_t bidx = row / q;
     const int i = (int)(row % q);
     if (a.dev_err != nullptr && *a.dev_err != 0 && i == 0) a.status[bidx] = BGB_DEVICE_TIMEOUT;
-    // K(X, X) and K(X, Xb) terms, float64
-    double gx[DMAX];
-#pragma unroll
-    for (int k = 0; k < DMAX; ++k) gx[k] = (double)g[k];
     const int64_t rbase = bidx * q;
     for (int j = 0; j < q + r; ++j) {
         if (j == i) continue;
@@ -763,6 +889,99 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
 #pragma unroll
     for (int k = 0; k < DMAX; ++k)
         if (k < d) a.grad[row * d + k] = 2.0 * a.outputscale * a.inv_ls[k] * gx[k];
+}
+
+template <typename T, int DMAX, bool FINISH>
+__global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
+                                                           int64_t ldd, const T* __restrict__ XsT,
+                                                           int64_t slab, T* __restrict__ part) {
+    using VT = typename Vec16<T>::type;
+    constexpr int E = Vec16<T>::E;
+    static_assert(DMAX % E == 0, "DMAX must hold whole 16-byte vectors");
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* Xc = reinterpret_cast<T*>(smraw);              // [kAdjChunk][DMAX], point-major
+    T* Dc = Xc + (size_t)kAdjChunk * DMAX;            // [kAdjRows][kAdjChunk + 1]
+    constexpr int LDD = kAdjChunk + 1;
+    const int d = a.d, kind = a.kernel;
+    const int64_t n = a.n, rows = a.b * a.q;
+    const int tid = threadIdx.x;
+    const int64_t row0 = (int64_t)blockIdx.x * kAdjRows;
+    const int64_t row = row0 + tid;
+    const bool active = row < rows;
+    const int64_t cbeg = (int64_t)blockIdx.y * slab;
+    const int64_t cend = (cbeg + slab < n) ? cbeg + slab : n;
+    T zx[DMAX], g[DMAX];
+#pragma unroll
+    for (int k = 0; k < DMAX; ++k) {
+        zx[k] = (active && k < d) ? (T)(a.X[row * d + k] * a.inv_ls[k]) : T(0);
+        g[k] = T(0);
+    }
+    for (int64_t c0 = cbeg; c0 < cend; c0 += kAdjChunk) {
+        const int cc = (int)((cend - c0) < kAdjChunk ? (cend - c0) : kAdjChunk);
+        __syncthreads();
+        for (int p = tid; p < kAdjRows * kAdjChunk; p += kAdjRows) {
+            const int rr = p / kAdjChunk, c = p % kAdjChunk;
+            Dc[rr * LDD + c] = (row0 + rr < rows && c < cc) ? Dm[(row0 + rr) * ldd + c0 + c] : T(0);
+        }
+        for (int p = tid; p < DMAX * kAdjChunk; p += kAdjRows) {
+            const int k = p / kAdjChunk, c = p % kAdjChunk;
+            Xc[c * DMAX + k] = (c < cc && k < d) ? XsT[(int64_t)k * n + c0 + c] : T(0);
+        }
+        __syncthreads();
+        for (int c = 0; c < cc; ++c) {
+            const T dk = Dc[tid * LDD + c];
+            const VT* xc = reinterpret_cast<const VT*>(Xc + c * DMAX);
+            T df[DMAX];
+            T r2a = T(0), r2b = T(0);
+#pragma unroll
+            for (int v = 0; v < DMAX / E; ++v) {
+                const VT x4 = xc[v];
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const int k = v * E + e;
+                    df[k] = zx[k] - Vec16<T>::at(x4, e);
+                    if (k % 2 == 0) r2a = fma(df[k], df[k], r2a);
+                    else r2b = fma(df[k], df[k], r2b);
+                }
+            }
+            const T coef = dk * dkappa_dr2<T>(kind, r2a + r2b);
+#pragma unroll
+            for (int k = 0; k < DMAX; ++k) g[k] = fma(coef, df[k], g[k]);
+        }
+    }
+    if (!active) return;
+    if constexpr (FINISH) {
+        double gx[DMAX];
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k) gx[k] = (double)g[k];
+        adjoint_finish_row<DMAX>(a, row, gx);
+        return;
+    }
+    if constexpr (!FINISH) {
+    T* pp = part + (int64_t)blockIdx.y * d * rows;
+#pragma unroll
+    for (int k = 0; k < DMAX; ++k)
+        if (k < d) pp[(int64_t)k * rows + row] = g[k];
+    }
+}
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(128) adjoint_finalize_kernel(QBatchArgs a, const T* __restrict__ part,
+                                                               int nslab) {
+    const int64_t rows = a.b * a.q;
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= rows) return;
+    const int d = a.d;
+    double gx[DMAX];
+#pragma unroll
+    for (int k = 0; k < DMAX; ++k) gx[k] = 0.0;
+    for (int s = 0; s < nslab; ++s) {
+        const T* pp = part + (int64_t)s * d * rows;
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k)
+            if (k < d) gx[k] += (double)pp[(int64_t)k * rows + row];
+    }
+    adjoint_finish_row<DMAX>(a, row, gx);
 }
 
 __global__ void posterior_out_kernel(QBatchArgs a, double* mean, double* covar) {
@@ -819,6 +1038,28 @@ int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bo
 }
 
 template <typename T>
+int launch_qstats(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb,
+                  cudaStream_t stream) {
+    if (a.b <= 0) return BGB_OK;
+    if (a.q > 8 || a.r > 4 || (a.r > 0 && Vb == nullptr)) return BGB_ERR_UNSUPPORTED;
+    constexpr int E = Vec16<T>::E;
+    auto al = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) % 16) == 0; };
+    const int vec_ok = (ldv % E == 0) && (a.n % E == 0) && al(V) && al(beta) &&
+                       (a.r == 0 || al(Vb));
+    const unsigned grid = (unsigned)a.b;
+    if (a.q <= 4 && a.r <= 2)
+        qstats_kernel<T, 4, 2><<<grid, kQstatsThreads, 0, stream>>>(a, V, ldv, beta, Vb, vec_ok);
+    else if (a.q <= 4)
+        qstats_kernel<T, 4, 4><<<grid, kQstatsThreads, 0, stream>>>(a, V, ldv, beta, Vb, vec_ok);
+    else if (a.r <= 2)
+        qstats_kernel<T, 8, 2><<<grid, kQstatsThreads, 0, stream>>>(a, V, ldv, beta, Vb, vec_ok);
+    else
+        qstats_kernel<T, 8, 4><<<grid, kQstatsThreads, 0, stream>>>(a, V, ldv, beta, Vb, vec_ok);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+template <typename T>
 int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb, T* P,
                     cudaStream_t stream) {
     const int64_t rows = a.b * a.q;
@@ -845,25 +1086,59 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
     return BGB_OK;
 }
 
-template <typename T>
-size_t adjoint_smem_bytes(int d) {
-    return sizeof(T) * ((size_t)d * kAdjChunk + (size_t)kAdjRows * (kAdjChunk + 1));
+template <typename T, int DMAX>
+size_t adjoint_smem_bytes() {
+    return sizeof(T) * ((size_t)kAdjChunk * DMAX + (size_t)kAdjRows * (kAdjChunk + 1));
 }
 
+// part_cap: elements of scratch available for the slab partials (0: one slab).
 template <typename T>
-int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, cudaStream_t stream) {
+int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T* part,
+                   int64_t part_cap, cudaStream_t stream) {
     const int64_t rows = a.b * a.q;
     if (rows <= 0) return BGB_OK;
-    const size_t smem = adjoint_smem_bytes<T>(a.d);
-    if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
-    const unsigned grid = (unsigned)ceil_div(rows, kAdjRows);
+    const int64_t row_blocks = ceil_div(rows, kAdjRows);
+    // slabs: about four waves of four CTAs per SM, slabs of whole chunks, partials
+    // within part_cap
+    static int num_sms = 0;
+    if (num_sms == 0) {
+        int dev = 0, v = 0;
+        BGB_CUDA_TRY(cudaGetDevice(&dev));
+        BGB_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        num_sms = v > 0 ? v : 1;
+    }
+    const int64_t chunks = ceil_div(a.n, kAdjChunk);
+    int64_t nslab = ceil_div((int64_t)num_sms * 16, row_blocks);
+    if (nslab > chunks) nslab = chunks;
+    if (nslab > 65535) nslab = 65535;
+    if (part == nullptr || part_cap <= 0) nslab = 1;
+    while (nslab > 1 && nslab * a.d * rows > part_cap) --nslab;
+    if (nslab < 1) nslab = 1;
+    const int64_t slab = ceil_div(chunks, nslab) * kAdjChunk;
+    nslab = ceil_div(a.n, slab);
+    T* pp = nslab > 1 ? part : nullptr;
+    dim3 grid((unsigned)row_blocks, (unsigned)nslab);
 #define BGB_ADJ(DM)                                                                              \
     do {                                                                                        \
-        if (smem > 48 * 1024)                                                                   \
-            BGB_CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel<T, DM>,                            \
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize,      \
-                                              (int)smem));                                      \
-        adjoint_kernel<T, DM><<<grid, kAdjRows, smem, stream>>>(a, D, ldd, XsT);                \
+        const size_t smem = adjoint_smem_bytes<T, DM>();                                        \
+        if (pp == nullptr) {                                                                    \
+            if (smem > 48 * 1024)                                                               \
+                BGB_CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel<T, DM, true>,                  \
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                                  (int)smem));                                  \
+            adjoint_kernel<T, DM, true><<<grid, kAdjRows, smem, stream>>>(a, D, ldd, XsT, slab, pp); \
+            BGB_CHECK_LAUNCH();                                                                 \
+        } else {                                                                                \
+            if (smem > 48 * 1024)                                                               \
+                BGB_CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel<T, DM, false>,                 \
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                                  (int)smem));                                  \
+            adjoint_kernel<T, DM, false><<<grid, kAdjRows, smem, stream>>>(a, D, ldd, XsT, slab, pp); \
+            BGB_CHECK_LAUNCH();                                                                 \
+            adjoint_finalize_kernel<T, DM><<<(unsigned)ceil_div(rows, 128), 128, 0, stream>>>(  \
+                a, pp, (int)nslab);                                                             \
+            BGB_CHECK_LAUNCH();                                                                 \
+        }                                                                                       \
     } while (0)
     if (a.d <= 8) BGB_ADJ(8);
     else if (a.d <= 16) BGB_ADJ(16);
@@ -872,7 +1147,6 @@ int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, c
     else if (a.d <= 64) BGB_ADJ(64);
     else return BGB_ERR_UNSUPPORTED;
 #undef BGB_ADJ
-    BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
 
@@ -888,6 +1162,10 @@ template int launch_sigma_reduce<double>(const QBatchArgs&, const double*, const
                                          cudaStream_t);
 template int launch_sigma_reduce<float>(const QBatchArgs&, const float*, const float*, int64_t,
                                         cudaStream_t);
+template int launch_qstats<double>(const QBatchArgs&, const double*, int64_t, const double*,
+                                   const double*, cudaStream_t);
+template int launch_qstats<float>(const QBatchArgs&, const float*, int64_t, const float*,
+                                  const float*, cudaStream_t);
 template int launch_row_dots<double>(const QBatchArgs&, const double*, int64_t, const double*,
                                      const double*, double*, cudaStream_t);
 template int launch_row_dots<float>(const QBatchArgs&, const float*, int64_t, const float*,
@@ -897,8 +1175,8 @@ template int launch_mix_rows<double>(const QBatchArgs&, const double*, int64_t, 
 template int launch_mix_rows<float>(const QBatchArgs&, const float*, int64_t, const float*,
                                     const float*, float*, cudaStream_t, float*, int64_t);
 template int launch_adjoint<double>(const QBatchArgs&, const double*, int64_t, const double*,
-                                    cudaStream_t);
+                                    double*, int64_t, cudaStream_t);
 template int launch_adjoint<float>(const QBatchArgs&, const float*, int64_t, const float*,
-                                   cudaStream_t);
+                                   float*, int64_t, cudaStream_t);
 
 }  // namespace bgb
