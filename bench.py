@@ -342,8 +342,9 @@ def run_ours(args) -> None:
         "data": "synthetic (seeded Branin-sum GP workload)",
         "config": {"workload": WORKLOAD, "n": N_TRAIN, "d": DIM, "q": Q, "mc_samples": S,
                    "batch_per_call": b, "baseline_points_r": acqf.r, "kernel": "matern52",
-                   "precision": "mixed: f32 kernel build + cross-covariance GEMMs, f64 Cholesky/"
-                                "sample step/log-mean-exp", "l2": "flushed before each step (256 MB write)",
+                   "precision": "mixed: f32 kernel build, 3xTF32 cross-covariance GEMMs, f64 q x q "
+                                "Cholesky + adjoint, f32 samples from exact f32 pairs of mu - best_f, "
+                                "f64 accumulations", "l2": "flushed before each step (256 MB write)",
                    "parallelism": f"replicas, weak scaling over t-batches x{world}"},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
         "gpu_launches": int(launches), "clocks": clk.summary(),

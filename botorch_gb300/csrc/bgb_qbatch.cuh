@@ -38,6 +38,8 @@ struct QBatchArgs {
     int32_t* status;        // b
     const int* dev_err;     // non-zero: a bounded wait in a tensor-core GEMM expired
     float* zt;              // mixed: candidates scaled by 1 / lengthscale, d x (b*q), k-major
+    float* z32;             // mixed: Z in float32 (S x (r+q))
+    float* bf32;            // mixed: best_f per sample as float (hi, lo) pairs (S x 2)
 };
 
 // mu, Sigma_qq and Sigma_qb in one pass over V (q <= 8, r <= 4); returns
@@ -55,7 +57,7 @@ int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc
                         cudaStream_t stream);
 // mixed: float32 evaluation of the per-sample smooth reductions (see qbatch.cu)
 int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bool mixed = false);
-size_t batch_step_smem_bytes(int q, int r, int S, bool mixed_backward);
+size_t batch_step_smem_bytes(int q, int r, int S);
 // H (b*q x n) = gmu beta^T - 2 Gqq V - Gqb Vb per t-batch
 // H_lo non-null (float32): write the tf32 hi/lo split (H = hi) with leading dimension ldh.
 template <typename T>

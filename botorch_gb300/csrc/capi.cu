@@ -95,7 +95,11 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
     total += align_up(sizeof(double) * b * a->q * rr) * 2;
     total += align_up(sizeof(double) * b * a->q) * 2;
     total += align_up(sizeof(int));
-    if (es == sizeof(float)) total += align_up(sizeof(float) * rows * a->gp.d);
+    if (es == sizeof(float)) {
+        total += align_up(sizeof(float) * rows * a->gp.d);
+        total += align_up(sizeof(float) * (size_t)a->n_samples * (a->r + a->q));
+        total += align_up(sizeof(float) * 2 * (size_t)a->n_samples);
+    }
     if (ar == nullptr) return total;
     if (ar->cap < total) return 0;
     if (es == sizeof(float)) {
@@ -115,7 +119,11 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
     qa->gmu = ar->take<double>(b * a->q);
     int* e = ar->take<int>(1);
     if (err != nullptr) *err = e;
-    if (es == sizeof(float)) qa->zt = ar->take<float>(rows * a->gp.d);
+    if (es == sizeof(float)) {
+        qa->zt = ar->take<float>(rows * a->gp.d);
+        qa->z32 = ar->take<float>((int64_t)a->n_samples * (a->r + a->q));
+        qa->bf32 = ar->take<float>(2 * (int64_t)a->n_samples);
+    }
     return total;
 }
 

@@ -453,11 +453,7 @@ __device__ int chol_small(double* A, int q) {
 //                          t S | dY SC*q | scratch q*q
 constexpr int kSampleChunk = 128;
 
-// MIXED: the per-sample log_fatplus / fatmax (and their derivatives, kept in
-// shared memory for the reverse pass) are evaluated in float32 from the
-// float64 improvement u = Y - best_f; Y, the Cholesky, log-mean-exp and every
-// accumulation stay float64.
-template <bool MIXED>
+// The float64 path's step (the mixed path's is batch_step_f32_kernel).
 __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backward) {
     extern __shared__ double sm[];
     const int q = a.q, r = a.r, S = a.S, D = r + q;
@@ -471,9 +467,6 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     double* tS = dmu + q;
     double* dY = tS + S;
     double* scr = dY + kSampleChunk * q;
-    // MIXED + backward: float li and d li / du per (sample, point) after scr
-    float* Lf = reinterpret_cast<float*>(scr + (q * q > q * r ? q * q : q * r));
-    float* Df = Lf + S * q;
     __shared__ int s_status;
     __shared__ double s_red[4];
     __shared__ double s_lse;
@@ -549,40 +542,11 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     }
     const bool qei = (a.acqf == BGB_ACQF_QEI);
     const double tau = a.tau_relu, taum = a.tau_max;
-    const double inv_tau = 1.0 / tau;
-    const float log_tau = (float)log(tau);
-    const float inv_taum = (float)(1.0 / taum);
     // (5) forward over samples: t_s (per-sample reduced utility)
     int local_bad = 0;
     for (int s = tid; s < S; s += blockDim.x) {
         const double* z = a.Z + (int64_t)s * D;
         const double bf = qei ? a.best_f[0] : a.best_f[s];
-        if (MIXED && !qei) {
-            float lf[kMaxQ];
-            float Mf = -INFINITY;
-            for (int i = 0; i < q; ++i) {
-                double y = mu[i];
-                for (int k = 0; k < r + i + 1; ++k) y += Lq[i * D + k] * z[k];
-                if (!isfinite(y)) local_bad = 1;
-                float dl;
-                log_fatplus_f((float)((y - bf) * inv_tau), log_tau, (float)inv_tau, lf[i], dl);
-                if (backward) {
-                    Lf[s * q + i] = lf[i];
-                    Df[s * q + i] = dl;
-                }
-                Mf = fmaxf(Mf, lf[i]);
-            }
-            float t;
-            if (isinf(Mf)) {
-                t = Mf;
-            } else {
-                float P = 0.f;
-                for (int i = 0; i < q; ++i) P += pareto2_f((Mf - lf[i]) * inv_taum);
-                t = Mf + (float)taum * logf(P);
-            }
-            tS[s] = (double)t;
-            continue;
-        }
         double li[kMaxQ];
         double Mx = -INFINITY;
         for (int i = 0; i < q; ++i) {
@@ -666,32 +630,6 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
         const int sc = min(kSampleChunk, S - s0);
         for (int ls = tid; ls < sc; ls += blockDim.x) {
             const int s = s0 + ls;
-            if (MIXED && !qei) {
-                const float* lf = Lf + s * q;
-                const float* df = Df + s * q;
-                float Mf = -INFINITY;
-                for (int i = 0; i < q; ++i) Mf = fmaxf(Mf, lf[i]);
-                int nt = 0;
-                for (int i = 0; i < q; ++i) nt += (lf[i] == Mf);
-                const double ws = isinf(mx) ? (tS[s] == mx ? 1.0 : 0.0) : exp(tS[s] - lse);
-                if (isinf(Mf)) {
-                    for (int i = 0; i < q; ++i) dY[ls * q + i] = (lf[i] == Mf) ? ws : 0.0;
-                } else {
-                    float P = 0.f, Pd = 0.f;
-                    for (int i = 0; i < q; ++i) {
-                        const float x = (Mf - lf[i]) * inv_taum;
-                        P += pareto2_f(x);
-                        Pd += dpareto2_f(x);
-                    }
-                    const float top = (1.f + Pd / P) / (float)nt;
-                    for (int i = 0; i < q; ++i) {
-                        const float x = (Mf - lf[i]) * inv_taum;
-                        const float dt = -dpareto2_f(x) / P + (lf[i] == Mf ? top : 0.f);
-                        dY[ls * q + i] = ws * (double)(dt * df[i]);
-                    }
-                }
-                continue;
-            }
             const double* z = a.Z + (int64_t)s * D;
             const double bf = qei ? a.best_f[0] : a.best_f[s];
             double u[kMaxQ], li[kMaxQ], g[kMaxQ];
@@ -797,6 +735,370 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     }
     for (int p = tid; p < q * q; p += blockDim.x) a.gqq[bidx * q * q + p] = sy2 * gA[p];
     for (int i = tid; i < q; i += blockDim.x) a.gmu[bidx * q + i] = sy * dmu[i];
+}
+
+// ---------------------------------------------------------------- batch_step (mixed)
+// Per-t-batch step of the mixed path. float64 for the q x q algebra: the
+// covariance blocks, bl = Sigma_qb Lb^-T, M = Sigma_qq - bl bl^T, its jittered
+// Cholesky and the Cholesky adjoint. float32 for the per-sample work: the
+// improvement
+//   u = (mu - best_f) + [bl, br] z
+// is formed from exact float pairs (hi, lo) of mu and best_f, the leading
+// difference mu_hi - bf_hi by an error-free two-sum, so the cancellation near
+// the incumbent is exact and only the zero-mean term [bl, br] z carries float32
+// rounding. The reverse pass recomputes each sample's forward rather than
+// storing it, and accumulates d[bl, br] = sum_s dY_s z_s^T per chunk of samples
+// (float32 within a chunk, float64 across chunks).
+constexpr int kBsThreads = 128;
+
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// u_i (i < q) of one sample; zs: the sample's D base-sample coordinates
+template <int QMAX>
+__device__ __forceinline__ void sample_u(const float* __restrict__ Lf, const float* __restrict__ zs,
+                                         int q, int r, int D, const float* muh, const float* mul,
+                                         float bh, float bl, float* u) {
+    float y[QMAX];
+#pragma unroll
+    for (int i = 0; i < QMAX; ++i) y[i] = 0.f;
+    for (int k = 0; k < D; ++k) {
+        const float zk = zs[k];
+#pragma unroll
+        for (int i = 0; i < QMAX; ++i)
+            if (i < q && k < r + i + 1) y[i] = fmaf(Lf[i * D + k], zk, y[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < QMAX; ++i) {
+        float dh, e;
+        two_sum_f(muh[i], -bh, dh, e);
+        u[i] = (i < q) ? dh + ((e + (mul[i] - bl)) + y[i]) : 0.f;
+    }
+}
+
+// psd_safe_cholesky of the q x q matrix M (float64, row-major) into scr: plain,
+// then jitter j * 10^t (t < max_tries) added to M's diagonal. Column pivots use
+// one reciprocal each. Returns 0, BGB_NOT_PSD or BGB_NAN.
+__device__ int psd_chol_rcp(double* M, double* scr, int q, int max_tries, double jitter) {
+    bool has_nan = false;
+    for (int p = 0; p < q * q; ++p) has_nan |= isnan(M[p]);
+    if (has_nan) return BGB_NAN;
+    double jprev = 0.0;
+    for (int t = -1; t < max_tries; ++t) {
+        if (t >= 0) {
+            const double jnew = jitter * pow(10.0, (double)t);
+            for (int i = 0; i < q; ++i) M[i * q + i] += jnew - jprev;
+            jprev = jnew;
+        }
+        for (int p = 0; p < q * q; ++p) scr[p] = M[p];
+        bool ok = true;
+        for (int j = 0; j < q && ok; ++j) {
+            double v = scr[j * q + j];
+            for (int k = 0; k < j; ++k) v -= scr[j * q + k] * scr[j * q + k];
+            if (!(v > 0.0)) { ok = false; break; }
+            const double djj = sqrt(v), rj = 1.0 / djj;
+            scr[j * q + j] = djj;
+            for (int i = j + 1; i < q; ++i) {
+                double s = scr[i * q + j];
+                for (int k = 0; k < j; ++k) s -= scr[i * q + k] * scr[j * q + k];
+                scr[i * q + j] = s * rj;
+            }
+            for (int k = j + 1; k < q; ++k) scr[j * q + k] = 0.0;
+        }
+        if (ok) return 0;
+    }
+    return BGB_NOT_PSD;
+}
+
+template <int QMAX>
+__global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a, int backward) {
+    extern __shared__ double smd[];
+    constexpr int NW = kBsThreads / 32;
+    const int q = a.q, r = a.r, S = a.S, D = r + q;
+    const int64_t bidx = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    double* M = smd;                 // q x q
+    double* Lq = M + q * q;          // q x D: [bl, br]
+    double* dLq = Lq + q * D;        // q x D
+    double* gA = dLq + q * D;        // q x q
+    double* scr = gA + q * q;        // max(q*q, q*r)
+    float* Lf = reinterpret_cast<float*>(scr + (q * q > q * r ? q * q : q * r));  // q x D
+    float* tS = Lf + q * D;          // S
+    float* dY = tS + S;              // kSampleChunk x q
+    __shared__ float s_muh[QMAX], s_mul[QMAX];
+    __shared__ double s_dmu[QMAX], s_rd[QMAX];
+    __shared__ int s_status;
+    __shared__ double s_red[NW];
+    __shared__ float s_redf[NW];
+    __shared__ double s_lse;
+    const double sy = a.y_std, sy2 = sy * sy;
+    auto fail = [&](int status) {
+        if (tid == 0) {
+            a.status[bidx] = status;
+            a.value[bidx] = NAN;
+        }
+        if (backward && status != BGB_DEVICE_TIMEOUT) {
+            for (int p = tid; p < q * q; p += kBsThreads) a.gqq[bidx * q * q + p] = 0.0;
+            for (int p = tid; p < q * r; p += kBsThreads) a.gqb[bidx * q * r + p] = 0.0;
+            for (int p = tid; p < q; p += kBsThreads) a.gmu[bidx * q + p] = 0.0;
+        }
+    };
+    if (tid == 0) s_status = (a.dev_err != nullptr && *a.dev_err != 0) ? BGB_DEVICE_TIMEOUT : 0;
+    __syncthreads();
+    if (s_status != 0) {
+        fail(s_status);
+        return;
+    }
+    // (1) untransformed mean as a float pair, covariance blocks
+    for (int i = tid; i < QMAX; i += kBsThreads) {
+        const double mu = (i < q) ? a.y_mean + sy * a.mu[bidx * q + i] : 0.0;
+        const float h = (float)mu;
+        s_muh[i] = h;
+        s_mul[i] = (float)(mu - (double)h);
+    }
+    for (int p = tid; p < q * q; p += kBsThreads) M[p] = sy2 * a.sig[bidx * q * q + p];
+    __syncthreads();
+    // (2) bl = Sigma_qb Lb^-T (Lb^-1 lower triangular)
+    for (int p = tid; p < q * r; p += kBsThreads) {
+        const int i = p / r, k = p % r;
+        double acc = 0.0;
+        for (int kk = 0; kk <= k; ++kk) acc += sy2 * a.sqb[(bidx * q + i) * r + kk] * a.Lb_inv[k * r + kk];
+        Lq[i * D + k] = acc;
+    }
+    __syncthreads();
+    // (3) M = Sigma_qq - bl bl^T
+    for (int p = tid; p < q * q; p += kBsThreads) {
+        const int i = p / q, j = p % q;
+        double acc = 0.0;
+        for (int k = 0; k < r; ++k) acc += Lq[i * D + k] * Lq[j * D + k];
+        M[p] -= acc;
+    }
+    __syncthreads();
+    // (4) br = psd_safe_cholesky(M) for this t-batch
+    if (tid == 0) {
+        const int st = psd_chol_rcp(M, scr, q, a.max_tries, a.jitter);
+        for (int i = 0; i < q; ++i)
+            for (int j = 0; j < q; ++j) Lq[i * D + r + j] = (j <= i) ? scr[i * q + j] : 0.0;
+        s_status = st;
+    }
+    __syncthreads();
+    if (s_status != 0) {
+        fail(s_status);
+        return;
+    }
+    for (int p = tid; p < q * D; p += kBsThreads) Lf[p] = (float)Lq[p];
+    __syncthreads();
+    const bool qei = (a.acqf == BGB_ACQF_QEI);
+    const float inv_tau = (float)(1.0 / a.tau_relu);
+    const float log_tau = (float)log(a.tau_relu);
+    const float taum = (float)a.tau_max, inv_taum = (float)(1.0 / a.tau_max);
+    const float* __restrict__ z32 = a.z32;
+    const float* __restrict__ bf32 = a.bf32;
+    // (5) forward: t_s per sample
+    int local_bad = 0;
+    for (int s = tid; s < S; s += kBsThreads) {
+        float u[QMAX];
+        sample_u<QMAX>(Lf, z32 + (int64_t)s * D, q, r, D, s_muh, s_mul, bf32[2 * s], bf32[2 * s + 1], u);
+        float Mx = -INFINITY, li[QMAX];
+#pragma unroll
+        for (int i = 0; i < QMAX; ++i) {
+            if (i >= q) { li[i] = -INFINITY; continue; }
+            if (!isfinite(u[i])) local_bad = 1;
+            if (qei) {
+                li[i] = fmaxf(u[i], 0.f);
+            } else {
+                float dl;
+                log_fatplus_f(u[i] * inv_tau, log_tau, inv_tau, li[i], dl);
+            }
+            Mx = fmaxf(Mx, li[i]);
+        }
+        float t = Mx;
+        if (!qei && !isinf(Mx)) {
+            float P = 0.f;
+#pragma unroll
+            for (int i = 0; i < QMAX; ++i)
+                if (i < q) P += pareto2_f((Mx - li[i]) * inv_taum);
+            t = Mx + taum * logf(P);
+        }
+        tS[s] = t;
+    }
+    if (__syncthreads_or(local_bad)) {
+        fail(BGB_NAN);
+        return;
+    }
+    // (6) reduction over samples: qEI mean, qLogNEI log-mean-exp (inf handling as the reference)
+    float mx = -INFINITY;
+    for (int s = tid; s < S; s += kBsThreads) mx = fmaxf(mx, tS[s]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s_redf[warp] = mx;
+    __syncthreads();
+    mx = s_redf[0];
+#pragma unroll
+    for (int w = 1; w < NW; ++w) mx = fmaxf(mx, s_redf[w]);
+    float part = 0.f;
+    for (int s = tid; s < S; s += kBsThreads) {
+        if (qei) part += tS[s];
+        else if (!isinf(mx)) part += expf(tS[s] - mx);
+    }
+    double acc = (double)part;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_red[warp] = acc;
+    __syncthreads();
+    if (tid == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < NW; ++w) tot += s_red[w];
+        double v, lse;
+        if (qei) {
+            v = tot / S;
+            lse = 0.0;
+        } else if (isinf(mx)) {
+            v = mx;
+            lse = mx;
+        } else {
+            lse = (double)mx + log(tot);
+            v = lse - log((double)S);
+        }
+        a.value[bidx] = v;
+        a.status[bidx] = 0;
+        s_lse = lse;
+    }
+    if (!backward) return;
+    for (int p = tid; p < q * D; p += kBsThreads) dLq[p] = 0.0;
+    for (int i = tid; i < QMAX; i += kBsThreads) s_dmu[i] = 0.0;
+    __syncthreads();
+    const float lse_f = (float)s_lse;
+    const bool inf_mx = isinf(mx);
+    // (7) reverse through the sample reduction and the sample step, a chunk of samples at a time
+    for (int s0 = 0; s0 < S; s0 += kSampleChunk) {
+        const int sc = min(kSampleChunk, S - s0);
+        for (int ls = tid; ls < sc; ls += kBsThreads) {
+            const int s = s0 + ls;
+            float u[QMAX], li[QMAX], dli[QMAX], g[QMAX];
+            sample_u<QMAX>(Lf, z32 + (int64_t)s * D, q, r, D, s_muh, s_mul, bf32[2 * s], bf32[2 * s + 1], u);
+            float Mx = -INFINITY;
+#pragma unroll
+            for (int i = 0; i < QMAX; ++i) {
+                if (i >= q) { li[i] = -INFINITY; dli[i] = 0.f; continue; }
+                if (qei) li[i] = fmaxf(u[i], 0.f);
+                else log_fatplus_f(u[i] * inv_tau, log_tau, inv_tau, li[i], dli[i]);
+                Mx = fmaxf(Mx, li[i]);
+            }
+            int nt = 0;
+#pragma unroll
+            for (int i = 0; i < QMAX; ++i) nt += (i < q && li[i] == Mx);
+            if (qei) {
+                const float w = 1.f / ((float)S * (float)nt);
+#pragma unroll
+                for (int i = 0; i < QMAX; ++i) g[i] = (i < q && li[i] == Mx && u[i] >= 0.f) ? w : 0.f;
+            } else {
+                float t = Mx, P = 0.f, Pd = 0.f;
+                if (!isinf(Mx)) {
+#pragma unroll
+                    for (int i = 0; i < QMAX; ++i) {
+                        if (i >= q) continue;
+                        const float x = (Mx - li[i]) * inv_taum;
+                        P += pareto2_f(x);
+                        Pd += dpareto2_f(x);
+                    }
+                    t = Mx + taum * logf(P);
+                }
+                const float ws = inf_mx ? (t == mx ? 1.f : 0.f) : expf(t - lse_f);
+                if (isinf(Mx)) {
+#pragma unroll
+                    for (int i = 0; i < QMAX; ++i) g[i] = (i < q && li[i] == Mx) ? ws : 0.f;
+                } else {
+                    const float top = (1.f + Pd / P) / (float)nt;
+#pragma unroll
+                    for (int i = 0; i < QMAX; ++i) {
+                        if (i >= q) { g[i] = 0.f; continue; }
+                        const float x = (Mx - li[i]) * inv_taum;
+                        const float dt = -dpareto2_f(x) / P + (li[i] == Mx ? top : 0.f);
+                        g[i] = ws * dt * dli[i];
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < QMAX; ++i)
+                if (i < q) dY[ls * q + i] = g[i];
+        }
+        __syncthreads();
+        for (int p = tid; p < q * D; p += kBsThreads) {
+            const int i = p / D, k = p % D;
+            if (k >= r + i + 1) continue;  // the upper part of br stays zero
+            float cs = 0.f;
+            for (int ls = 0; ls < sc; ++ls) cs = fmaf(dY[ls * q + i], z32[(int64_t)(s0 + ls) * D + k], cs);
+            dLq[p] += (double)cs;
+        }
+        for (int i = tid; i < q; i += kBsThreads) {
+            float cs = 0.f;
+            for (int ls = 0; ls < sc; ++ls) cs += dY[ls * q + i];
+            s_dmu[i] += (double)cs;
+        }
+        __syncthreads();
+    }
+    // (8) reverse through br = chol(M): gA = L^-T Phi(L^T dL) L^-1 (symmetric), float64
+    if (tid == 0) {
+        for (int i = 0; i < q; ++i) s_rd[i] = 1.0 / Lq[i * D + r + i];
+        for (int i = 0; i < q; ++i)
+            for (int j = 0; j < q; ++j) {
+                double acc2 = 0.0;
+                if (j <= i)
+                    for (int k = i; k < q; ++k) acc2 += Lq[k * D + r + i] * dLq[k * D + r + j];
+                scr[i * q + j] = acc2;
+            }
+        for (int i = 0; i < q; ++i)
+            for (int j = 0; j < q; ++j)
+                gA[i * q + j] = 0.5 * (j <= i ? scr[i * q + j] : scr[j * q + i]);
+        for (int c = 0; c < q; ++c)
+            for (int i = q - 1; i >= 0; --i) {
+                double acc2 = gA[i * q + c];
+                for (int k = i + 1; k < q; ++k) acc2 -= Lq[k * D + r + i] * gA[k * q + c];
+                gA[i * q + c] = acc2 * s_rd[i];
+            }
+        for (int row = 0; row < q; ++row)
+            for (int j = q - 1; j >= 0; --j) {
+                double acc2 = gA[row * q + j];
+                for (int k = j + 1; k < q; ++k) acc2 -= gA[row * q + k] * Lq[k * D + r + j];
+                gA[row * q + j] = acc2 * s_rd[j];
+            }
+    }
+    __syncthreads();
+    // (9) d bl += -2 gA bl;  dSigma_qb = d bl Lb^-1;  seeds in standardised units
+    for (int p = tid; p < q * r; p += kBsThreads) {
+        const int i = p / r, k = p % r;
+        double acc2 = dLq[i * D + k];
+        for (int j = 0; j < q; ++j) acc2 -= 2.0 * gA[i * q + j] * Lq[j * D + k];
+        scr[p] = acc2;
+    }
+    __syncthreads();
+    for (int p = tid; p < q * r; p += kBsThreads) dLq[(p / r) * D + (p % r)] = scr[p];
+    __syncthreads();
+    for (int p = tid; p < q * r; p += kBsThreads) {
+        const int i = p / r, kp = p % r;
+        double acc2 = 0.0;
+        for (int k = kp; k < r; ++k) acc2 += dLq[i * D + k] * a.Lb_inv[k * r + kp];
+        a.gqb[(bidx * q + i) * r + kp] = sy2 * acc2;
+    }
+    for (int p = tid; p < q * q; p += kBsThreads) a.gqq[bidx * q * q + p] = sy2 * gA[p];
+    for (int i = tid; i < q; i += kBsThreads) a.gmu[bidx * q + i] = sy * s_dmu[i];
+}
+
+__global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
+                                    const double* __restrict__ best_f, int S, int qei,
+                                    float* __restrict__ z32, float* __restrict__ bf32) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < nz) z32[idx] = (float)Z[idx];
+    if (idx < S) {
+        const double bf = best_f[qei ? 0 : idx];
+        const float h = (float)bf;
+        bf32[2 * idx] = h;
+        bf32[2 * idx + 1] = (float)(bf - (double)h);
+    }
 }
 
 // ---------------------------------------------------------------- mix_rows
@@ -1008,31 +1310,52 @@ int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc
     return BGB_OK;
 }
 
-size_t batch_step_smem_bytes(int q, int r, int S, bool mixed_backward) {
+size_t batch_step_smem_bytes(int q, int r, int S) {
     const int D = r + q;
-    size_t bytes = sizeof(double) * (size_t)(2 * q * D + 2 * q * q + 2 * q + S + kSampleChunk * q +
-                                             (q * q > q * r ? q * q : q * r));
-    if (mixed_backward) bytes += 2 * sizeof(float) * (size_t)S * q;
-    return bytes;
+    return sizeof(double) * (size_t)(2 * q * D + 2 * q * q + 2 * q + S + kSampleChunk * q +
+                                     (q * q > q * r ? q * q : q * r));
+}
+
+size_t batch_step_f32_smem_bytes(int q, int r, int S) {
+    const int D = r + q;
+    return sizeof(double) * (size_t)(2 * q * q + 2 * q * D + (q * q > q * r ? q * q : q * r)) +
+           sizeof(float) * (size_t)(q * D + S + kSampleChunk * q);
 }
 
 int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bool mixed) {
     if (a.b <= 0) return BGB_OK;
     if (a.q > kMaxQ) return BGB_ERR_UNSUPPORTED;
-    const bool mb = mixed && backward && a.acqf != BGB_ACQF_QEI;
-    size_t smem = batch_step_smem_bytes(a.q, a.r, a.S, mb);
-    if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
-    if (mixed) {
+    if (!mixed) {
+        const size_t smem = batch_step_smem_bytes(a.q, a.r, a.S);
+        if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
         if (smem > 48 * 1024)
-            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_kernel<true>,
+            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_kernel,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        batch_step_kernel<true><<<(unsigned)a.b, 128, smem, stream>>>(a, backward);
-    } else {
-        if (smem > 48 * 1024)
-            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_kernel<false>,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        batch_step_kernel<false><<<(unsigned)a.b, 128, smem, stream>>>(a, backward);
+        batch_step_kernel<<<(unsigned)a.b, 128, smem, stream>>>(a, backward);
+        BGB_CHECK_LAUNCH();
+        return BGB_OK;
     }
+    if (a.z32 == nullptr || a.bf32 == nullptr) return BGB_ERR_ARG;
+    const size_t smem = batch_step_f32_smem_bytes(a.q, a.r, a.S);
+    if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
+    const int64_t nz = (int64_t)a.S * (a.r + a.q);
+    const int64_t np = nz > a.S ? nz : a.S;
+    prep_samples_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, stream>>>(
+        a.Z, nz, a.best_f, a.S, a.acqf == BGB_ACQF_QEI, a.z32, a.bf32);
+    BGB_CHECK_LAUNCH();
+#define BGB_BS(QM)                                                                               \
+    do {                                                                                        \
+        if (smem > 48 * 1024)                                                                   \
+            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_f32_kernel<QM>,                        \
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                              (int)smem));                                      \
+        batch_step_f32_kernel<QM><<<(unsigned)a.b, kBsThreads, smem, stream>>>(a, backward);    \
+    } while (0)
+    if (a.q <= 4) BGB_BS(4);
+    else if (a.q <= 8) BGB_BS(8);
+    else if (a.q <= 16) BGB_BS(16);
+    else BGB_BS(32);
+#undef BGB_BS
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
