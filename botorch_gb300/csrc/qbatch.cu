@@ -245,6 +245,34 @@ __device__ __forceinline__ void add_pair(T& h, T& l, T bh, T bl) {
 
 constexpr int kQstatsThreads = 256;
 
+// outputscale * kappa between row `ri` of X and row `rj` of X (rj >= 0) or
+// baseline point `kb` (rj < 0). Float path (T = float with a.zt set): float32
+// over the scaled candidate coordinates a.zt, like the float32 kernel build;
+// otherwise float64.
+template <typename T>
+__device__ __forceinline__ double kernel_pair(const QBatchArgs& a, int64_t ri, int64_t rj, int kb) {
+    const int d = a.d;
+    if (sizeof(T) == 4 && a.zt != nullptr) {
+        const int64_t rows = a.b * a.q;
+        float r2 = 0.f;
+        for (int k = 0; k < d; ++k) {
+            const float zj = rj >= 0 ? a.zt[(int64_t)k * rows + rj]
+                                     : (float)(a.Xb[(int64_t)kb * d + k] * a.inv_ls[k]);
+            const float df = a.zt[(int64_t)k * rows + ri] - zj;
+            r2 = fmaf(df, df, r2);
+        }
+        return (double)((float)a.outputscale * kappa<float>(a.kernel, r2));
+    }
+    const double* xi = a.X + ri * d;
+    const double* xj = rj >= 0 ? a.X + rj * d : a.Xb + (int64_t)kb * d;
+    double r2 = 0.0;
+    for (int k = 0; k < d; ++k) {
+        const double df = (xi[k] - xj[k]) * a.inv_ls[k];
+        r2 = fma(df, df, r2);
+    }
+    return a.outputscale * kappa<double>(a.kernel, r2);
+}
+
 template <int NV>
 struct PadPow2 {
     static constexpr int value = NV <= 32 ? 32 : NV <= 64 ? 64 : 128;
@@ -347,20 +375,12 @@ __global__ void __launch_bounds__(kQstatsThreads) qstats_kernel(QBatchArgs a, co
     double tot = 0.0;
 #pragma unroll
     for (int w = 0; w < kQstatsThreads / 32; ++w) tot += red[w][tid];
-    const int d = a.d;
     if (tid < NG) {
         int i = 0;
         while ((i + 1) * (i + 2) / 2 <= tid) ++i;
         const int j = tid - i * (i + 1) / 2;
         if (i >= q) return;
-        const double* xi = a.X + (rbase + i) * d;
-        const double* xj = a.X + (rbase + j) * d;
-        double r2 = 0.0;
-        for (int k = 0; k < d; ++k) {
-            const double df = (xi[k] - xj[k]) * a.inv_ls[k];
-            r2 = fma(df, df, r2);
-        }
-        const double v = a.outputscale * kappa<double>(a.kernel, r2) - tot;
+        const double v = kernel_pair<T>(a, rbase + i, rbase + j, 0) - tot;
         a.sig[(bidx * q + i) * q + j] = v;
         a.sig[(bidx * q + j) * q + i] = v;
     } else if (tid < NG + QMAX) {
@@ -369,15 +389,8 @@ __global__ void __launch_bounds__(kQstatsThreads) qstats_kernel(QBatchArgs a, co
     } else {
         const int i = (tid - NG - QMAX) / RM, kb = (tid - NG - QMAX) % RM;
         if (i >= q || kb >= r) return;
-        const double* xi = a.X + (rbase + i) * d;
-        const double* xb = a.Xb + (int64_t)kb * d;
-        double r2 = 0.0;
-        for (int k = 0; k < d; ++k) {
-            const double df = (xi[k] - xb[k]) * a.inv_ls[k];
-            r2 = fma(df, df, r2);
-        }
         // P rounded to T as the two-kernel path stores it
-        a.sqb[(bidx * q + i) * r + kb] = a.outputscale * kappa<double>(a.kernel, r2) - (double)(T)tot;
+        a.sqb[(bidx * q + i) * r + kb] = kernel_pair<T>(a, rbase + i, -1, kb) - (double)(T)tot;
     }
 }
 
@@ -780,34 +793,41 @@ __device__ __forceinline__ void sample_u(const float* __restrict__ Lf, const flo
 }
 
 // psd_safe_cholesky of the q x q matrix M (float64, row-major) into scr: plain,
-// then jitter j * 10^t (t < max_tries) added to M's diagonal. Column pivots use
-// one reciprocal each. Returns 0, BGB_NOT_PSD or BGB_NAN.
-__device__ int psd_chol_rcp(double* M, double* scr, int q, int max_tries, double jitter) {
+// then jitter j * 10^t (t < max_tries) added to M's diagonal. Returns 0,
+// BGB_NOT_PSD or BGB_NAN. Run by the 32 lanes of one warp: each column step
+// computes its pivot in every lane (one reciprocal per column) and lane i
+// updates row i, which spreads the float64 work over the warp.
+__device__ int psd_chol_warp(double* M, double* scr, int q, int max_tries, double jitter, int lane) {
     bool has_nan = false;
-    for (int p = 0; p < q * q; ++p) has_nan |= isnan(M[p]);
-    if (has_nan) return BGB_NAN;
+    for (int p = lane; p < q * q; p += 32) has_nan |= isnan(M[p]);
+    if (__any_sync(0xffffffffu, has_nan)) return BGB_NAN;
     double jprev = 0.0;
     for (int t = -1; t < max_tries; ++t) {
         if (t >= 0) {
             const double jnew = jitter * pow(10.0, (double)t);
-            for (int i = 0; i < q; ++i) M[i * q + i] += jnew - jprev;
+            if (lane < q) M[lane * q + lane] += jnew - jprev;
             jprev = jnew;
+            __syncwarp();
         }
-        for (int p = 0; p < q * q; ++p) scr[p] = M[p];
+        for (int p = lane; p < q * q; p += 32) scr[p] = M[p];
+        __syncwarp();
         bool ok = true;
-        for (int j = 0; j < q && ok; ++j) {
+        for (int j = 0; j < q; ++j) {
             double v = scr[j * q + j];
             for (int k = 0; k < j; ++k) v -= scr[j * q + k] * scr[j * q + k];
             if (!(v > 0.0)) { ok = false; break; }
             const double djj = sqrt(v), rj = 1.0 / djj;
-            scr[j * q + j] = djj;
-            for (int i = j + 1; i < q; ++i) {
-                double s = scr[i * q + j];
-                for (int k = 0; k < j; ++k) s -= scr[i * q + k] * scr[j * q + k];
-                scr[i * q + j] = s * rj;
+            __syncwarp();
+            if (lane == j) scr[j * q + j] = djj;
+            if (lane > j && lane < q) {
+                double acc = scr[lane * q + j];
+                for (int k = 0; k < j; ++k) acc -= scr[lane * q + k] * scr[j * q + k];
+                scr[lane * q + j] = acc * rj;
+                scr[j * q + lane] = 0.0;
             }
-            for (int k = j + 1; k < q; ++k) scr[j * q + k] = 0.0;
+            __syncwarp();
         }
+        __syncwarp();
         if (ok) return 0;
     }
     return BGB_NOT_PSD;
@@ -877,12 +897,14 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
         M[p] -= acc;
     }
     __syncthreads();
-    // (4) br = psd_safe_cholesky(M) for this t-batch
-    if (tid == 0) {
-        const int st = psd_chol_rcp(M, scr, q, a.max_tries, a.jitter);
-        for (int i = 0; i < q; ++i)
-            for (int j = 0; j < q; ++j) Lq[i * D + r + j] = (j <= i) ? scr[i * q + j] : 0.0;
-        s_status = st;
+    // (4) br = psd_safe_cholesky(M) for this t-batch (warp 0)
+    if (warp == 0) {
+        const int st = psd_chol_warp(M, scr, q, a.max_tries, a.jitter, lane);
+        for (int p = lane; p < q * q; p += 32) {
+            const int i = p / q, j = p % q;
+            Lq[i * D + r + j] = (j <= i) ? scr[p] : 0.0;
+        }
+        if (lane == 0) s_status = st;
     }
     __syncthreads();
     if (s_status != 0) {
@@ -1041,31 +1063,41 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
         }
         __syncthreads();
     }
-    // (8) reverse through br = chol(M): gA = L^-T Phi(L^T dL) L^-1 (symmetric), float64
-    if (tid == 0) {
-        for (int i = 0; i < q; ++i) s_rd[i] = 1.0 / Lq[i * D + r + i];
-        for (int i = 0; i < q; ++i)
-            for (int j = 0; j < q; ++j) {
-                double acc2 = 0.0;
-                if (j <= i)
-                    for (int k = i; k < q; ++k) acc2 += Lq[k * D + r + i] * dLq[k * D + r + j];
-                scr[i * q + j] = acc2;
-            }
-        for (int i = 0; i < q; ++i)
-            for (int j = 0; j < q; ++j)
-                gA[i * q + j] = 0.5 * (j <= i ? scr[i * q + j] : scr[j * q + i]);
-        for (int c = 0; c < q; ++c)
+    // (8) reverse through br = chol(M): gA = L^-T Phi(L^T dL) L^-1 (symmetric),
+    // float64, warp 0: entries of L^T dL over the lanes, then one column (first
+    // solve) or one row (second solve) per lane.
+    if (warp == 0) {
+        if (lane < q) s_rd[lane] = 1.0 / Lq[lane * D + r + lane];
+        for (int p = lane; p < q * q; p += 32) {
+            const int i = p / q, j = p % q;
+            double acc2 = 0.0;
+            if (j <= i)
+                for (int k = i; k < q; ++k) acc2 += Lq[k * D + r + i] * dLq[k * D + r + j];
+            scr[p] = acc2;
+        }
+        __syncwarp();
+        for (int p = lane; p < q * q; p += 32) {
+            const int i = p / q, j = p % q;
+            gA[p] = 0.5 * (j <= i ? scr[i * q + j] : scr[j * q + i]);
+        }
+        __syncwarp();
+        if (lane < q) {
+            const int c = lane;
             for (int i = q - 1; i >= 0; --i) {
                 double acc2 = gA[i * q + c];
                 for (int k = i + 1; k < q; ++k) acc2 -= Lq[k * D + r + i] * gA[k * q + c];
                 gA[i * q + c] = acc2 * s_rd[i];
             }
-        for (int row = 0; row < q; ++row)
+        }
+        __syncwarp();
+        if (lane < q) {
+            const int row = lane;
             for (int j = q - 1; j >= 0; --j) {
                 double acc2 = gA[row * q + j];
                 for (int k = j + 1; k < q; ++k) acc2 -= gA[row * q + k] * Lq[k * D + r + j];
                 gA[row * q + j] = acc2 * s_rd[j];
             }
+        }
     }
     __syncthreads();
     // (9) d bl += -2 gA bl;  dSigma_qb = d bl Lb^-1;  seeds in standardised units
@@ -1103,9 +1135,27 @@ __global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
 
 // ---------------------------------------------------------------- mix_rows
 // H[row i of t-batch] = gmu_i beta - 2 sum_j Gqq[i,j] V[j,:] - sum_k Gqb[i,k] Vb[k,:]
-// (d value / d V through mu = V beta, Sigma_qq and Sigma_qb). One thread per
-// column of one t-batch; QM >= q bounds the register arrays.
-template <typename T, int QM>
+// (d value / d V through mu = V beta, Sigma_qq and Sigma_qb). Each thread owns
+// E consecutive columns of one t-batch (one 16-byte vector per row when the
+// layout allows, else E = 1), so every seed read from shared memory feeds E
+// columns; QM >= q bounds the register arrays.
+template <typename T>
+__device__ __forceinline__ void store_h(T* H, T* H_lo, int64_t off, T h) {
+    if constexpr (sizeof(T) == 4) {
+        if (H_lo != nullptr) {  // tf32 split for the tensor-core adjoint GEMM
+            uint32_t hb, lb;
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"((float)h));
+            const float hh = __uint_as_float(hb);
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"((float)h - hh));
+            H[off] = hh;
+            H_lo[off] = __uint_as_float(lb);
+            return;
+        }
+    }
+    H[off] = h;
+}
+
+template <typename T, int QM, int E>
 __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __restrict__ V,
                                                        int64_t ldv, const T* __restrict__ Vb,
                                                        const T* __restrict__ beta,
@@ -1121,32 +1171,91 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
     for (int p = threadIdx.x; p < q * r; p += blockDim.x) gqb[p] = (T)(-a.gqb[bidx * q * r + p]);
     for (int p = threadIdx.x; p < q; p += blockDim.x) gm[p] = (T)a.gmu[bidx * q + p];
     __syncthreads();
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    T v[QM];
+    const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * E;
+    if (c0 >= n) return;
+    using VT = typename Vec16<T>::type;
+    T v[QM][E], h[QM][E], bc[E];
 #pragma unroll
-    for (int j = 0; j < QM; ++j) v[j] = (j < q) ? V[(rbase + j) * ldv + c] : T(0);
-    const T bc = beta[c];
+    for (int j = 0; j < QM; ++j) {
+        if constexpr (E > 1) {
+            VT w;
+            if (j < q) w = *reinterpret_cast<const VT*>(V + (rbase + j) * ldv + c0);
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[j][e] = (j < q) ? Vec16<T>::at(w, e) : T(0);
+        } else {
+            v[j][0] = (j < q) ? V[(rbase + j) * ldv + c0] : T(0);
+        }
+    }
+    if constexpr (E > 1) {
+        const VT w = *reinterpret_cast<const VT*>(beta + c0);
+#pragma unroll
+        for (int e = 0; e < E; ++e) bc[e] = Vec16<T>::at(w, e);
+    } else {
+        bc[0] = beta[c0];
+    }
+#pragma unroll
+    for (int i = 0; i < QM; ++i) {
+        const T gmi = (i < q) ? gm[i] : T(0);
+#pragma unroll
+        for (int e = 0; e < E; ++e) h[i][e] = gmi * bc[e];
+#pragma unroll
+        for (int j = 0; j < QM; ++j) {
+            if (i < q && j < q) {
+                const T gij = gq[i * q + j];
+#pragma unroll
+                for (int e = 0; e < E; ++e) h[i][e] = fma(gij, v[j][e], h[i][e]);
+            }
+        }
+    }
+    for (int k = 0; k < r; ++k) {
+        T vb[E];
+        if constexpr (E > 1) {
+            const VT w = *reinterpret_cast<const VT*>(Vb + (int64_t)k * n + c0);
+#pragma unroll
+            for (int e = 0; e < E; ++e) vb[e] = Vec16<T>::at(w, e);
+        } else {
+            vb[0] = Vb[(int64_t)k * n + c0];
+        }
+#pragma unroll
+        for (int i = 0; i < QM; ++i) {
+            if (i < q) {
+                const T gik = gqb[i * r + k];
+#pragma unroll
+                for (int e = 0; e < E; ++e) h[i][e] = fma(gik, vb[e], h[i][e]);
+            }
+        }
+    }
 #pragma unroll
     for (int i = 0; i < QM; ++i) {
         if (i >= q) break;
-        T h = gm[i] * bc;
+        const int64_t off = (rbase + i) * ldh + c0;
+        if constexpr (E > 1 && sizeof(T) == 4) {
+            if (H_lo != nullptr) {
+                float4 hh, ll;
+                float* ph = &hh.x;
+                float* pl = &ll.x;
 #pragma unroll
-        for (int j = 0; j < QM; ++j)
-            if (j < q) h = fma(gq[i * q + j], v[j], h);
-        for (int k = 0; k < r; ++k) h = fma(gqb[i * r + k], Vb[(int64_t)k * n + c], h);
-        if constexpr (sizeof(T) == 4) {
-            if (H_lo != nullptr) {  // tf32 split for the tensor-core adjoint GEMM
-                uint32_t hb, lb;
-                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"((float)h));
-                const float hh = __uint_as_float(hb);
-                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"((float)h - hh));
-                H[(rbase + i) * ldh + c] = hh;
-                H_lo[(rbase + i) * ldh + c] = __uint_as_float(lb);
+                for (int e = 0; e < E; ++e) {
+                    uint32_t hb, lb;
+                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"((float)h[i][e]));
+                    ph[e] = __uint_as_float(hb);
+                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"((float)h[i][e] - ph[e]));
+                    pl[e] = __uint_as_float(lb);
+                }
+                *reinterpret_cast<float4*>(H + off) = hh;
+                *reinterpret_cast<float4*>(H_lo + off) = ll;
                 continue;
             }
         }
-        H[(rbase + i) * ldh + c] = h;
+        if constexpr (E > 1) {
+            VT o;
+            T* po = reinterpret_cast<T*>(&o);
+#pragma unroll
+            for (int e = 0; e < E; ++e) po[e] = h[i][e];
+            *reinterpret_cast<VT*>(H + off) = o;
+        } else {
+            store_h<T>(H, H_lo, off, h[i][0]);
+        }
     }
 }
 
@@ -1164,33 +1273,45 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
 constexpr int kAdjRows = 128;
 constexpr int kAdjChunk = 64;
 
-// K(X, X) and K(X, Xb) terms of the gradient (float64), then the chain rule
-// through the scaled coordinates; writes grad[row, :].
-template <int DMAX>
-__device__ __forceinline__ void adjoint_finish_row(const QBatchArgs& a, int64_t row, double* gx) {
+// K(X, X) and K(X, Xb) terms of the gradient, then the chain rule through the
+// scaled coordinates; writes grad[row, :]. Arithmetic in T: float64 for the
+// float64 path; float32 for the mixed one, whose coordinates come scaled from
+// a.zt (candidates) like the rest of its float32 kernel algebra.
+template <typename T, int DMAX>
+__device__ __forceinline__ void adjoint_finish_row(const QBatchArgs& a, int64_t row, T* gx) {
     const int q = a.q, r = a.r, d = a.d, kind = a.kernel;
+    const int64_t rows = a.b * q;
     const int64_t bidx = row / q;
     const int i = (int)(row % q);
     if (a.dev_err != nullptr && *a.dev_err != 0 && i == 0) a.status[bidx] = BGB_DEVICE_TIMEOUT;
     const int64_t rbase = bidx * q;
+    const bool zs = (sizeof(T) == 4) && a.zt != nullptr;
+    T zi[DMAX];
+#pragma unroll
+    for (int k = 0; k < DMAX; ++k)
+        zi[k] = (k < d) ? (zs ? (T)a.zt[(int64_t)k * rows + row] : (T)(a.X[row * d + k] * a.inv_ls[k])) : T(0);
     for (int j = 0; j < q + r; ++j) {
         if (j == i) continue;
-        const double* y = (j < q) ? a.X + (rbase + j) * d : a.Xb + (int64_t)(j - q) * d;
-        const double w = (j < q) ? 2.0 * a.gqq[(bidx * q + i) * q + j] : a.gqb[(bidx * q + i) * r + (j - q)];
-        double dfx[DMAX];
-        double r2 = 0.0;
+        const T w = (T)((j < q) ? 2.0 * a.gqq[(bidx * q + i) * q + j] : a.gqb[(bidx * q + i) * r + (j - q)]);
+        T dfx[DMAX];
+        T r2 = T(0);
 #pragma unroll
         for (int k = 0; k < DMAX; ++k) {
-            dfx[k] = (k < d) ? (a.X[row * d + k] - y[k]) * a.inv_ls[k] : 0.0;
-            r2 += dfx[k] * dfx[k];
+            T zj = T(0);
+            if (k < d) {
+                if (j < q) zj = zs ? (T)a.zt[(int64_t)k * rows + rbase + j] : (T)(a.X[(rbase + j) * d + k] * a.inv_ls[k]);
+                else zj = (T)(a.Xb[(int64_t)(j - q) * d + k] * a.inv_ls[k]);
+            }
+            dfx[k] = zi[k] - zj;
+            r2 = fma(dfx[k], dfx[k], r2);
         }
-        const double coef = w * dkappa_dr2<double>(kind, r2);
+        const T coef = w * dkappa_dr2<T>(kind, r2);
 #pragma unroll
-        for (int k = 0; k < DMAX; ++k) gx[k] += coef * dfx[k];
+        for (int k = 0; k < DMAX; ++k) gx[k] = fma(coef, dfx[k], gx[k]);
     }
 #pragma unroll
     for (int k = 0; k < DMAX; ++k)
-        if (k < d) a.grad[row * d + k] = 2.0 * a.outputscale * a.inv_ls[k] * gx[k];
+        if (k < d) a.grad[row * d + k] = 2.0 * a.outputscale * a.inv_ls[k] * (double)gx[k];
 }
 
 template <typename T, int DMAX, bool FINISH>
@@ -1213,9 +1334,12 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
     const int64_t cbeg = (int64_t)blockIdx.y * slab;
     const int64_t cend = (cbeg + slab < n) ? cbeg + slab : n;
     T zx[DMAX], g[DMAX];
+    const bool zs = (sizeof(T) == 4) && a.zt != nullptr;
 #pragma unroll
     for (int k = 0; k < DMAX; ++k) {
-        zx[k] = (active && k < d) ? (T)(a.X[row * d + k] * a.inv_ls[k]) : T(0);
+        zx[k] = (active && k < d)
+                    ? (zs ? (T)a.zt[(int64_t)k * rows + row] : (T)(a.X[row * d + k] * a.inv_ls[k]))
+                    : T(0);
         g[k] = T(0);
     }
     for (int64_t c0 = cbeg; c0 < cend; c0 += kAdjChunk) {
@@ -1253,10 +1377,7 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
     }
     if (!active) return;
     if constexpr (FINISH) {
-        double gx[DMAX];
-#pragma unroll
-        for (int k = 0; k < DMAX; ++k) gx[k] = (double)g[k];
-        adjoint_finish_row<DMAX>(a, row, gx);
+        adjoint_finish_row<T, DMAX>(a, row, g);
         return;
     }
     if constexpr (!FINISH) {
@@ -1274,16 +1395,18 @@ __global__ void __launch_bounds__(128) adjoint_finalize_kernel(QBatchArgs a, con
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= rows) return;
     const int d = a.d;
-    double gx[DMAX];
+    T gx[DMAX], gc[DMAX];  // compensated sum over the slabs
 #pragma unroll
-    for (int k = 0; k < DMAX; ++k) gx[k] = 0.0;
+    for (int k = 0; k < DMAX; ++k) { gx[k] = T(0); gc[k] = T(0); }
     for (int s = 0; s < nslab; ++s) {
         const T* pp = part + (int64_t)s * d * rows;
 #pragma unroll
         for (int k = 0; k < DMAX; ++k)
-            if (k < d) gx[k] += (double)pp[(int64_t)k * rows + row];
+            if (k < d) comp_add<T>(gx[k], gc[k], pp[(int64_t)k * rows + row]);
     }
-    adjoint_finish_row<DMAX>(a, row, gx);
+#pragma unroll
+    for (int k = 0; k < DMAX; ++k) gx[k] -= gc[k];
+    adjoint_finish_row<T, DMAX>(a, row, gx);
 }
 
 __global__ void posterior_out_kernel(QBatchArgs a, double* mean, double* covar) {
@@ -1399,12 +1522,26 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
     if (a.q > kMaxQ) return BGB_ERR_UNSUPPORTED;
     const size_t smem = sizeof(T) * (size_t)(a.q * a.q + a.q * a.r + a.q);
     if (smem > 48 * 1024) return BGB_ERR_UNSUPPORTED;
-    dim3 grid((unsigned)ceil_div(a.n, 256), (unsigned)a.b);
     const int64_t ld = ldh > 0 ? ldh : a.n;
-    if (a.q <= 4) mix_rows_kernel<T, 4><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld);
-    else if (a.q <= 8) mix_rows_kernel<T, 8><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld);
-    else if (a.q <= 16) mix_rows_kernel<T, 16><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld);
-    else mix_rows_kernel<T, 32><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld);
+    constexpr int E = Vec16<T>::E;
+    auto al = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) % 16) == 0; };
+    const bool vec = (a.n % E == 0) && (ldv % E == 0) && (ld % E == 0) && al(V) && al(beta) &&
+                     al(H) && (H_lo == nullptr || al(H_lo)) && (a.r == 0 || al(Vb));
+#define BGB_MIX(QM)                                                                              \
+    do {                                                                                        \
+        if (vec) {                                                                              \
+            dim3 grid((unsigned)ceil_div(a.n, 256 * E), (unsigned)a.b);                         \
+            mix_rows_kernel<T, QM, E><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld); \
+        } else {                                                                                \
+            dim3 grid((unsigned)ceil_div(a.n, 256), (unsigned)a.b);                             \
+            mix_rows_kernel<T, QM, 1><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld); \
+        }                                                                                       \
+    } while (0)
+    if (a.q <= 4) BGB_MIX(4);
+    else if (a.q <= 8) BGB_MIX(8);
+    else if (a.q <= 16) BGB_MIX(16);
+    else BGB_MIX(32);
+#undef BGB_MIX
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
