@@ -338,11 +338,12 @@ def run_ours(args) -> None:
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "evals/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(total_ms / args.steps, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16-split+f32+f64",
         "data": "synthetic (seeded Branin-sum GP workload)",
         "config": {"workload": WORKLOAD, "n": N_TRAIN, "d": DIM, "q": Q, "mc_samples": S,
                    "batch_per_call": b, "baseline_points_r": acqf.r, "kernel": "matern52",
-                   "precision": "mixed: f32 kernel build, 3xTF32 cross-covariance GEMMs, f64 q x q "
+                   "precision": "mixed: f32 kernel build, cross-covariance GEMMs on scaled f16 hi/lo "
+                                "splits (3 tcgen05 products, f32 accumulation), f64 q x q "
                                 "Cholesky + adjoint, f32 samples from exact f32 pairs of mu - best_f, "
                                 "f64 accumulations", "l2": "flushed before each step (256 MB write)",
                    "parallelism": f"replicas, weak scaling over t-batches x{world}"},

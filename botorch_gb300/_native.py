@@ -57,7 +57,8 @@ class BgbAcq(ctypes.Structure):
                 ("B32", c_vp), ("Linv64", c_vp), ("Linv32", c_vp), ("Vb64", c_vp), ("Vb32", c_vp),
                 ("VbT64", c_vp), ("VbT32", c_vp), ("beta64", c_vp), ("beta32", c_vp),
                 ("Xs64", c_vp), ("Xs32", c_vp),
-                ("Lhi", c_vp), ("Llo", c_vp), ("LThi", c_vp), ("LTlo", c_vp), ("ldl", c_i64),
+                ("Lhi", c_vp), ("Llo", c_vp), ("LThi", c_vp), ("LTlo", c_vp), ("Lmul", c_vp),
+                ("LTmul", c_vp), ("ldl", c_i64), ("beta_absmax", c_f64),
                 ("X_baseline", c_vp), ("Lb_inv", c_vp),
                 ("Z", c_vp), ("best_f", c_vp), ("tau_relu", c_f64), ("tau_max", c_f64)]
 
@@ -78,9 +79,10 @@ _SIGNATURES = {
     "bgb_gp_operands": (c_i32, [ctypes.POINTER(BgbGP), c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp,
                                 c_vp, c_vp, c_vp]),
     "bgb_gp_tc_operands": (c_i32, [ctypes.POINTER(BgbGP), c_vp, c_i64, c_vp, c_vp, c_vp, c_vp,
-                                   c_vp]),
-    "bgb_crosscov_gemm_tf32x3": (c_i32, [c_i64, c_i64, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64,
-                                         c_vp, c_i64, c_i32, c_vp, c_vp]),
+                                   c_vp, c_vp, c_vp]),
+    "bgb_crosscov_gemm_f16x3": (c_i32, [c_i64, c_i64, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64,
+                                        c_vp, c_i64, c_vp, ctypes.c_float, c_vp, c_i32, c_vp,
+                                        c_vp]),
     "bgb_baseline_operands": (c_i32, [ctypes.POINTER(BgbGP), c_vp, c_vp, c_i32, c_vp, c_vp, c_vp,
                                       c_vp, c_vp, c_size, c_vp]),
     "bgb_baseline_operands_workspace_bytes": (c_size, [c_i64, c_i32]),

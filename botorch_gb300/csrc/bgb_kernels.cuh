@@ -1,5 +1,6 @@
 // Internal launchers shared between the translation units of the library.
 #pragma once
+#include <cuda_fp16.h>
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -7,18 +8,18 @@
 namespace bgb {
 
 // kernel_build.cu
-// K_lo non-null (float32 output only): write the tf32 hi/lo split (K = hi).
 template <typename TIn, typename TAcc, typename TOut>
 int launch_kernel_matrix(const TIn* X1, int64_t m, const TIn* X2, int64_t n2, int d,
                          const double* inv_ls, double outputscale, int kind, double diag_add,
-                         int same, TOut* K, int64_t ldk, cudaStream_t stream,
-                         TOut* K_lo = nullptr);
+                         int same, TOut* K, int64_t ldk, cudaStream_t stream);
 // Float32 form over coordinates already scaled by 1 / lengthscale, both k-major
-// (Z1T: d x m with leading dimension ldz1, Z2T: d x n2 with ldz2). Same tile
-// arithmetic as the float instantiation above, without rescaling per tile.
+// (Z1T: d x m with leading dimension ldz1, Z2T: d x n2 with ldz2), without
+// rescaling per tile. Output: K (float32), or with K16 set the float16 split
+// of k16_scale * K into K16 / K16_lo; leading dimension ldk either way.
 int launch_kernel_matrix_zt(const float* Z1T, int64_t ldz1, int64_t m, const float* Z2T,
                             int64_t ldz2, int64_t n2, int d, double outputscale, int kind,
-                            float* K, int64_t ldk, cudaStream_t stream, float* K_lo = nullptr);
+                            float* K, __half* K16, __half* K16_lo, float k16_scale, int64_t ldk,
+                            cudaStream_t stream);
 
 // dense_f64.cu ------------------------------------------------------------
 // k-range modes of the GEMMs (structure of triangular operands):
@@ -59,15 +60,20 @@ int transpose_f64(const double* src, int64_t rows, int64_t cols, int64_t lds, do
 
 // crosscov_tc.cu ------------------------------------------------------------
 bool tc_gemm_available();
-// C = A op(B) on tcgen05 tensor cores, 3xTF32. A: hi/lo (M x K, lda); B given by its
-// K-major storage Bs (N x K, hi/lo, ldbs), op(B)[k][j] = Bs[j][k]; kmode KB_UPPER/KB_LOWER.
-// err: device int set non-zero when a bounded wait expired.
-int tc_gemm_tf32x3(int64_t M, int64_t N, int64_t K, const float* A_hi, const float* A_lo,
-                   int64_t lda, const float* B_hi, const float* B_lo, int64_t ldbs, float* C,
-                   int64_t ldc, int kmode, int* err, cudaStream_t stream);
-int split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, float* hi, float* lo,
-               int64_t ldd, cudaStream_t stream);
-int split_f64_tf32(const double* src, int64_t rows, int64_t cols, int64_t lds, int transpose,
-                   float* hi, float* lo, int64_t ldd, cudaStream_t stream);
+// C = diag(row_mul) A op(B) diag(col_mul) on tcgen05 tensor cores from float16
+// hi/lo splits (ah*bh + ah*bl + al*bh, float32 accumulation). A: hi/lo (M x K,
+// lda); B given by its K-major storage Bs (N x K, hi/lo, ldbs), op(B)[k][j] =
+// Bs[j][k]; row_mul nullptr: row_mul_const for every row; kmode KB_UPPER /
+// KB_LOWER / KFULL. err: device int set non-zero when a bounded wait expired.
+int tc_gemm_f16x3(int64_t M, int64_t N, int64_t K, const __half* A_hi, const __half* A_lo,
+                  int64_t lda, const __half* B_hi, const __half* B_lo, int64_t ldbs, float* C,
+                  int64_t ldc, int kmode, const float* row_mul, float row_mul_const,
+                  const float* col_mul, int* err, cudaStream_t stream);
+// Row-scaled float16 split of a float64 matrix (or of its transpose): per
+// storage row i a power-of-two s_i bringing max |x_i.| to at most 2^14,
+// hi = f16(s_i x), lo = f16(s_i x - hi) (ldd-strided rows, columns >= cols
+// zero), mul[i] = 1 / s_i.
+int split_f64_f16(const double* src, int64_t rows, int64_t cols, int64_t lds, int transpose,
+                  __half* hi, __half* lo, int64_t ldd, float* mul, cudaStream_t stream);
 
 }  // namespace bgb

@@ -1,6 +1,7 @@
 // Arguments of the per-t-batch kernels (device pointers, float64 unless noted).
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -40,6 +41,8 @@ struct QBatchArgs {
     float* zt;              // mixed: candidates scaled by 1 / lengthscale, d x (b*q), k-major
     float* z32;             // mixed: Z in float32 (S x (r+q))
     float* bf32;            // mixed: best_f per sample as float (hi, lo) pairs (S x 2)
+    double beta_absmax;     // max |beta| (row-scale bound of the float16 adjoint operand)
+    float* hmul;            // tensor cores: b*q inverse row scales of the float16 H
 };
 
 // mu, Sigma_qq and Sigma_qb in one pass over V (q <= 8, r <= 4); returns
@@ -62,7 +65,8 @@ size_t batch_step_smem_bytes(int q, int r, int S);
 // H_lo non-null (float32): write the tf32 hi/lo split (H = hi) with leading dimension ldh.
 template <typename T>
 int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, const T* beta, T* H,
-                    cudaStream_t stream, T* H_lo = nullptr, int64_t ldh = 0);
+                    cudaStream_t stream, __half* H16 = nullptr, __half* H16_lo = nullptr,
+                    int64_t ldh = 0);
 // d value / d X from D (b*q x n) = H L^-1; XsT: training inputs scaled by 1 / lengthscale,
 // d x n (k-major). part: scratch of part_cap elements for per-slab partial
 // gradients (nullptr / 0: a single slab, no finalize pass).

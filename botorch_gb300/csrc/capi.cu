@@ -3,6 +3,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <cmath>
 #include <mutex>
 
 #include "bgb_common.cuh"
@@ -69,16 +70,24 @@ int valid_gp(const bgb_gp_t* gp) {
     return 1;
 }
 
-// The mixed path runs its GEMMs on the tensor cores when the tf32 operands are set.
+// The mixed path runs its GEMMs on the tensor cores when the float16 operands are set.
 bool use_tc(const bgb_acq_t* a) {
     return a->precision == BGB_PREC_MIXED && !(a->flags & BGB_FLAG_SIMT) && a->Lhi != nullptr &&
-           a->Llo != nullptr && a->LThi != nullptr && a->LTlo != nullptr && a->ldl >= a->gp.n &&
-           (a->ldl % 8) == 0 && (a->ldb % 4) == 0 && tc_gemm_available();
+           a->Llo != nullptr && a->LThi != nullptr && a->LTlo != nullptr && a->Lmul != nullptr &&
+           a->LTmul != nullptr && a->ldl >= a->gp.n && (a->ldl % 8) == 0 && (a->ldb % 4) == 0 &&
+           tc_gemm_available();
 }
 
-// Workspace of one call: Kc (later H) rows x n (tensor-core path: hi and lo,
-// rows x ldl each), C = V (later D) rows x ldb, P rows x r, the float64
-// per-batch blocks and the device error word.
+// Elements (of the path's float type) of the Kc / H region: rows x n, or on the
+// tensor cores the float16 hi and lo halves, rows x ldl each (= rows x ldl floats).
+int64_t kc_region_elems(const bgb_acq_t* a, int64_t rows) {
+    return use_tc(a) ? rows * a->ldl : rows * a->gp.n;
+}
+
+// Workspace of one call: the Kc (later H, later the adjoint's slab partials)
+// region, C = V (later D) rows x ldb, P rows x r, the float64 per-batch blocks,
+// the device error word, and for the mixed path the scaled candidates, the
+// float32 base samples and best_f pairs, and (tensor cores) H's row multipliers.
 size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, void** Kc,
                      void** C, void** P, int** err = nullptr) {
     const int64_t n = a->gp.n;
@@ -86,7 +95,7 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
     const int64_t rr = a->r > 0 ? a->r : 1;
     const size_t es = (a->precision == BGB_PREC_MIXED) ? sizeof(float) : sizeof(double);
     const bool tc = use_tc(a);
-    const int64_t kc_elems = tc ? 2 * rows * a->ldl : rows * n;
+    const int64_t kc_elems = kc_region_elems(a, rows);
     size_t total = 0;
     total += align_up(kc_elems * es);
     total += align_up(rows * a->ldb * es);
@@ -99,6 +108,7 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
         total += align_up(sizeof(float) * rows * a->gp.d);
         total += align_up(sizeof(float) * (size_t)a->n_samples * (a->r + a->q));
         total += align_up(sizeof(float) * 2 * (size_t)a->n_samples);
+        if (tc) total += align_up(sizeof(float) * rows);
     }
     if (ar == nullptr) return total;
     if (ar->cap < total) return 0;
@@ -123,6 +133,7 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
         qa->zt = ar->take<float>(rows * a->gp.d);
         qa->z32 = ar->take<float>((int64_t)a->n_samples * (a->r + a->q));
         qa->bf32 = ar->take<float>(2 * (int64_t)a->n_samples);
+        if (tc) qa->hmul = ar->take<float>(rows);
     }
     return total;
 }
@@ -151,6 +162,7 @@ void fill_qargs(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa) 
     qa->Lb_inv = a->Lb_inv;
     qa->Z = a->Z;
     qa->best_f = a->best_f;
+    qa->beta_absmax = a->beta_absmax;
 }
 
 int valid_acq(const bgb_acq_t* a) {
@@ -189,13 +201,14 @@ template <> struct Ops<float> {
     // K(X, Xt) in float32 from the scaled coordinates (zt: d x rows, Xs32: d x n);
     // K_lo non-null: the tf32 hi / lo split with leading dimension ldk
     static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, float* zt, float* K,
-                    int64_t ldk, float* K_lo, cudaStream_t st) {
+                    int64_t ldk, __half* K16, __half* K16_lo, float k16_scale, cudaStream_t st) {
         const int64_t tot = rows * a->gp.d;
         scale_rows_t_kernel<<<(unsigned)ceil_div(tot, 256), 256, 0, st>>>(
             X, rows, a->gp.d, a->gp.inv_lengthscale, zt);
         BGB_CHECK_LAUNCH();
         return launch_kernel_matrix_zt(zt, rows, rows, a->Xs32, a->gp.n, a->gp.n, a->gp.d,
-                                       a->gp.outputscale, a->gp.kernel, K, ldk, st, K_lo);
+                                       a->gp.outputscale, a->gp.kernel, K, K16, K16_lo, k16_scale,
+                                       ldk, st);
     }
 };
 template <> struct Ops<double> {
@@ -212,12 +225,22 @@ template <> struct Ops<double> {
                         n_tri);
     }
     static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, float* /*zt*/, double* K,
-                    int64_t ldk, double* /*K_lo*/, cudaStream_t st) {
+                    int64_t ldk, __half* /*K16*/, __half* /*K16_lo*/, float /*k16_scale*/,
+                    cudaStream_t st) {
         return launch_kernel_matrix<double, double, double>(
             X, rows, a->gp.train_X, a->gp.n, a->gp.d, a->gp.inv_lengthscale, a->gp.outputscale,
             a->gp.kernel, 0.0, 0, K, ldk, st);
     }
 };
+
+// Power of two s with outputscale * s <= 2^14: the float16 scale of K(X, Xt),
+// whose entries are at most outputscale.
+float kc_scale(double outputscale) {
+    if (!(outputscale > 0.0) || std::isinf(outputscale)) return 1.f;
+    int e;
+    frexp(outputscale, &e);
+    return ldexpf(1.f, 14 - e);
+}
 
 // Kernel build, V = K(X,Xt) L^-T, mu = m + V beta and P = V Vb^T, covariance reduction.
 template <typename T>
@@ -228,19 +251,21 @@ int run_front(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa, T*
     int rc;
     if constexpr (sizeof(T) == 4) {
         if (use_tc(a)) {
-            // tensor cores: K(X, Xt) as its tf32 split, then V = K L^-T
-            float* Khi = Kc;
-            float* Klo = Kc + rows * a->ldl;
-            rc = Ops<float>::kmat(a, X, rows, qa->zt, Khi, a->ldl, Klo, st);
+            // tensor cores: K(X, Xt) as its scaled float16 split, then V = K L^-T
+            __half* Khi = reinterpret_cast<__half*>(Kc);
+            __half* Klo = Khi + rows * a->ldl;
+            const float ks = kc_scale(a->gp.outputscale);
+            rc = Ops<float>::kmat(a, X, rows, qa->zt, nullptr, a->ldl, Khi, Klo, ks, st);
             if (rc) return rc;
             if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[1], st));
-            rc = tc_gemm_tf32x3(rows, n, n, Khi, Klo, a->ldl, a->Lhi, a->Llo, a->ldl, C, a->ldb,
-                                KB_UPPER, const_cast<int*>(qa->dev_err), st);
+            rc = tc_gemm_f16x3(rows, n, n, Khi, Klo, a->ldl, reinterpret_cast<const __half*>(a->Lhi),
+                               reinterpret_cast<const __half*>(a->Llo), a->ldl, C, a->ldb, KB_UPPER,
+                               nullptr, 1.f / ks, a->Lmul, const_cast<int*>(qa->dev_err), st);
             if (rc) return rc;
             goto after_gemm;
         }
     }
-    rc = Ops<T>::kmat(a, X, rows, qa->zt, Kc, n, nullptr, st);
+    rc = Ops<T>::kmat(a, X, rows, qa->zt, Kc, n, nullptr, nullptr, 0.f, st);
     if (rc) return rc;
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[1], st));
     rc = Ops<T>::gemm(rows, n, n, Kc, n, Ops<T>::B(a), a->ldb, C, a->ldb, KB_UPPER, n, st);
@@ -278,13 +303,17 @@ int run_call(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs& qa, T* 
     bool tc = false;
     if constexpr (sizeof(T) == 4) tc = use_tc(a);
     if (tc) {
-        T* Hlo = Kc + rows * a->ldl;
-        rc = launch_mix_rows<T>(qa, C, a->ldb, Ops<T>::Vb(a), Ops<T>::beta(a), H, st, Hlo, a->ldl);
+        __half* Hhi = reinterpret_cast<__half*>(Kc);
+        __half* Hlo = Hhi + rows * a->ldl;
+        rc = launch_mix_rows<T>(qa, C, a->ldb, Ops<T>::Vb(a), Ops<T>::beta(a), nullptr, st, Hhi,
+                                Hlo, a->ldl);
         if (rc) return rc;
         if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[5], st));
         if constexpr (sizeof(T) == 4) {
-            rc = tc_gemm_tf32x3(rows, n, n, H, Hlo, a->ldl, a->LThi, a->LTlo, a->ldl, C, a->ldb,
-                                KB_LOWER, const_cast<int*>(qa.dev_err), st);
+            rc = tc_gemm_f16x3(rows, n, n, Hhi, Hlo, a->ldl,
+                               reinterpret_cast<const __half*>(a->LThi),
+                               reinterpret_cast<const __half*>(a->LTlo), a->ldl, C, a->ldb, KB_LOWER,
+                               qa.hmul, 1.f, a->LTmul, const_cast<int*>(qa.dev_err), st);
             if (rc) return rc;
         }
     } else {
@@ -296,7 +325,7 @@ int run_call(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs& qa, T* 
     }
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[6], st));
     // the Kc / H region is free once the adjoint GEMM has read H: slab partials go there
-    const int64_t kc_elems = tc ? 2 * rows * a->ldl : rows * n;
+    const int64_t kc_elems = kc_region_elems(a, rows);
     rc = launch_adjoint<T>(qa, C, a->ldb, Ops<T>::Xs(a), Kc, kc_elems, st);
     if (rc) return rc;
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[7], st));
@@ -512,31 +541,38 @@ int bgb_gp_operands(const bgb_gp_t* gp, const double* Linv, const double* beta, 
     return BGB_OK;
 }
 
-int bgb_gp_tc_operands(const bgb_gp_t* gp, const double* Linv, int64_t ldl, float* Lhi,
-                       float* Llo, float* LThi, float* LTlo, void* stream) {
+int bgb_gp_tc_operands(const bgb_gp_t* gp, const double* Linv, int64_t ldl, uint16_t* Lhi,
+                       uint16_t* Llo, uint16_t* LThi, uint16_t* LTlo, float* Lmul, float* LTmul,
+                       void* stream) {
     if (!valid_gp(gp) || Linv == nullptr || Lhi == nullptr || Llo == nullptr || LThi == nullptr ||
-        LTlo == nullptr)
+        LTlo == nullptr || Lmul == nullptr || LTmul == nullptr)
         return BGB_ERR_ARG;
     const int64_t n = gp->n;
     if (ldl < n || (ldl % 8) != 0) return BGB_ERR_ARG;
     cudaStream_t st = as_stream(stream);
-    int rc = split_f64_tf32(Linv, n, n, n, 0, Lhi, Llo, ldl, st);
+    int rc = split_f64_f16(Linv, n, n, n, 0, reinterpret_cast<__half*>(Lhi),
+                           reinterpret_cast<__half*>(Llo), ldl, Lmul, st);
     if (rc) return rc;
-    return split_f64_tf32(Linv, n, n, n, 1, LThi, LTlo, ldl, st);
+    return split_f64_f16(Linv, n, n, n, 1, reinterpret_cast<__half*>(LThi),
+                         reinterpret_cast<__half*>(LTlo), ldl, LTmul, st);
 }
 
-int bgb_crosscov_gemm_tf32x3(int64_t M, int64_t N, int64_t K, const float* A_hi,
-                             const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
-                             int64_t ldbs, float* C, int64_t ldc, int32_t kmode, int32_t* err_dev,
-                             void* stream) {
+int bgb_crosscov_gemm_f16x3(int64_t M, int64_t N, int64_t K, const uint16_t* A_hi,
+                            const uint16_t* A_lo, int64_t lda, const uint16_t* B_hi,
+                            const uint16_t* B_lo, int64_t ldbs, float* C, int64_t ldc,
+                            const float* row_mul, float row_mul_const, const float* col_mul,
+                            int32_t kmode, int32_t* err_dev, void* stream) {
     if (M < 0 || N < 0 || K <= 0 || A_hi == nullptr || A_lo == nullptr || B_hi == nullptr ||
-        B_lo == nullptr || C == nullptr || (lda % 4) || (ldbs % 4) || (ldc % 4) || lda < K ||
-        ldbs < K || ldc < N)
+        B_lo == nullptr || C == nullptr || col_mul == nullptr || (lda % 8) || (ldbs % 8) ||
+        (ldc % 4) || lda < K || ldbs < K || ldc < N)
         return BGB_ERR_ARG;
     if (kmode != KB_UPPER && kmode != KB_LOWER && kmode != KFULL) return BGB_ERR_ARG;
     if (!tc_gemm_available()) return BGB_ERR_UNSUPPORTED;
-    return tc_gemm_tf32x3(M, N, K, A_hi, A_lo, lda, B_hi, B_lo, ldbs, C, ldc, kmode, err_dev,
-                          as_stream(stream));
+    return tc_gemm_f16x3(M, N, K, reinterpret_cast<const __half*>(A_hi),
+                         reinterpret_cast<const __half*>(A_lo), lda,
+                         reinterpret_cast<const __half*>(B_hi), reinterpret_cast<const __half*>(B_lo),
+                         ldbs, C, ldc, kmode, row_mul, row_mul_const, col_mul, err_dev,
+                         as_stream(stream));
 }
 
 size_t bgb_baseline_operands_workspace_bytes(int64_t n, int32_t r) {

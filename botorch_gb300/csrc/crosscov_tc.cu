@@ -1,7 +1,13 @@
-// (c) Cross-covariance GEMMs on the 5th-generation tensor cores: tcgen05.mma with
-// TMEM accumulators, operands staged by TMA (cp.async.bulk.tensor, 128-byte
-// swizzle), float32 accuracy from the 3xTF32 split a*b ~ ah*bh + ah*bl + al*bh
-// (al = a - tf32(a)).
+// (c) Cross-covariance GEMMs on the 5th-generation tensor cores: tcgen05.mma
+// (kind::f16, float32 accumulation) with TMEM accumulators, operands staged by
+// TMA (cp.async.bulk.tensor, 128-byte swizzle). Float32 accuracy comes from a
+// two-term float16 split of power-of-two-scaled operands,
+//   a * b ~ ah*bh + ah*bl + al*bh,   ah = f16(s a), al = f16(s a - ah),
+// which carries 22 significand bits like a two-term tf32 split, at twice the
+// tf32 tensor rate and half the operand bytes. Power-of-two scales bring the
+// largest entry of every operand row (A) and column (B) to at most 2^14, so the
+// float16 subnormal floor sits about 2^-38 below it; the epilogue multiplies
+// each output by row_mul[i] * col_mul[j] to undo them.
 //
 //   forward  V = Kc L^-T   (B operand stored as L^-1, K-major; k < n0 + BN)
 //   adjoint  D = H  L^-1   (B operand stored as L^-T, K-major; k >= n0)
@@ -9,18 +15,19 @@
 // One CTA computes a 128 x 256 tile of C. Warp roles: warp 0 issues the TMA
 // loads (one elected lane), warp 1 owns the TMEM allocation and issues the
 // MMAs (one elected lane), warps 2-9 drain the accumulators. Two shared-memory
-// stages of {A_hi, A_lo, B_hi, B_lo} (96 KB each).
+// stages of {A_hi, A_lo, B_hi, B_lo} (96 KB each, 64 K-elements deep).
 //
 // Accumulation: the K range is cut into chunks of TC_FLUSH k-blocks; each chunk
 // is accumulated in one of two TMEM accumulators (ping-pong, 2 x 256 columns)
 // while the epilogue warps add the previous chunk into float32 registers
 // (round-to-nearest). Keeping each tensor-core accumulation short holds the
-// 3xTF32 product to float32 accuracy over long K.
+// split product to float32 accuracy over long K.
 //
 // Every mbarrier wait is bounded in time; on expiry the CTA records an error
 // code, stops issuing work, waits (bounded) for its copies in flight, frees
 // its TMEM and returns.
 #include <cuda.h>
+#include <cuda_fp16.h>
 
 #include "bgb_common.cuh"
 #include "bgb_kernels.cuh"
@@ -29,11 +36,11 @@ namespace bgb {
 
 namespace {
 
-constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 32;  // BK: float32 elements (128 bytes)
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64;  // BK: float16 elements (128 bytes)
 constexpr int TC_STAGES = 2;
-constexpr int TC_UMMA_K = 8;                          // tf32 K per tcgen05.mma
-constexpr uint32_t A_TILE = TC_BM * TC_BK * 4;        // 16 KB
-constexpr uint32_t B_TILE = TC_BN * TC_BK * 4;        // 32 KB
+constexpr int TC_UMMA_K = 16;                         // float16 K per tcgen05.mma
+constexpr uint32_t A_TILE = TC_BM * TC_BK * 2;        // 16 KB
+constexpr uint32_t B_TILE = TC_BN * TC_BK * 2;        // 32 KB
 constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr int TC_THREADS = 320;                       // 10 warps
 constexpr int TC_FLUSH = 1;                           // k-blocks per TMEM accumulation chunk
@@ -41,8 +48,8 @@ constexpr uint32_t TMEM_COLS = 512;                   // two 128 x 256 float32 a
 constexpr size_t TC_SMEM = TC_STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
-// instruction descriptor: D f32, A/B tf32, both K-major, N = 256, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
+// instruction descriptor (kind::f16): D f32, A/B f16, both K-major, N = 256, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
                             ((uint32_t)(TC_BM >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -110,12 +117,12 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
     return d;
 }
 
-__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                          uint32_t accumulate) {
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
 }
 
@@ -147,7 +154,8 @@ struct TcMaps {
 // kmode: KB_UPPER (forward, k < n0 + BN) or KB_LOWER (adjoint, k >= n0).
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ TcMaps maps, float* __restrict__ C, int64_t ldc,
-                   int M, int N, int K, int kmode, int n_tiles, int* __restrict__ err) {
+                   int M, int N, int K, int kmode, int n_tiles, const float* __restrict__ row_mul,
+                   float row_mul_const, const float* __restrict__ col_mul, int* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smraw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) &
                                                ~(uintptr_t)1023);
@@ -241,11 +249,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                b_lo = sa + 2 * A_TILE + B_TILE;
 #pragma unroll
                 for (int kk = 0; kk < TC_BK / TC_UMMA_K; ++kk) {
-                    const uint32_t off = kk * TC_UMMA_K * 4;  // bytes along K in the 128-B row
+                    const uint32_t off = kk * TC_UMMA_K * 2;  // bytes along K in the 128-B row
                     const uint32_t acc = (kb > c * TC_FLUSH || kk > 0) ? 1u : 0u;
-                    umma_tf32(tacc, sdesc(a_lo + off), sdesc(b_hi + off), acc);
-                    umma_tf32(tacc, sdesc(a_hi + off), sdesc(b_lo + off), 1u);
-                    umma_tf32(tacc, sdesc(a_hi + off), sdesc(b_hi + off), 1u);
+                    umma_f16(tacc, sdesc(a_lo + off), sdesc(b_hi + off), acc);
+                    umma_f16(tacc, sdesc(a_hi + off), sdesc(b_lo + off), 1u);
+                    umma_f16(tacc, sdesc(a_hi + off), sdesc(b_hi + off), 1u);
                 }
                 umma_commit(&empty[s]);
             }
@@ -287,17 +295,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (lane == 0) mbar_arrive(&acce[a]);
         }
         if (good && row < M) {
+            // undo the operand scales: row multiplier times column multiplier
             const int c0 = n0 + half * (TC_BN / 2);
+            const float rm = row_mul != nullptr ? row_mul[row] : row_mul_const;
             float* dst = C + (int64_t)row * ldc + c0;
-            if (c0 + TC_BN / 2 <= N && (ldc % 4) == 0) {
+            if (c0 + TC_BN / 2 <= N && (ldc % 4) == 0 &&
+                (reinterpret_cast<uintptr_t>(col_mul + c0) % 16) == 0) {
+                const float4* cm4 = reinterpret_cast<const float4*>(col_mul + c0);
 #pragma unroll
-                for (int v = 0; v < TC_BN / 2 / 4; ++v)
+                for (int v = 0; v < TC_BN / 2 / 4; ++v) {
+                    const float4 cm = cm4[v];
                     reinterpret_cast<float4*>(dst)[v] =
-                        make_float4(tot[4 * v], tot[4 * v + 1], tot[4 * v + 2], tot[4 * v + 3]);
+                        make_float4(tot[4 * v] * rm * cm.x, tot[4 * v + 1] * rm * cm.y,
+                                    tot[4 * v + 2] * rm * cm.z, tot[4 * v + 3] * rm * cm.w);
+                }
             } else {
 #pragma unroll
                 for (int v = 0; v < TC_BN / 2; ++v)
-                    if (c0 + v < N) dst[v] = tot[v];
+                    if (c0 + v < N) dst[v] = tot[v] * rm * col_mul[c0 + v];
             }
         }
     }
@@ -311,37 +326,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (threadIdx.x == 0 && *fail) atomicExch(err, *fail);
 }
 
-// tf32 split of a float32 value: hi = rna(x), lo = rna(x - hi)
-__device__ __forceinline__ float tf32_rna(float x) {
-    uint32_t y;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(y) : "f"(x));
-    return __uint_as_float(y);
+// Power-of-two scale that brings the largest magnitude m of a row to at most
+// 2^14: s = 2^(14 - e) with m = f 2^e, f in [0.5, 1); s = 1 for m = 0 or non-finite m.
+__device__ __forceinline__ float pow2_scale(double m) {
+    if (!(m > 0.0) || isinf(m)) return 1.f;
+    int e;
+    frexp(m, &e);
+    return ldexpf(1.f, 14 - e);
 }
 
-__global__ void split_tf32_kernel(const float* __restrict__ src, int64_t rows, int64_t cols,
-                                  int64_t lds, float* __restrict__ hi, float* __restrict__ lo,
-                                  int64_t ldd) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= rows * ldd) return;
-    const int64_t i = idx / ldd, j = idx % ldd;
-    const float x = (j < cols) ? src[i * lds + j] : 0.f;
-    const float h = tf32_rna(x);
-    hi[idx] = h;
-    lo[idx] = tf32_rna(x - h);
-}
-
-// hi/lo tf32 split of a float64 matrix (optionally transposed): dst[i][j] = src[i][j] or src[j][i]
-__global__ void split_f64_tf32_kernel(const double* __restrict__ src, int64_t rows, int64_t cols,
-                                      int64_t lds, int transpose, float* __restrict__ hi,
-                                      float* __restrict__ lo, int64_t ldd) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= rows * ldd) return;
-    const int64_t i = idx / ldd, j = idx % ldd;
-    double x = 0.0;
-    if (j < cols) x = transpose ? src[j * lds + i] : src[i * lds + j];
-    const float h = tf32_rna((float)x);
-    hi[idx] = h;
-    lo[idx] = tf32_rna((float)(x - (double)h));
+// Per storage row i of src (or of its transpose): scale s_i = pow2_scale(max_j |x_ij|)
+// and the float16 split hi = f16(s_i x), lo = f16(s_i x - hi) into ldd-strided
+// rows (columns >= cols are 0); mul[i] = 1 / s_i. One warp per row.
+__global__ void split_f64_f16_kernel(const double* __restrict__ src, int64_t rows, int64_t cols,
+                                     int64_t lds, int transpose, __half* __restrict__ hi,
+                                     __half* __restrict__ lo, int64_t ldd, float* __restrict__ mul) {
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (i >= rows) return;
+    auto at = [&](int64_t j) { return transpose ? src[j * lds + i] : src[i * lds + j]; };
+    double m = 0.0;
+    for (int64_t j = lane; j < cols; j += 32) m = fmax(m, fabs(at(j)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const float sc = pow2_scale(m);
+    for (int64_t j = lane; j < ldd; j += 32) {
+        const float x = (j < cols) ? (float)(at(j) * (double)sc) : 0.f;
+        const __half h = __float2half_rn(x);
+        hi[i * ldd + j] = h;
+        lo[i * ldd + j] = __float2half_rn(x - __half2float(h));
+    }
+    if (lane == 0) mul[i] = 1.f / sc;
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -362,18 +377,18 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 2-D row-major float32 matrix (rows x cols, leading dimension ld) as a TMA map
-// with a 32-column x box_rows box and 128-byte swizzle; out-of-range reads are 0.
-bool make_map(CUtensorMap* map, const float* ptr, int64_t rows, int64_t cols, int64_t ld,
+// 2-D row-major float16 matrix (rows x cols, leading dimension ld) as a TMA map
+// with a 64-column x box_rows box and 128-byte swizzle; out-of-range reads are 0.
+bool make_map(CUtensorMap* map, const __half* ptr, int64_t rows, int64_t cols, int64_t ld,
               int box_rows) {
     EncodeTiledFn fn = encode_fn();
     if (fn == nullptr) return false;
-    if ((reinterpret_cast<uintptr_t>(ptr) & 15) != 0 || (ld * 4) % 16 != 0) return false;
+    if ((reinterpret_cast<uintptr_t>(ptr) & 15) != 0 || (ld * 2) % 16 != 0) return false;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
     cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides,
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half*>(ptr), dims, strides,
                     box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
@@ -383,32 +398,26 @@ bool make_map(CUtensorMap* map, const float* ptr, int64_t rows, int64_t cols, in
 
 bool tc_gemm_available() { return encode_fn() != nullptr; }
 
-int split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, float* hi, float* lo,
-               int64_t ldd, cudaStream_t stream) {
+int split_f64_f16(const double* src, int64_t rows, int64_t cols, int64_t lds, int transpose,
+                  __half* hi, __half* lo, int64_t ldd, float* mul, cudaStream_t stream) {
     if (rows <= 0 || cols <= 0) return BGB_OK;
-    const int64_t tot = rows * ldd;
-    split_tf32_kernel<<<(unsigned)ceil_div(tot, 256), 256, 0, stream>>>(src, rows, cols, lds, hi, lo,
-                                                                       ldd);
+    if (ldd < cols) return BGB_ERR_ARG;
+    split_f64_f16_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, stream>>>(
+        src, rows, cols, lds, transpose, hi, lo, ldd, mul);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
 
-int split_f64_tf32(const double* src, int64_t rows, int64_t cols, int64_t lds, int transpose,
-                   float* hi, float* lo, int64_t ldd, cudaStream_t stream) {
-    if (rows <= 0 || cols <= 0) return BGB_OK;
-    const int64_t tot = rows * ldd;
-    split_f64_tf32_kernel<<<(unsigned)ceil_div(tot, 256), 256, 0, stream>>>(src, rows, cols, lds,
-                                                                           transpose, hi, lo, ldd);
-    BGB_CHECK_LAUNCH();
-    return BGB_OK;
-}
-
-// C (M x N) = A (M x K) * op(B), A given as tf32 hi/lo (lda), B as its K-major
-// storage Bs (N x K, hi/lo, ldbs): op(B)[k][j] = Bs[j][k]. kmode KB_UPPER or KB_LOWER.
-int tc_gemm_tf32x3(int64_t M, int64_t N, int64_t K, const float* A_hi, const float* A_lo,
-                   int64_t lda, const float* B_hi, const float* B_lo, int64_t ldbs, float* C,
-                   int64_t ldc, int kmode, int* err, cudaStream_t stream) {
+// C (M x N) = diag(row_mul) (A (M x K) * op(B)) diag(col_mul), A given as its
+// float16 split hi/lo (lda), B as its K-major storage Bs (N x K, hi/lo, ldbs):
+// op(B)[k][j] = Bs[j][k]. row_mul: M multipliers, or nullptr for row_mul_const.
+// kmode KB_UPPER or KB_LOWER.
+int tc_gemm_f16x3(int64_t M, int64_t N, int64_t K, const __half* A_hi, const __half* A_lo,
+                  int64_t lda, const __half* B_hi, const __half* B_lo, int64_t ldbs, float* C,
+                  int64_t ldc, int kmode, const float* row_mul, float row_mul_const,
+                  const float* col_mul, int* err, cudaStream_t stream) {
     if (M <= 0 || N <= 0) return BGB_OK;
+    if (col_mul == nullptr) return BGB_ERR_ARG;
     TcMaps maps;
     if (!make_map(&maps.a_hi, A_hi, M, K, lda, TC_BM) || !make_map(&maps.a_lo, A_lo, M, K, lda, TC_BM) ||
         !make_map(&maps.b_hi, B_hi, N, K, ldbs, TC_BN) || !make_map(&maps.b_lo, B_lo, N, K, ldbs, TC_BN))
@@ -421,7 +430,7 @@ int tc_gemm_tf32x3(int64_t M, int64_t N, int64_t K, const float* A_hi, const flo
     }
     const int m_tiles = (int)ceil_div(M, TC_BM), n_tiles = (int)ceil_div(N, TC_BN);
     tc_gemm_kernel<<<(unsigned)(m_tiles * n_tiles), TC_THREADS, TC_SMEM, stream>>>(
-        maps, C, ldc, (int)M, (int)N, (int)K, kmode, n_tiles, err);
+        maps, C, ldc, (int)M, (int)N, (int)K, kmode, n_tiles, row_mul, row_mul_const, col_mul, err);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }

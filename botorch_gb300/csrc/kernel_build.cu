@@ -17,20 +17,17 @@ namespace {
 constexpr int KB_TILE = 64;
 constexpr int KB_DCHUNK = 32;
 
-__device__ __forceinline__ float tf32_round(float x) {
-    uint32_t y;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(y) : "f"(x));
-    return __uint_as_float(y);
-}
 
-// K_lo == nullptr: plain output. Otherwise (float32 only) the output is split
-// for the 3xTF32 tensor-core GEMM: K = tf32(v), K_lo = tf32(v - tf32(v)).
+// K16 == nullptr: plain output K. Otherwise (float32 arithmetic only) the output
+// is the scaled float16 split for the tensor-core GEMM: with w = k16_scale * v,
+// K16 = f16(w), K16_lo = f16(w - K16) (K is not written).
 template <typename TIn, typename TAcc, typename TOut>
 __global__ void __launch_bounds__(256) kernel_matrix_kernel(
     const TIn* __restrict__ X1, int64_t m, const TIn* __restrict__ X2, int64_t n2, int d,
     const double* __restrict__ inv_ls, double outputscale, int kind, double diag_add,
-    int same, TOut* __restrict__ K, int64_t ldk, TOut* __restrict__ K_lo,
-    const float* __restrict__ Z1T, int64_t ldz1, const float* __restrict__ Z2T, int64_t ldz2) {
+    int same, TOut* __restrict__ K, int64_t ldk, __half* __restrict__ K16,
+    __half* __restrict__ K16_lo, float k16_scale, const float* __restrict__ Z1T, int64_t ldz1,
+    const float* __restrict__ Z2T, int64_t ldz2) {
     __shared__ TAcc s1[KB_DCHUNK][KB_TILE + 1];
     __shared__ TAcc s2[KB_DCHUNK][KB_TILE + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -84,11 +81,12 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
             if (j >= n2) continue;
             TAcc val = TAcc(outputscale) * kappa<TAcc>(kind, acc[u][v]);
             if (same && i == j) val += TAcc(diag_add);
-            if constexpr (sizeof(TOut) == 4) {
-                if (K_lo != nullptr) {
-                    const float h = tf32_round((float)val);
-                    K[i * ldk + j] = (TOut)h;
-                    K_lo[i * ldk + j] = (TOut)tf32_round((float)val - h);
+            if constexpr (sizeof(TAcc) == 4) {
+                if (K16 != nullptr) {
+                    const float w = (float)val * k16_scale;
+                    const __half h = __float2half_rn(w);
+                    K16[i * ldk + j] = h;
+                    K16_lo[i * ldk + j] = __float2half_rn(w - __half2float(h));
                     continue;
                 }
             }
@@ -102,25 +100,27 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
 template <typename TIn, typename TAcc, typename TOut>
 int launch_kernel_matrix(const TIn* X1, int64_t m, const TIn* X2, int64_t n2, int d,
                          const double* inv_ls, double outputscale, int kind, double diag_add,
-                         int same, TOut* K, int64_t ldk, cudaStream_t stream, TOut* K_lo) {
+                         int same, TOut* K, int64_t ldk, cudaStream_t stream) {
     if (m <= 0 || n2 <= 0) return BGB_OK;
     dim3 grid((unsigned)ceil_div(n2, KB_TILE), (unsigned)ceil_div(m, KB_TILE));
     kernel_matrix_kernel<TIn, TAcc, TOut><<<grid, 256, 0, stream>>>(
-        X1, m, X2, n2, d, inv_ls, outputscale, kind, diag_add, same, K, ldk, K_lo, nullptr, 0,
-        nullptr, 0);
+        X1, m, X2, n2, d, inv_ls, outputscale, kind, diag_add, same, K, ldk, nullptr, nullptr,
+        0.f, nullptr, 0, nullptr, 0);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
 
 int launch_kernel_matrix_zt(const float* Z1T, int64_t ldz1, int64_t m, const float* Z2T,
                             int64_t ldz2, int64_t n2, int d, double outputscale, int kind,
-                            float* K, int64_t ldk, cudaStream_t stream, float* K_lo) {
+                            float* K, __half* K16, __half* K16_lo, float k16_scale, int64_t ldk,
+                            cudaStream_t stream) {
     if (m <= 0 || n2 <= 0) return BGB_OK;
     if (Z1T == nullptr || Z2T == nullptr || ldz1 < m || ldz2 < n2) return BGB_ERR_ARG;
+    if (K == nullptr && (K16 == nullptr || K16_lo == nullptr)) return BGB_ERR_ARG;
     dim3 grid((unsigned)ceil_div(n2, KB_TILE), (unsigned)ceil_div(m, KB_TILE));
     kernel_matrix_kernel<float, float, float><<<grid, 256, 0, stream>>>(
-        nullptr, m, nullptr, n2, d, nullptr, outputscale, kind, 0.0, 0, K, ldk, K_lo, Z1T, ldz1,
-        Z2T, ldz2);
+        nullptr, m, nullptr, n2, d, nullptr, outputscale, kind, 0.0, 0, K, ldk, K16, K16_lo,
+        k16_scale, Z1T, ldz1, Z2T, ldz2);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
@@ -128,10 +128,10 @@ int launch_kernel_matrix_zt(const float* Z1T, int64_t ldz1, int64_t m, const flo
 template int launch_kernel_matrix<double, double, double>(const double*, int64_t, const double*,
                                                           int64_t, int, const double*, double,
                                                           int, double, int, double*, int64_t,
-                                                          cudaStream_t, double*);
+                                                          cudaStream_t);
 template int launch_kernel_matrix<double, float, float>(const double*, int64_t, const double*,
                                                         int64_t, int, const double*, double, int,
                                                         double, int, float*, int64_t,
-                                                        cudaStream_t, float*);
+                                                        cudaStream_t);
 
 }  // namespace bgb

@@ -1139,38 +1139,45 @@ __global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
 // E consecutive columns of one t-batch (one 16-byte vector per row when the
 // layout allows, else E = 1), so every seed read from shared memory feeds E
 // columns; QM >= q bounds the register arrays.
-template <typename T>
-__device__ __forceinline__ void store_h(T* H, T* H_lo, int64_t off, T h) {
-    if constexpr (sizeof(T) == 4) {
-        if (H_lo != nullptr) {  // tf32 split for the tensor-core adjoint GEMM
-            uint32_t hb, lb;
-            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"((float)h));
-            const float hh = __uint_as_float(hb);
-            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"((float)h - hh));
-            H[off] = hh;
-            H_lo[off] = __uint_as_float(lb);
-            return;
-        }
-    }
-    H[off] = h;
-}
-
+// H16 set (float32 only): H is written as the float16 split of s_i H[i,:] for
+// the tensor-core adjoint GEMM, s_i a power of two from the bound
+//   |H[i,c]| <= |gmu_i| max|beta| + sqrt(outputscale) (sum_j 2|Gqq[i,j]| + sum_k |Gqb[i,k]|)
+// (every row of V and Vb has 2-norm <= sqrt(outputscale) since V V^T <= K(X,X)),
+// and hmul[i] = 1 / s_i.
 template <typename T, int QM, int E>
 __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __restrict__ V,
                                                        int64_t ldv, const T* __restrict__ Vb,
                                                        const T* __restrict__ beta,
-                                                       T* __restrict__ H, T* __restrict__ H_lo,
-                                                       int64_t ldh) {
-    extern __shared__ __align__(16) unsigned char gsraw[];  // q*q + q*r + q seeds (as T)
+                                                       T* __restrict__ H, __half* __restrict__ H16,
+                                                       __half* __restrict__ H16_lo, int64_t ldh) {
+    extern __shared__ __align__(16) unsigned char gsraw[];  // q*q + q*r + q seeds (as T), q scales
     T* gq = reinterpret_cast<T*>(gsraw);
     const int q = a.q, r = a.r;
     const int64_t n = a.n, bidx = blockIdx.y, rbase = bidx * q;
     T* gqb = gq + q * q;
     T* gm = gqb + q * r;
+    float* hs = reinterpret_cast<float*>(gm + q);
     for (int p = threadIdx.x; p < q * q; p += blockDim.x) gq[p] = (T)(-2.0 * a.gqq[bidx * q * q + p]);
     for (int p = threadIdx.x; p < q * r; p += blockDim.x) gqb[p] = (T)(-a.gqb[bidx * q * r + p]);
     for (int p = threadIdx.x; p < q; p += blockDim.x) gm[p] = (T)a.gmu[bidx * q + p];
     __syncthreads();
+    if (H16 != nullptr) {
+        for (int i = threadIdx.x; i < q; i += blockDim.x) {
+            float bound = fabsf((float)gm[i]) * (float)a.beta_absmax, sv = 0.f;
+            for (int j = 0; j < q; ++j) sv += fabsf((float)gq[i * q + j]);
+            for (int k = 0; k < r; ++k) sv += fabsf((float)gqb[i * r + k]);
+            bound += sqrtf((float)a.outputscale) * sv;
+            float sc = 1.f;
+            if (bound > 0.f && !isinf(bound)) {
+                int e;
+                frexpf(bound, &e);
+                sc = ldexpf(1.f, 14 - e);
+            }
+            hs[i] = sc;
+            if (blockIdx.x == 0) a.hmul[rbase + i] = 1.f / sc;
+        }
+        __syncthreads();
+    }
     const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * E;
     if (c0 >= n) return;
     using VT = typename Vec16<T>::type;
@@ -1229,23 +1236,25 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
     for (int i = 0; i < QM; ++i) {
         if (i >= q) break;
         const int64_t off = (rbase + i) * ldh + c0;
-        if constexpr (E > 1 && sizeof(T) == 4) {
-            if (H_lo != nullptr) {
-                float4 hh, ll;
-                float* ph = &hh.x;
-                float* pl = &ll.x;
+        if (H16 != nullptr) {
+            __half hh[E], ll[E];
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const float w = (float)h[i][e] * hs[i];
+                hh[e] = __float2half_rn(w);
+                ll[e] = __float2half_rn(w - __half2float(hh[e]));
+            }
+            if constexpr (E == 4) {
+                *reinterpret_cast<uint2*>(H16 + off) = *reinterpret_cast<const uint2*>(hh);
+                *reinterpret_cast<uint2*>(H16_lo + off) = *reinterpret_cast<const uint2*>(ll);
+            } else {
 #pragma unroll
                 for (int e = 0; e < E; ++e) {
-                    uint32_t hb, lb;
-                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"((float)h[i][e]));
-                    ph[e] = __uint_as_float(hb);
-                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"((float)h[i][e] - ph[e]));
-                    pl[e] = __uint_as_float(lb);
+                    H16[off + e] = hh[e];
+                    H16_lo[off + e] = ll[e];
                 }
-                *reinterpret_cast<float4*>(H + off) = hh;
-                *reinterpret_cast<float4*>(H_lo + off) = ll;
-                continue;
             }
+            continue;
         }
         if constexpr (E > 1) {
             VT o;
@@ -1254,7 +1263,7 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
             for (int e = 0; e < E; ++e) po[e] = h[i][e];
             *reinterpret_cast<VT*>(H + off) = o;
         } else {
-            store_h<T>(H, H_lo, off, h[i][0]);
+            H[off] = h[i][0];
         }
     }
 }
@@ -1517,24 +1526,28 @@ int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta,
 
 template <typename T>
 int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, const T* beta, T* H,
-                    cudaStream_t stream, T* H_lo, int64_t ldh) {
+                    cudaStream_t stream, __half* H16, __half* H16_lo, int64_t ldh) {
     if (a.b <= 0) return BGB_OK;
     if (a.q > kMaxQ) return BGB_ERR_UNSUPPORTED;
-    const size_t smem = sizeof(T) * (size_t)(a.q * a.q + a.q * a.r + a.q);
+    if (H16 != nullptr && (sizeof(T) != 4 || H16_lo == nullptr || a.hmul == nullptr)) return BGB_ERR_ARG;
+    const size_t smem = sizeof(T) * (size_t)(a.q * a.q + a.q * a.r + a.q) + sizeof(float) * a.q;
     if (smem > 48 * 1024) return BGB_ERR_UNSUPPORTED;
     const int64_t ld = ldh > 0 ? ldh : a.n;
     constexpr int E = Vec16<T>::E;
-    auto al = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) % 16) == 0; };
-    const bool vec = (a.n % E == 0) && (ldv % E == 0) && (ld % E == 0) && al(V) && al(beta) &&
-                     al(H) && (H_lo == nullptr || al(H_lo)) && (a.r == 0 || al(Vb));
+    auto al = [](const void* p, int b) { return (reinterpret_cast<uintptr_t>(p) % b) == 0; };
+    const bool vec = (a.n % E == 0) && (ldv % E == 0) && (ld % E == 0) && al(V, 16) &&
+                     al(beta, 16) && (a.r == 0 || al(Vb, 16)) &&
+                     (H16 != nullptr ? (al(H16, 8) && al(H16_lo, 8)) : al(H, 16));
 #define BGB_MIX(QM)                                                                              \
     do {                                                                                        \
         if (vec) {                                                                              \
             dim3 grid((unsigned)ceil_div(a.n, 256 * E), (unsigned)a.b);                         \
-            mix_rows_kernel<T, QM, E><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld); \
+            mix_rows_kernel<T, QM, E><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H16,   \
+                                                                   H16_lo, ld);                 \
         } else {                                                                                \
             dim3 grid((unsigned)ceil_div(a.n, 256), (unsigned)a.b);                             \
-            mix_rows_kernel<T, QM, 1><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H_lo, ld); \
+            mix_rows_kernel<T, QM, 1><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H16,   \
+                                                                   H16_lo, ld);                 \
         }                                                                                       \
     } while (0)
     if (a.q <= 4) BGB_MIX(4);
@@ -1631,9 +1644,10 @@ template int launch_row_dots<double>(const QBatchArgs&, const double*, int64_t, 
 template int launch_row_dots<float>(const QBatchArgs&, const float*, int64_t, const float*,
                                     const float*, float*, cudaStream_t);
 template int launch_mix_rows<double>(const QBatchArgs&, const double*, int64_t, const double*,
-                                     const double*, double*, cudaStream_t, double*, int64_t);
+                                     const double*, double*, cudaStream_t, __half*, __half*,
+                                     int64_t);
 template int launch_mix_rows<float>(const QBatchArgs&, const float*, int64_t, const float*,
-                                    const float*, float*, cudaStream_t, float*, int64_t);
+                                    const float*, float*, cudaStream_t, __half*, __half*, int64_t);
 template int launch_adjoint<double>(const QBatchArgs&, const double*, int64_t, const double*,
                                     double*, int64_t, cudaStream_t);
 template int launch_adjoint<float>(const QBatchArgs&, const float*, int64_t, const float*,

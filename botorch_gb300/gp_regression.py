@@ -167,8 +167,9 @@ class SingleTaskGP:
 
         Returns (B64, B32, ldb, Linv32, beta32, tc, Xs64, Xs32) with B = L^-T,
         float32 copies of L^-1 and beta, for the mixed path ``tc`` = (Lhi, Llo,
-        LThi, LTlo, ldl): the tf32 hi/lo split of L^-1 and L^-T used by the
-        tensor-core GEMMs, and the training inputs scaled by 1 / lengthscale.
+        LThi, LTlo, Lmul, LTmul, ldl, beta_absmax): the row-scaled float16 hi/lo
+        split of L^-1 and L^-T used by the tensor-core GEMMs with the inverse row
+        scales, and max |beta|; and the training inputs scaled by 1 / lengthscale.
         """
         if precision in self._operands:
             return self._operands[precision]
@@ -191,10 +192,13 @@ class SingleTaskGP:
             nat.check(rc, "model operands")
             tc = None
             if mixed:
-                tc = tuple(torch.empty(n, ldb, dtype=torch.float32, device=dev) for _ in range(4)) + (ldb,)
+                halves = tuple(torch.empty(n, ldb, dtype=torch.float16, device=dev) for _ in range(4))
+                muls = tuple(torch.empty(n, dtype=torch.float32, device=dev) for _ in range(2))
                 rc = lib.bgb_gp_tc_operands(ctypes.byref(gp), nat.ptr(self.Linv), ldb,
-                                            *(nat.ptr(t) for t in tc[:4]), nat.stream_handle(dev))
+                                            *(nat.ptr(t) for t in halves + muls),
+                                            nat.stream_handle(dev))
                 nat.check(rc, "tensor-core operands")
+                tc = halves + muls + (ldb, float(self.beta.abs().max()))
         self._operands[precision] = (B64, B32, ldb, L32, b32, tc, Xs64, Xs32)
         return self._operands[precision]
 
@@ -207,7 +211,8 @@ class SingleTaskGP:
                   Xs64=nat.ptr(Xs64), Xs32=nat.ptr(Xs32))
         if tc is not None:
             kw.update(Lhi=nat.ptr(tc[0]), Llo=nat.ptr(tc[1]), LThi=nat.ptr(tc[2]),
-                      LTlo=nat.ptr(tc[3]), ldl=tc[4])
+                      LTlo=nat.ptr(tc[3]), Lmul=nat.ptr(tc[4]), LTmul=nat.ptr(tc[5]), ldl=tc[6],
+                      beta_absmax=tc[7])
         if not tensor_cores:
             kw["flags"] = nat.BGB_FLAG_SIMT
         return kw

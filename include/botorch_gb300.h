@@ -100,13 +100,18 @@ typedef struct bgb_acq {
     const float* beta32;
     const double* Xs64;      /* d x n (k-major): training inputs / lengthscale (adjoint) */
     const float* Xs32;
-    /* tensor-core operands of MIXED (tf32 hi/lo, n x ldl, ldl >= n, ldl % 8 == 0):
-     * L^-1 for the forward GEMM and L^-T for the adjoint GEMM; NULL: FFMA GEMM */
-    const float* Lhi;
-    const float* Llo;
-    const float* LThi;
-    const float* LTlo;
+    /* tensor-core operands of MIXED (IEEE binary16 bit patterns, n x ldl,
+     * ldl >= n, ldl % 8 == 0; from bgb_gp_tc_operands): the scaled float16
+     * hi/lo split of L^-1 for the forward GEMM and of L^-T for the adjoint
+     * GEMM, with the inverse row scales; NULL: FFMA GEMM */
+    const uint16_t* Lhi;
+    const uint16_t* Llo;
+    const uint16_t* LThi;
+    const uint16_t* LTlo;
+    const float* Lmul;       /* n: 1 / scale of row j of L^-1 */
+    const float* LTmul;      /* n: 1 / scale of row j of L^-T */
     int64_t ldl;
+    double beta_absmax;      /* max_j |beta_j| (bounds the adjoint GEMM's rows) */
     const double* X_baseline;/* r x d */
     const double* Lb_inv;    /* r x r: inverse of the Cholesky factor of the
                                 untransformed baseline posterior covariance */
@@ -168,23 +173,31 @@ int bgb_gp_operands(const bgb_gp_t* gp, const double* Linv, const double* beta, 
                     float* B32, int64_t ldb, float* Linv32, float* beta32, double* Xs64,
                     float* Xs32, void* stream);
 
-/* (c) Tensor-core operands of the mixed path: the tf32 hi/lo split of L^-1
- * (Lhi, Llo) and of L^-T (LThi, LTlo), n x ldl each (ldl >= n, ldl % 8 == 0). */
-int bgb_gp_tc_operands(const bgb_gp_t* gp, const double* Linv, int64_t ldl, float* Lhi,
-                       float* Llo, float* LThi, float* LTlo, void* stream);
+/* (c) Tensor-core operands of the mixed path: each row j of L^-1 (and of
+ * L^-T) scaled by a power of two s_j that brings its largest magnitude to at
+ * most 2^14, split into float16 hi = f16(s_j x), lo = f16(s_j x - hi):
+ * (Lhi, Llo) and (LThi, LTlo), n x ldl each (ldl >= n, ldl % 8 == 0, columns
+ * >= n zero); Lmul / LTmul (n floats) receive 1 / s_j. */
+int bgb_gp_tc_operands(const bgb_gp_t* gp, const double* Linv, int64_t ldl, uint16_t* Lhi,
+                       uint16_t* Llo, uint16_t* LThi, uint16_t* LTlo, float* Lmul, float* LTmul,
+                       void* stream);
 
 /* (c) The tensor-core GEMM of the mixed path on caller operands:
- * C (M x N, ldc) = A (M x K) op(B), with A given as its tf32 hi/lo split (lda)
- * and B by its K-major storage Bs (N x K, hi/lo, ldbs): op(B)[k][j] = Bs[j][k].
- * kmode 3: op(B) upper triangular (k <= j); kmode 1: op(B) lower triangular
- * (k >= j). 3xTF32 products accumulated in float32 TMEM. *err_dev (device
- * int, may be NULL) is set non-zero if a bounded wait expired. lda, ldbs and
- * ldc must be multiples of 4 and the pointers 16-byte aligned. Exposed for
- * tests and for callers with their own operands. */
-int bgb_crosscov_gemm_tf32x3(int64_t M, int64_t N, int64_t K, const float* A_hi,
-                             const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
-                             int64_t ldbs, float* C, int64_t ldc, int32_t kmode, int32_t* err_dev,
-                             void* stream);
+ *   C (M x N, ldc) = diag(row_mul) A op(B) diag(col_mul),
+ * with A given as its float16 hi/lo split (M x K, lda) and B by its K-major
+ * storage Bs (N x K, float16 hi/lo, ldbs): op(B)[k][j] = Bs[j][k]; the product
+ * is ah*bh + ah*bl + al*bh accumulated in float32 (TMEM, drained into float32
+ * registers every 64 k). row_mul (M floats) may be NULL, then every row uses
+ * row_mul_const; col_mul (N floats) is required. kmode 3: op(B) upper
+ * triangular (k <= j); kmode 1: op(B) lower triangular (k >= j); kmode 0:
+ * full. *err_dev (device int, may be NULL) is set non-zero if a bounded wait
+ * expired. lda and ldbs must be multiples of 8, ldc of 4, the pointers 16-byte
+ * aligned. Exposed for tests and for callers with their own operands. */
+int bgb_crosscov_gemm_f16x3(int64_t M, int64_t N, int64_t K, const uint16_t* A_hi,
+                            const uint16_t* A_lo, int64_t lda, const uint16_t* B_hi,
+                            const uint16_t* B_lo, int64_t ldbs, float* C, int64_t ldc,
+                            const float* row_mul, float row_mul_const, const float* col_mul,
+                            int32_t kmode, int32_t* err_dev, void* stream);
 
 /* (c) Baseline operands of qLogNEI: Vb = K(X_baseline, Xt) L^-T (r x n) and
  * VbT (n x r), float64 and float32 (the float32 pointers may be NULL). */

@@ -1,7 +1,7 @@
-"""The tcgen05 3xTF32 cross-covariance GEMM through the C ABI.
+"""The tcgen05 float16-split cross-covariance GEMM through the C ABI.
 
 Float32 accuracy is the bar: ||C - C_ref|| / ||C_ref|| below 5e-6 against a
-float64 product of the same (float32) operands.
+float64 product of the operands the float16 hi/lo splits represent.
 """
 
 import ctypes
@@ -15,14 +15,17 @@ pytestmark = pytest.mark.gpu
 DEV = torch.device("cuda:0")
 
 
-def split(x: torch.Tensor):
-    """tf32 round-to-nearest split in float64 arithmetic: hi = tf32(x), lo = tf32(x - hi)."""
-    def tf32(t):
-        i = t.float().contiguous().view(torch.int32)
-        i = (i + 0x1000) & ~0x1FFF
-        return i.view(torch.float32)
-    hi = tf32(x)
-    lo = tf32(x.double() - hi.double())
+def pow2_scale(m: torch.Tensor) -> torch.Tensor:
+    """2^(14 - e) with m = f 2^e, f in [0.5, 1): brings m to at most 2^14 (1 for m = 0)."""
+    _, e = torch.frexp(m)
+    return torch.where(m > 0, torch.exp2(14.0 - e.double()), torch.ones_like(m))
+
+
+def split16(x: torch.Tensor, scale: torch.Tensor):
+    """Row-scaled float16 split: hi = f16(s x), lo = f16(s x - hi), rows scaled by `scale`."""
+    xs = x * scale[:, None]
+    hi = xs.half()
+    lo = (xs - hi.double()).half()
     return hi, lo
 
 
@@ -30,8 +33,10 @@ def split(x: torch.Tensor):
 @pytest.mark.parametrize("kmode", [0, 1, 3])
 def test_tc_gemm_matches_float64(cuda_lib, M, N, K, kmode):
     g = torch.Generator().manual_seed(M + N + K + kmode)
-    A = torch.rand(M, K, generator=g, dtype=torch.float64) - 0.3
-    Bs = torch.randn(N, K, generator=g, dtype=torch.float64)
+    A = (torch.rand(M, K, generator=g, dtype=torch.float64) - 0.3) * torch.exp2(
+        torch.randint(-12, 12, (M, 1), generator=g).double())
+    Bs = torch.randn(N, K, generator=g, dtype=torch.float64) * torch.exp2(
+        torch.randint(-12, 12, (N, 1), generator=g).double())
     jj, kk = torch.meshgrid(torch.arange(N), torch.arange(K), indexing="ij")
     if kmode == 3:    # op(B) upper triangular: op(B)[k][j] = Bs[j][k] != 0 only for k <= j
         Bs = Bs * (kk <= jj)
@@ -39,21 +44,52 @@ def test_tc_gemm_matches_float64(cuda_lib, M, N, K, kmode):
         Bs = Bs * (kk >= jj)
     lda = (K + 7) // 8 * 8
     ldc = (N + 7) // 8 * 8
-    Ahi, Alo = split(A)
-    Bhi, Blo = split(Bs)
+    sa, sb = pow2_scale(A.abs().amax(1)), pow2_scale(Bs.abs().amax(1))
+    Ahi, Alo = split16(A, sa)
+    Bhi, Blo = split16(Bs, sb)
     pad = lambda t, ld: torch.nn.functional.pad(t, (0, ld - t.shape[1])).contiguous().to(DEV)  # noqa: E731
     Ahi_d, Alo_d, Bhi_d, Blo_d = pad(Ahi, lda), pad(Alo, lda), pad(Bhi, lda), pad(Blo, lda)
+    row_mul = (1.0 / sa).float().to(DEV)
+    col_mul = (1.0 / sb).float().to(DEV)
     C = torch.full((M, ldc), float("nan"), dtype=torch.float32, device=DEV)
     err = torch.zeros(1, dtype=torch.int32, device=DEV)
-    rc = cuda_lib.bgb_crosscov_gemm_tf32x3(M, N, K, Ahi_d.data_ptr(), Alo_d.data_ptr(), lda,
-                                           Bhi_d.data_ptr(), Blo_d.data_ptr(), lda, C.data_ptr(),
-                                           ldc, kmode, err.data_ptr(), nat.stream_handle(DEV))
+    rc = cuda_lib.bgb_crosscov_gemm_f16x3(M, N, K, Ahi_d.data_ptr(), Alo_d.data_ptr(), lda,
+                                          Bhi_d.data_ptr(), Blo_d.data_ptr(), lda, C.data_ptr(), ldc,
+                                          row_mul.data_ptr(), 0.0, col_mul.data_ptr(), kmode,
+                                          err.data_ptr(), nat.stream_handle(DEV))
     assert rc == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 0
-    ref = (Ahi.double() + Alo.double()) @ (Bhi.double() + Blo.double()).T
+    Arep = (Ahi.double() + Alo.double()) / sa[:, None]
+    Brep = (Bhi.double() + Blo.double()) / sb[:, None]
+    ref = Arep @ Brep.T
     out = C[:, :N].double().cpu()
     assert torch.isfinite(out).all()
+    assert float((out - ref).norm() / ref.norm()) < 5e-6
+    # the represented operands are the originals to 2^-22 relative
+    assert float((Arep - A).norm() / A.norm()) < 1e-6
+
+
+def test_tc_gemm_constant_row_multiplier(cuda_lib):
+    """row_mul NULL: every row uses row_mul_const (the forward GEMM's form)."""
+    g = torch.Generator().manual_seed(5)
+    M, N, K = 256, 256, 256
+    A = torch.rand(M, K, generator=g, dtype=torch.float64)
+    Bs = torch.randn(N, K, generator=g, dtype=torch.float64)
+    sa = torch.full((M,), 2.0 ** 14, dtype=torch.float64)
+    sb = pow2_scale(Bs.abs().amax(1))
+    Ahi, Alo = split16(A, sa)
+    Bhi, Blo = split16(Bs, sb)
+    Ahi_d, Alo_d, Bhi_d, Blo_d = (t.contiguous().to(DEV) for t in (Ahi, Alo, Bhi, Blo))
+    col_mul = (1.0 / sb).float().to(DEV)
+    C = torch.empty(M, N, dtype=torch.float32, device=DEV)
+    rc = cuda_lib.bgb_crosscov_gemm_f16x3(M, N, K, Ahi_d.data_ptr(), Alo_d.data_ptr(), K,
+                                          Bhi_d.data_ptr(), Blo_d.data_ptr(), K, C.data_ptr(), N,
+                                          None, 2.0 ** -14, col_mul.data_ptr(), 0, None,
+                                          nat.stream_handle(DEV))
+    assert rc == 0
+    ref = ((Ahi.double() + Alo.double()) / 2.0 ** 14) @ ((Bhi.double() + Blo.double()) / sb[:, None]).T
+    out = C.double().cpu()
     assert float((out - ref).norm() / ref.norm()) < 5e-6
 
 
