@@ -199,6 +199,7 @@ def cpu_baseline(w, model_kw, n_batches: int = 32) -> dict:
 # ---------------------------------------------------------------- our arm
 def run_ours(args) -> None:
     from botorch_gb300 import _native as nat
+    from botorch_gb300 import replicas
     from botorch_gb300 import testing as T
 
     world, rank, local = dist_info()
@@ -208,9 +209,7 @@ def run_ours(args) -> None:
     torch.cuda.set_device(device)
     b = args.b
     w = T.qlognei_branin(n=N_TRAIN, b=b, q=Q, d=DIM, seed=0)
-    if rank > 0:  # weak scaling: every rank evaluates its own candidates
-        g = torch.Generator().manual_seed(1000 + rank)
-        w.X = torch.rand(b, Q, DIM, generator=g, dtype=torch.float64)
+    w.X = replicas.rank_candidates(w.X, rank)  # weak scaling: every rank its own candidates
     model = make_model(device, w)
     acqf = make_acqf(model, w, "mixed")
     acqf.check_status = False
@@ -244,14 +243,11 @@ def run_ours(args) -> None:
         t_wall = time.perf_counter() - t_wall0
     launches = lib.bgb_launch_count() - launches0
     torch.cuda.synchronize(device)
-    total_ms = sum(step_ms)
+    total_ms = replicas.max_over_ranks(sum(step_ms), device)
     if world > 1:
-        t = torch.tensor([total_ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         torch.distributed.barrier()
-        total_ms = float(t.item())
     status_ok = int(out[2].max().item()) == 0
-    value = world * b * args.steps / (total_ms / 1e3)
+    value = replicas.evals_per_second(world, b, args.steps, total_ms)
 
     # roofline of the cross-covariance GEMMs, timed live per stage
     import ctypes

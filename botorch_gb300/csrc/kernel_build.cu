@@ -29,7 +29,10 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
     __half* __restrict__ K16_lo, float k16_scale, const float* __restrict__ Z1T, int64_t ldz1,
     const float* __restrict__ Z2T, int64_t ldz2) {
     __shared__ TAcc s1[KB_DCHUNK][KB_TILE + 1];
-    __shared__ TAcc s2[KB_DCHUNK][KB_TILE + 1];
+    __shared__ __align__(16) TAcc s2[KB_DCHUNK][KB_TILE];
+    // thread (tx, ty): rows ty + 16 u, columns 4 tx + v (u, v < 4): the column
+    // coordinates are one 16-byte shared load per k and the outputs are
+    // vector stores of 4 consecutive entries
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int64_t row0 = (int64_t)blockIdx.y * KB_TILE, col0 = (int64_t)blockIdx.x * KB_TILE;
     TAcc acc[4][4];
@@ -54,12 +57,18 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
             s2[kk][rr] = v2;
         }
         __syncthreads();
+#pragma unroll 4
         for (int kk = 0; kk < kc; ++kk) {
             TAcc a[4], b[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                a[u] = s1[kk][ty + 16 * u];
-                b[u] = s2[kk][tx + 16 * u];
+            for (int u = 0; u < 4; ++u) a[u] = s1[kk][ty + 16 * u];
+            if constexpr (sizeof(TAcc) == 4) {
+                const float4 bv = *reinterpret_cast<const float4*>(&s2[kk][4 * tx]);
+                b[0] = bv.x; b[1] = bv.y; b[2] = bv.z; b[3] = bv.w;
+            } else {
+                const double2 b01 = *reinterpret_cast<const double2*>(&s2[kk][4 * tx]);
+                const double2 b23 = *reinterpret_cast<const double2*>(&s2[kk][4 * tx + 2]);
+                b[0] = b01.x; b[1] = b01.y; b[2] = b23.x; b[3] = b23.y;
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u)
@@ -71,26 +80,49 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
         }
         __syncthreads();
     }
+    const int64_t j0 = col0 + 4 * tx;
+    const bool full = (j0 + 3 < n2) && (ldk % 4) == 0;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        int64_t i = row0 + ty + 16 * u;
+        const int64_t i = row0 + ty + 16 * u;
         if (i >= m) continue;
+        TAcc val[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            int64_t j = col0 + tx + 16 * v;
-            if (j >= n2) continue;
-            TAcc val = TAcc(outputscale) * kappa<TAcc>(kind, acc[u][v]);
-            if (same && i == j) val += TAcc(diag_add);
-            if constexpr (sizeof(TAcc) == 4) {
-                if (K16 != nullptr) {
-                    const float w = (float)val * k16_scale;
-                    const __half h = __float2half_rn(w);
-                    K16[i * ldk + j] = h;
-                    K16_lo[i * ldk + j] = __float2half_rn(w - __half2float(h));
-                    continue;
+            val[v] = TAcc(outputscale) * kappa<TAcc>(kind, acc[u][v]);
+            if (same && i == j0 + v) val[v] += TAcc(diag_add);
+        }
+        if constexpr (sizeof(TAcc) == 4) {
+            if (K16 != nullptr) {
+                __half hh[4], ll[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const float w = (float)val[v] * k16_scale;
+                    hh[v] = __float2half_rn(w);
+                    ll[v] = __float2half_rn(w - __half2float(hh[v]));
                 }
+                if (full && (reinterpret_cast<uintptr_t>(K16) % 8) == 0 &&
+                    (reinterpret_cast<uintptr_t>(K16_lo) % 8) == 0) {
+                    *reinterpret_cast<uint2*>(K16 + i * ldk + j0) = *reinterpret_cast<const uint2*>(hh);
+                    *reinterpret_cast<uint2*>(K16_lo + i * ldk + j0) = *reinterpret_cast<const uint2*>(ll);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v)
+                        if (j0 + v < n2) {
+                            K16[i * ldk + j0 + v] = hh[v];
+                            K16_lo[i * ldk + j0 + v] = ll[v];
+                        }
+                }
+                continue;
             }
-            K[i * ldk + j] = (TOut)val;
+        }
+        if (full && sizeof(TOut) == 4 && (reinterpret_cast<uintptr_t>(K) % 16) == 0) {
+            *reinterpret_cast<float4*>(K + i * ldk + j0) =
+                make_float4((float)val[0], (float)val[1], (float)val[2], (float)val[3]);
+        } else {
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+                if (j0 + v < n2) K[i * ldk + j0 + v] = (TOut)val[v];
         }
     }
 }

@@ -847,7 +847,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     double* scr = gA + q * q;        // max(q*q, q*r)
     float* Lf = reinterpret_cast<float*>(scr + (q * q > q * r ? q * q : q * r));  // q x D
     float* tS = Lf + q * D;          // S
-    float* dY = tS + S;              // kSampleChunk x q
+    float* dY = tS + S;              // q x kSampleChunk
     __shared__ float s_muh[QMAX], s_mul[QMAX];
     __shared__ double s_dmu[QMAX], s_rd[QMAX];
     __shared__ int s_status;
@@ -1046,19 +1046,21 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
             }
 #pragma unroll
             for (int i = 0; i < QMAX; ++i)
-                if (i < q) dY[ls * q + i] = g[i];
+                if (i < q) dY[i * kSampleChunk + ls] = g[i];  // point-major: no bank conflicts
         }
         __syncthreads();
         for (int p = tid; p < q * D; p += kBsThreads) {
             const int i = p / D, k = p % D;
             if (k >= r + i + 1) continue;  // the upper part of br stays zero
             float cs = 0.f;
-            for (int ls = 0; ls < sc; ++ls) cs = fmaf(dY[ls * q + i], z32[(int64_t)(s0 + ls) * D + k], cs);
+            const float* dyi = dY + i * kSampleChunk;
+            for (int ls = 0; ls < sc; ++ls) cs = fmaf(dyi[ls], z32[(int64_t)(s0 + ls) * D + k], cs);
             dLq[p] += (double)cs;
         }
         for (int i = tid; i < q; i += kBsThreads) {
             float cs = 0.f;
-            for (int ls = 0; ls < sc; ++ls) cs += dY[ls * q + i];
+            const float* dyi = dY + i * kSampleChunk;
+            for (int ls = 0; ls < sc; ++ls) cs += dyi[ls];
             s_dmu[i] += (double)cs;
         }
         __syncthreads();
@@ -1181,7 +1183,7 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
     const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * E;
     if (c0 >= n) return;
     using VT = typename Vec16<T>::type;
-    T v[QM][E], h[QM][E], bc[E];
+    T v[QM][E], bc[E];
 #pragma unroll
     for (int j = 0; j < QM; ++j) {
         if constexpr (E > 1) {
@@ -1200,47 +1202,38 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
     } else {
         bc[0] = beta[c0];
     }
-#pragma unroll
-    for (int i = 0; i < QM; ++i) {
-        const T gmi = (i < q) ? gm[i] : T(0);
-#pragma unroll
-        for (int e = 0; e < E; ++e) h[i][e] = gmi * bc[e];
-#pragma unroll
-        for (int j = 0; j < QM; ++j) {
-            if (i < q && j < q) {
-                const T gij = gq[i * q + j];
-#pragma unroll
-                for (int e = 0; e < E; ++e) h[i][e] = fma(gij, v[j][e], h[i][e]);
-            }
-        }
-    }
-    for (int k = 0; k < r; ++k) {
-        T vb[E];
-        if constexpr (E > 1) {
-            const VT w = *reinterpret_cast<const VT*>(Vb + (int64_t)k * n + c0);
-#pragma unroll
-            for (int e = 0; e < E; ++e) vb[e] = Vec16<T>::at(w, e);
-        } else {
-            vb[0] = Vb[(int64_t)k * n + c0];
-        }
-#pragma unroll
-        for (int i = 0; i < QM; ++i) {
-            if (i < q) {
-                const T gik = gqb[i * r + k];
-#pragma unroll
-                for (int e = 0; e < E; ++e) h[i][e] = fma(gik, vb[e], h[i][e]);
-            }
-        }
-    }
+    // one output row at a time (the Vb rows are re-read from L1 per row)
 #pragma unroll
     for (int i = 0; i < QM; ++i) {
         if (i >= q) break;
+        T h[E];
+        const T gmi = gm[i];
+#pragma unroll
+        for (int e = 0; e < E; ++e) h[e] = gmi * bc[e];
+#pragma unroll
+        for (int j = 0; j < QM; ++j) {
+            if (j < q) {
+                const T gij = gq[i * q + j];
+#pragma unroll
+                for (int e = 0; e < E; ++e) h[e] = fma(gij, v[j][e], h[e]);
+            }
+        }
+        for (int k = 0; k < r; ++k) {
+            const T gik = gqb[i * r + k];
+            if constexpr (E > 1) {
+                const VT w = *reinterpret_cast<const VT*>(Vb + (int64_t)k * n + c0);
+#pragma unroll
+                for (int e = 0; e < E; ++e) h[e] = fma(gik, Vec16<T>::at(w, e), h[e]);
+            } else {
+                h[0] = fma(gik, Vb[(int64_t)k * n + c0], h[0]);
+            }
+        }
         const int64_t off = (rbase + i) * ldh + c0;
         if (H16 != nullptr) {
             __half hh[E], ll[E];
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                const float w = (float)h[i][e] * hs[i];
+                const float w = (float)h[e] * hs[i];
                 hh[e] = __float2half_rn(w);
                 ll[e] = __float2half_rn(w - __half2float(hh[e]));
             }
@@ -1260,10 +1253,10 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
             VT o;
             T* po = reinterpret_cast<T*>(&o);
 #pragma unroll
-            for (int e = 0; e < E; ++e) po[e] = h[i][e];
+            for (int e = 0; e < E; ++e) po[e] = h[e];
             *reinterpret_cast<VT*>(H + off) = o;
         } else {
-            H[off] = h[i][0];
+            H[off] = h[0];
         }
     }
 }
@@ -1397,24 +1390,26 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
     }
 }
 
+// Sum of the slab partials, one thread per (k, row) element (coalesced over
+// rows), compensated; the total overwrites slab 0.
+template <typename T>
+__global__ void adjoint_slab_sum_kernel(T* __restrict__ part, int64_t elems, int nslab) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= elems) return;
+    T acc = T(0), c = T(0);
+    for (int s = 0; s < nslab; ++s) comp_add<T>(acc, c, part[(int64_t)s * elems + e]);
+    part[e] = acc - c;
+}
+
 template <typename T, int DMAX>
-__global__ void __launch_bounds__(128) adjoint_finalize_kernel(QBatchArgs a, const T* __restrict__ part,
-                                                               int nslab) {
+__global__ void __launch_bounds__(128) adjoint_finalize_kernel(QBatchArgs a, const T* __restrict__ part) {
     const int64_t rows = a.b * a.q;
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= rows) return;
     const int d = a.d;
-    T gx[DMAX], gc[DMAX];  // compensated sum over the slabs
+    T gx[DMAX];
 #pragma unroll
-    for (int k = 0; k < DMAX; ++k) { gx[k] = T(0); gc[k] = T(0); }
-    for (int s = 0; s < nslab; ++s) {
-        const T* pp = part + (int64_t)s * d * rows;
-#pragma unroll
-        for (int k = 0; k < DMAX; ++k)
-            if (k < d) comp_add<T>(gx[k], gc[k], pp[(int64_t)k * rows + row]);
-    }
-#pragma unroll
-    for (int k = 0; k < DMAX; ++k) gx[k] -= gc[k];
+    for (int k = 0; k < DMAX; ++k) gx[k] = (k < d) ? part[(int64_t)k * rows + row] : T(0);
     adjoint_finish_row<T, DMAX>(a, row, gx);
 }
 
@@ -1608,13 +1603,19 @@ int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T
                                                   (int)smem));                                  \
             adjoint_kernel<T, DM, false><<<grid, kAdjRows, smem, stream>>>(a, D, ldd, XsT, slab, pp); \
             BGB_CHECK_LAUNCH();                                                                 \
+            const int64_t elems = (int64_t)a.d * rows;                                          \
+            adjoint_slab_sum_kernel<T><<<(unsigned)ceil_div(elems, 256), 256, 0, stream>>>(      \
+                pp, elems, (int)nslab);                                                         \
+            BGB_CHECK_LAUNCH();                                                                 \
             adjoint_finalize_kernel<T, DM><<<(unsigned)ceil_div(rows, 128), 128, 0, stream>>>(  \
-                a, pp, (int)nslab);                                                             \
+                a, pp);                                                                         \
             BGB_CHECK_LAUNCH();                                                                 \
         }                                                                                       \
     } while (0)
     if (a.d <= 8) BGB_ADJ(8);
+    else if (a.d <= 12) BGB_ADJ(12);
     else if (a.d <= 16) BGB_ADJ(16);
+    else if (a.d <= 20) BGB_ADJ(20);
     else if (a.d <= 24) BGB_ADJ(24);
     else if (a.d <= 32) BGB_ADJ(32);
     else if (a.d <= 64) BGB_ADJ(64);
