@@ -66,6 +66,7 @@ class _MCAcquisition:
         self.device = model.device
         self._ws = nat.Workspace(self.device)
         self._Z: dict[int, Tensor] = {}
+        self._structs: dict = {}  # (q, tensor cores) -> (BgbAcq, its Z tensor, {b: workspace bytes})
         self.check_status = True
         self.use_tensor_cores = True  # mixed path: tcgen05 GEMMs (False: FFMA GEMMs)
         self.X_pending: Tensor | None = None
@@ -114,14 +115,16 @@ class _MCAcquisition:
         if b == 0:
             empty = torch.empty(0, dtype=torch.float64, device=self.device)
             return empty, (torch.empty(0, q, d, dtype=torch.float64, device=self.device) if need_grad else None)
-        acq = self._acq_struct(q)
+        acq, ws_bytes = self._call_struct(q)
         if out is None:
             value = torch.empty(b, dtype=torch.float64, device=self.device)
             grad = torch.empty(b, q, d, dtype=torch.float64, device=self.device) if need_grad else None
             status = torch.empty(b, dtype=torch.int32, device=self.device)
         else:
             value, grad, status = out
-        wp, wb = self._ws.get(lib.bgb_acq_workspace_bytes(ctypes.byref(acq), b))
+        if b not in ws_bytes:
+            ws_bytes[b] = lib.bgb_acq_workspace_bytes(ctypes.byref(acq), b)
+        wp, wb = self._ws.get(ws_bytes[b])
         stream = nat.stream_handle(self.device)
         if need_grad:
             rc = lib.bgb_acq_forward_backward(ctypes.byref(acq), nat.ptr(Xd), b, nat.ptr(value),
@@ -139,6 +142,17 @@ class _MCAcquisition:
             if worst == nat.BGB_DEVICE_TIMEOUT:
                 raise RuntimeError("a bounded wait in a tensor-core GEMM expired")
         return value, grad
+
+    def _call_struct(self, q: int):
+        """The call struct for q points, rebuilt only when its base samples change
+        (a new baseline or pending points) or the GEMM form is switched."""
+        key = (q, bool(self.use_tensor_cores))
+        hit = self._structs.get(key)
+        if hit is None or hit[1] is not self._Z.get(q):
+            acq = self._acq_struct(q)
+            hit = (acq, self._Z.get(q), {})
+            self._structs[key] = hit
+        return hit[0], hit[2]
 
     def _device_Z(self, q: int) -> Tensor:
         if q not in self._Z:
