@@ -36,10 +36,13 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int64_t row0 = (int64_t)blockIdx.y * KB_TILE, col0 = (int64_t)blockIdx.x * KB_TILE;
     TAcc acc[4][4];
+    float2 acc2[4][2];  // packed accumulators of the float32 form
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int a = 0; a < 4; ++a) {
 #pragma unroll
         for (int b = 0; b < 4; ++b) acc[a][b] = TAcc(0);
+        acc2[a][0] = acc2[a][1] = make_float2(0.f, 0.f);
+    }
     for (int k0 = 0; k0 < d; k0 += KB_DCHUNK) {
         const int kc = min(KB_DCHUNK, d - k0);
         for (int idx = threadIdx.x; idx < KB_DCHUNK * KB_TILE; idx += blockDim.x) {
@@ -57,28 +60,52 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
             s2[kk][rr] = v2;
         }
         __syncthreads();
+        if constexpr (sizeof(TAcc) == 4) {
+            // packed float32 pairs of columns: the same correctly rounded
+            // (a - b) and fma(df, df, acc) as the scalar form, two lanes at a time
+            const float2 m1 = make_float2(-1.f, -1.f);
 #pragma unroll 4
-        for (int kk = 0; kk < kc; ++kk) {
-            TAcc a[4], b[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) a[u] = s1[kk][ty + 16 * u];
-            if constexpr (sizeof(TAcc) == 4) {
+            for (int kk = 0; kk < kc; ++kk) {
                 const float4 bv = *reinterpret_cast<const float4*>(&s2[kk][4 * tx]);
-                b[0] = bv.x; b[1] = bv.y; b[2] = bv.z; b[3] = bv.w;
-            } else {
+                const float2 b01 = make_float2(bv.x, bv.y), b23 = make_float2(bv.z, bv.w);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float au = s1[kk][ty + 16 * u];
+                    const float2 a2 = make_float2(au, au);
+                    const float2 d01 = __ffma2_rn(b01, m1, a2);
+                    const float2 d23 = __ffma2_rn(b23, m1, a2);
+                    acc2[u][0] = __ffma2_rn(d01, d01, acc2[u][0]);
+                    acc2[u][1] = __ffma2_rn(d23, d23, acc2[u][1]);
+                }
+            }
+        } else {
+#pragma unroll 4
+            for (int kk = 0; kk < kc; ++kk) {
+                TAcc a[4], b[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) a[u] = s1[kk][ty + 16 * u];
                 const double2 b01 = *reinterpret_cast<const double2*>(&s2[kk][4 * tx]);
                 const double2 b23 = *reinterpret_cast<const double2*>(&s2[kk][4 * tx + 2]);
                 b[0] = b01.x; b[1] = b01.y; b[2] = b23.x; b[3] = b23.y;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        TAcc df = a[u] - b[v];
+                        acc[u][v] += df * df;
+                    }
             }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int v = 0; v < 4; ++v) {
-                    TAcc df = a[u] - b[v];
-                    acc[u][v] += df * df;
-                }
         }
         __syncthreads();
+    }
+    if constexpr (sizeof(TAcc) == 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            acc[u][0] = acc2[u][0].x;
+            acc[u][1] = acc2[u][0].y;
+            acc[u][2] = acc2[u][1].x;
+            acc[u][3] = acc2[u][1].y;
+        }
     }
     const int64_t j0 = col0 + 4 * tx;
     const bool full = (j0 + 3 < n2) && (ldk % 4) == 0;

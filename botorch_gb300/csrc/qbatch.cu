@@ -1336,6 +1336,7 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
     const int64_t cbeg = (int64_t)blockIdx.y * slab;
     const int64_t cend = (cbeg + slab < n) ? cbeg + slab : n;
     T zx[DMAX], g[DMAX];
+    float2 zx2[DMAX / 2], g2[DMAX / 2];  // packed copies for the float32 sweep
     const bool zs = (sizeof(T) == 4) && a.zt != nullptr;
 #pragma unroll
     for (int k = 0; k < DMAX; ++k) {
@@ -1343,6 +1344,11 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
                     ? (zs ? (T)a.zt[(int64_t)k * rows + row] : (T)(a.X[row * d + k] * a.inv_ls[k]))
                     : T(0);
         g[k] = T(0);
+    }
+#pragma unroll
+    for (int v = 0; v < DMAX / 2; ++v) {
+        zx2[v] = make_float2((float)zx[2 * v], (float)zx[2 * v + 1]);
+        g2[v] = make_float2(0.f, 0.f);
     }
     for (int64_t c0 = cbeg; c0 < cend; c0 += kAdjChunk) {
         const int cc = (int)((cend - c0) < kAdjChunk ? (cend - c0) : kAdjChunk);
@@ -1356,25 +1362,56 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
             Xc[c * DMAX + k] = (c < cc && k < d) ? XsT[(int64_t)k * n + c0 + c] : T(0);
         }
         __syncthreads();
-        for (int c = 0; c < cc; ++c) {
-            const T dk = Dc[tid * LDD + c];
-            const VT* xc = reinterpret_cast<const VT*>(Xc + c * DMAX);
-            T df[DMAX];
-            T r2a = T(0), r2b = T(0);
+        if constexpr (sizeof(T) == 4) {
+            // packed float32 pairs (even, odd coordinate): the same correctly rounded
+            // operations as the scalar form below, two lanes per instruction
+            const float2 m1 = make_float2(-1.f, -1.f);
+            for (int c = 0; c < cc; ++c) {
+                const float dk = Dc[tid * LDD + c];
+                const float4* xc = reinterpret_cast<const float4*>(Xc + c * DMAX);
+                float2 df2[DMAX / 2];
+                float2 r2v = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int v = 0; v < DMAX / E; ++v) {
-                const VT x4 = xc[v];
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    const int k = v * E + e;
-                    df[k] = zx[k] - Vec16<T>::at(x4, e);
-                    if (k % 2 == 0) r2a = fma(df[k], df[k], r2a);
-                    else r2b = fma(df[k], df[k], r2b);
+                for (int v = 0; v < DMAX / 4; ++v) {
+                    const float4 x4 = xc[v];
+                    df2[2 * v] = __ffma2_rn(make_float2(x4.x, x4.y), m1, zx2[2 * v]);
+                    df2[2 * v + 1] = __ffma2_rn(make_float2(x4.z, x4.w), m1, zx2[2 * v + 1]);
+                    r2v = __ffma2_rn(df2[2 * v], df2[2 * v], r2v);
+                    r2v = __ffma2_rn(df2[2 * v + 1], df2[2 * v + 1], r2v);
                 }
-            }
-            const T coef = dk * dkappa_dr2<T>(kind, r2a + r2b);
+                const float coef = dk * dkappa_dr2<float>(kind, r2v.x + r2v.y);
+                const float2 coef2 = make_float2(coef, coef);
 #pragma unroll
-            for (int k = 0; k < DMAX; ++k) g[k] = fma(coef, df[k], g[k]);
+                for (int v = 0; v < DMAX / 2; ++v) g2[v] = __ffma2_rn(coef2, df2[v], g2[v]);
+            }
+        } else {
+            for (int c = 0; c < cc; ++c) {
+                const T dk = Dc[tid * LDD + c];
+                const VT* xc = reinterpret_cast<const VT*>(Xc + c * DMAX);
+                T df[DMAX];
+                T r2a = T(0), r2b = T(0);
+#pragma unroll
+                for (int v = 0; v < DMAX / E; ++v) {
+                    const VT x4 = xc[v];
+#pragma unroll
+                    for (int e = 0; e < E; ++e) {
+                        const int k = v * E + e;
+                        df[k] = zx[k] - Vec16<T>::at(x4, e);
+                        if (k % 2 == 0) r2a = fma(df[k], df[k], r2a);
+                        else r2b = fma(df[k], df[k], r2b);
+                    }
+                }
+                const T coef = dk * dkappa_dr2<T>(kind, r2a + r2b);
+#pragma unroll
+                for (int k = 0; k < DMAX; ++k) g[k] = fma(coef, df[k], g[k]);
+            }
+        }
+    }
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int v = 0; v < DMAX / 2; ++v) {
+            g[2 * v] = g2[v].x;
+            g[2 * v + 1] = g2[v].y;
         }
     }
     if (!active) return;
