@@ -1265,9 +1265,10 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
 // d value / d X through K(X, Xt): one thread per row of X, kAdjRows rows per CTA.
 // The training points are split into grid.y slabs, since the rows alone give
 // too few threads to hide latency. Per chunk of kAdjChunk points the CTA stages
-// the D tile of its rows (coalesced row segments) and the points' scaled
-// coordinates point-major (16-byte broadcast reads); each thread then sweeps the
-// chunk with its row's coordinates and gradient accumulator in registers:
+// the points' scaled coordinates point-major (16-byte broadcast reads); the
+// float32 form streams each thread's row of D from global memory, the float64
+// form stages the D tile of its rows. Each thread sweeps the chunk with its
+// row's coordinates and gradient accumulator in registers:
 //   g += D[i,c] kappa'(r2_ic) (z_i - zt_c),   r2_ic = |z_i - zt_c|^2.
 // One slab: the CTA finishes its rows (adjoint_finish_row). Several: each slab
 // writes its partial g to part[slab][k][row] and adjoint_finalize_kernel adds
@@ -1325,7 +1326,7 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
     static_assert(DMAX % E == 0, "DMAX must hold whole 16-byte vectors");
     extern __shared__ __align__(16) unsigned char smraw[];
     T* Xc = reinterpret_cast<T*>(smraw);              // [kAdjChunk][DMAX], point-major
-    T* Dc = Xc + (size_t)kAdjChunk * DMAX;            // [kAdjRows][kAdjChunk + 1]
+    T* Dc = Xc + (size_t)kAdjChunk * DMAX;            // [kAdjRows][kAdjChunk + 1] (float64 only)
     constexpr int LDD = kAdjChunk + 1;
     const int d = a.d, kind = a.kernel;
     const int64_t n = a.n, rows = a.b * a.q;
@@ -1353,9 +1354,11 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
     for (int64_t c0 = cbeg; c0 < cend; c0 += kAdjChunk) {
         const int cc = (int)((cend - c0) < kAdjChunk ? (cend - c0) : kAdjChunk);
         __syncthreads();
-        for (int p = tid; p < kAdjRows * kAdjChunk; p += kAdjRows) {
-            const int rr = p / kAdjChunk, c = p % kAdjChunk;
-            Dc[rr * LDD + c] = (row0 + rr < rows && c < cc) ? Dm[(row0 + rr) * ldd + c0 + c] : T(0);
+        if constexpr (sizeof(T) != 4) {
+            for (int p = tid; p < kAdjRows * kAdjChunk; p += kAdjRows) {
+                const int rr = p / kAdjChunk, c = p % kAdjChunk;
+                Dc[rr * LDD + c] = (row0 + rr < rows && c < cc) ? Dm[(row0 + rr) * ldd + c0 + c] : T(0);
+            }
         }
         for (int p = tid; p < DMAX * kAdjChunk; p += kAdjRows) {
             const int k = p / kAdjChunk, c = p % kAdjChunk;
@@ -1363,11 +1366,13 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
         }
         __syncthreads();
         if constexpr (sizeof(T) == 4) {
-            // packed float32 pairs (even, odd coordinate): the same correctly rounded
-            // operations as the scalar form below, two lanes per instruction
+            // each thread streams its own row of D from global memory (16-byte
+            // loads along the row; L1 serves the rest of each line), and the pair
+            // arithmetic runs on packed float32 pairs (even, odd coordinate): the
+            // same correctly rounded operations as the scalar form below
             const float2 m1 = make_float2(-1.f, -1.f);
-            for (int c = 0; c < cc; ++c) {
-                const float dk = Dc[tid * LDD + c];
+            const float* drow = reinterpret_cast<const float*>(Dm) + row * ldd + c0;
+            auto pair = [&](float dk, int c) {
                 const float4* xc = reinterpret_cast<const float4*>(Xc + c * DMAX);
                 float2 df2[DMAX / 2];
                 float2 r2v = make_float2(0.f, 0.f);
@@ -1383,6 +1388,20 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
                 const float2 coef2 = make_float2(coef, coef);
 #pragma unroll
                 for (int v = 0; v < DMAX / 2; ++v) g2[v] = __ffma2_rn(coef2, df2[v], g2[v]);
+            };
+            if (active) {
+                const bool vec = ((reinterpret_cast<uintptr_t>(drow) & 15) == 0);
+                int c = 0;
+                if (vec) {
+                    for (; c + 4 <= cc; c += 4) {
+                        const float4 d4 = *reinterpret_cast<const float4*>(drow + c);
+                        pair(d4.x, c);
+                        pair(d4.y, c + 1);
+                        pair(d4.z, c + 2);
+                        pair(d4.w, c + 3);
+                    }
+                }
+                for (; c < cc; ++c) pair(drow[c], c);
             }
         } else {
             for (int c = 0; c < cc; ++c) {
@@ -1593,7 +1612,9 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
 
 template <typename T, int DMAX>
 size_t adjoint_smem_bytes() {
-    return sizeof(T) * ((size_t)kAdjChunk * DMAX + (size_t)kAdjRows * (kAdjChunk + 1));
+    // float32 rows stream D from global memory; float64 stages its D tile
+    return sizeof(T) * ((size_t)kAdjChunk * DMAX +
+                        (sizeof(T) == 4 ? 0 : (size_t)kAdjRows * (kAdjChunk + 1)));
 }
 
 // part_cap: elements of scratch available for the slab partials (0: one slab).
