@@ -421,26 +421,34 @@ __device__ __forceinline__ double dpareto2(double x) {
     return -4.0 * (1.0 + x) / (den * den);
 }
 
-// float32 forms for the mixed path (the argument v = u / tau is formed in float64)
-__device__ __forceinline__ float softplus_f(float x) { return x > 20.f ? x : log1pf(expf(x)); }
-__device__ __forceinline__ float softplus_grad_f(float x) {
-    if (x > 20.f) return 1.f;
-    const float z = expf(x);
-    return z / (z + 1.f);
-}
-// log_fatplus(u) = log(tau) + log(h(v)), d/du = h'(v) / (tau h(v)), v = u / tau
+// float32 forms for the mixed path. One exponential serves softplus and its
+// derivative; the divisions and the outer logarithm use the fast intrinsics
+// (__fdividef, __logf: a few ulp), far inside the per-sample error budget.
+// log_fatplus(u) = log(tau) + log(h(v)), d/du = h'(v) / (tau h(v)), v = u / tau,
+// h(v) = softplus(v) + 0.1 / (1 + v^2)
 __device__ __forceinline__ void log_fatplus_f(float v, float log_tau, float inv_tau, float& li,
                                               float& dli) {
-    const float c = 1.f / (1.f + v * v);
-    const float h = softplus_f(v) + 0.1f * c;
-    const float hp = softplus_grad_f(v) - 0.2f * v * c * c;
-    li = log_tau + logf(h);
-    dli = hp * inv_tau / h;
+    const float c = __fdividef(1.f, fmaf(v, v, 1.f));
+    float sp, sg;
+    if (v > 20.f) {  // torch softplus threshold (beta = 1)
+        sp = v;
+        sg = 1.f;
+    } else {
+        const float e = __expf(v);
+        sp = log1pf(e);
+        sg = __fdividef(e, e + 1.f);
+    }
+    const float h = fmaf(0.1f, c, sp);
+    const float hp = sg - 0.2f * v * c * c;
+    li = log_tau + __logf(h);
+    dli = __fdividef(hp * inv_tau, h);
 }
-__device__ __forceinline__ float pareto2_f(float x) { return 2.f / (2.f + 2.f * x + x * x); }
+__device__ __forceinline__ float pareto2_f(float x) {
+    return __fdividef(2.f, 2.f + 2.f * x + x * x);
+}
 __device__ __forceinline__ float dpareto2_f(float x) {
     const float den = 2.f + 2.f * x + x * x;
-    return -4.f * (1.f + x) / (den * den);
+    return __fdividef(-4.f * (1.f + x), den * den);
 }
 
 // In-place Cholesky of a q x q row-major matrix (lower). Returns 0 or pivot+1.
@@ -770,25 +778,29 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) 
     e = (a - (s - bb)) + (b - bb);
 }
 
-// u_i (i < q) of one sample; zs: the sample's D base-sample coordinates
+// u_i (i < q) of one sample; zs: the sample's D base-sample coordinates; LfT:
+// [bl, br] k-major with QMAX entries per k (zero above the diagonal of br and
+// for i >= q), so pairs of points take one packed FMA per coordinate
 template <int QMAX>
-__device__ __forceinline__ void sample_u(const float* __restrict__ Lf, const float* __restrict__ zs,
-                                         int q, int r, int D, const float* muh, const float* mul,
-                                         float bh, float bl, float* u) {
-    float y[QMAX];
+__device__ __forceinline__ void sample_u(const float* __restrict__ LfT, const float* __restrict__ zs,
+                                         int q, int D, const float* muh, const float* mul, float bh,
+                                         float bl, float* u) {
+    float2 y2[QMAX / 2];
 #pragma unroll
-    for (int i = 0; i < QMAX; ++i) y[i] = 0.f;
+    for (int j = 0; j < QMAX / 2; ++j) y2[j] = make_float2(0.f, 0.f);
     for (int k = 0; k < D; ++k) {
         const float zk = zs[k];
+        const float2 z2 = make_float2(zk, zk);
+        const float2* L2 = reinterpret_cast<const float2*>(LfT + k * QMAX);
 #pragma unroll
-        for (int i = 0; i < QMAX; ++i)
-            if (i < q && k < r + i + 1) y[i] = fmaf(Lf[i * D + k], zk, y[i]);
+        for (int j = 0; j < QMAX / 2; ++j) y2[j] = __ffma2_rn(L2[j], z2, y2[j]);
     }
 #pragma unroll
     for (int i = 0; i < QMAX; ++i) {
         float dh, e;
         two_sum_f(muh[i], -bh, dh, e);
-        u[i] = (i < q) ? dh + ((e + (mul[i] - bl)) + y[i]) : 0.f;
+        const float y = (i % 2 == 0) ? y2[i / 2].x : y2[i / 2].y;
+        u[i] = (i < q) ? dh + ((e + (mul[i] - bl)) + y) : 0.f;
     }
 }
 
@@ -845,8 +857,8 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     double* dLq = Lq + q * D;        // q x D
     double* gA = dLq + q * D;        // q x q
     double* scr = gA + q * q;        // max(q*q, q*r)
-    float* Lf = reinterpret_cast<float*>(scr + (q * q > q * r ? q * q : q * r));  // q x D
-    float* tS = Lf + q * D;          // S
+    float* Lf = reinterpret_cast<float*>(scr + (q * q > q * r ? q * q : q * r));  // D x QMAX (k-major)
+    float* tS = Lf + D * QMAX;       // S
     float* dY = tS + S;              // q x kSampleChunk
     __shared__ float s_muh[QMAX], s_mul[QMAX];
     __shared__ double s_dmu[QMAX], s_rd[QMAX];
@@ -911,7 +923,10 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
         fail(s_status);
         return;
     }
-    for (int p = tid; p < q * D; p += kBsThreads) Lf[p] = (float)Lq[p];
+    for (int p = tid; p < D * QMAX; p += kBsThreads) {
+        const int k = p / QMAX, i = p % QMAX;
+        Lf[p] = (i < q) ? (float)Lq[i * D + k] : 0.f;
+    }
     __syncthreads();
     const bool qei = (a.acqf == BGB_ACQF_QEI);
     const float inv_tau = (float)(1.0 / a.tau_relu);
@@ -923,7 +938,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     int local_bad = 0;
     for (int s = tid; s < S; s += kBsThreads) {
         float u[QMAX];
-        sample_u<QMAX>(Lf, z32 + (int64_t)s * D, q, r, D, s_muh, s_mul, bf32[2 * s], bf32[2 * s + 1], u);
+        sample_u<QMAX>(Lf, z32 + (int64_t)s * D, q, D, s_muh, s_mul, bf32[2 * s], bf32[2 * s + 1], u);
         float Mx = -INFINITY, li[QMAX];
 #pragma unroll
         for (int i = 0; i < QMAX; ++i) {
@@ -943,7 +958,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
 #pragma unroll
             for (int i = 0; i < QMAX; ++i)
                 if (i < q) P += pareto2_f((Mx - li[i]) * inv_taum);
-            t = Mx + taum * logf(P);
+            t = Mx + taum * __logf(P);
         }
         tS[s] = t;
     }
@@ -964,7 +979,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     float part = 0.f;
     for (int s = tid; s < S; s += kBsThreads) {
         if (qei) part += tS[s];
-        else if (!isinf(mx)) part += expf(tS[s] - mx);
+        else if (!isinf(mx)) part += __expf(tS[s] - mx);
     }
     double acc = (double)part;
 #pragma unroll
@@ -1001,7 +1016,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
         for (int ls = tid; ls < sc; ls += kBsThreads) {
             const int s = s0 + ls;
             float u[QMAX], li[QMAX], dli[QMAX], g[QMAX];
-            sample_u<QMAX>(Lf, z32 + (int64_t)s * D, q, r, D, s_muh, s_mul, bf32[2 * s], bf32[2 * s + 1], u);
+            sample_u<QMAX>(Lf, z32 + (int64_t)s * D, q, D, s_muh, s_mul, bf32[2 * s], bf32[2 * s + 1], u);
             float Mx = -INFINITY;
 #pragma unroll
             for (int i = 0; i < QMAX; ++i) {
@@ -1027,9 +1042,9 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
                         P += pareto2_f(x);
                         Pd += dpareto2_f(x);
                     }
-                    t = Mx + taum * logf(P);
+                    t = Mx + taum * __logf(P);
                 }
-                const float ws = inf_mx ? (t == mx ? 1.f : 0.f) : expf(t - lse_f);
+                const float ws = inf_mx ? (t == mx ? 1.f : 0.f) : __expf(t - lse_f);
                 if (isinf(Mx)) {
 #pragma unroll
                     for (int i = 0; i < QMAX; ++i) g[i] = (i < q && li[i] == Mx) ? ws : 0.f;
@@ -1501,8 +1516,9 @@ size_t batch_step_smem_bytes(int q, int r, int S) {
 
 size_t batch_step_f32_smem_bytes(int q, int r, int S) {
     const int D = r + q;
+    const int qmax = q <= 4 ? 4 : q <= 8 ? 8 : q <= 16 ? 16 : 32;
     return sizeof(double) * (size_t)(2 * q * q + 2 * q * D + (q * q > q * r ? q * q : q * r)) +
-           sizeof(float) * (size_t)(q * D + S + kSampleChunk * q);
+           sizeof(float) * (size_t)(D * qmax + S + kSampleChunk * q);
 }
 
 int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bool mixed) {
