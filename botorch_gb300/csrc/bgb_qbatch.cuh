@@ -62,7 +62,8 @@ int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc
 int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bool mixed = false);
 size_t batch_step_smem_bytes(int q, int r, int S);
 // H (b*q x n) = gmu beta^T - 2 Gqq V - Gqb Vb per t-batch
-// H_lo non-null (float32): write the tf32 hi/lo split (H = hi) with leading dimension ldh.
+// H16 non-null (float32 only): write H as the row-scaled float16 hi/lo split
+// (H16, H16_lo, leading dimension ldh) with the inverse row scales in a.hmul.
 template <typename T>
 int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, const T* beta, T* H,
                     cudaStream_t stream, __half* H16 = nullptr, __half* H16_lo = nullptr,

@@ -199,7 +199,7 @@ template <> struct Ops<float> {
         return gemm_f32(M, N, K, A, lda, B, ldb, C, ldc, kmode, n_tri, st);
     }
     // K(X, Xt) in float32 from the scaled coordinates (zt: d x rows, Xs32: d x n);
-    // K_lo non-null: the tf32 hi / lo split with leading dimension ldk
+    // K16 non-null: the float16 hi / lo split of k16_scale * K with leading dimension ldk
     static int kmat(const bgb_acq_t* a, const double* X, int64_t rows, float* zt, float* K,
                     int64_t ldk, __half* K16, __half* K16_lo, float k16_scale, cudaStream_t st) {
         const int64_t tot = rows * a->gp.d;

@@ -42,9 +42,12 @@ extern "C" {
 #define BGB_KERNEL_RBF 3
 
 /* Arithmetic of the per-call path. FP64: every step in float64 (the plain
- * FP64 GPU path). MIXED: kernel build, cross-covariance GEMM and adjoint in
- * float32, everything that stability needs (q x q Cholesky, sample step,
- * log-mean-exp, all reductions across tiles) in float64. */
+ * FP64 GPU path). MIXED: kernel build, row mix and adjoint in float32, the
+ * cross-covariance GEMMs on float16 hi/lo splits with float32 accumulation
+ * (tensor cores) or in float32 (BGB_FLAG_SIMT); the q x q algebra (Sigma
+ * assembly, psd_safe_cholesky, its adjoint) and every sum across tiles, lanes,
+ * samples and slabs in float64 or compensated float32; per-sample improvements
+ * in float32 from exact float pairs of mu and best_f. */
 #define BGB_PREC_FP64 0
 #define BGB_PREC_MIXED 1
 

@@ -156,7 +156,7 @@ def test_qlognei_differentiation_config(cuda_lib, precision):
         # dominant MC samples lie within ~100 tau_relu of the incumbent amplify it by
         # up to 1 / tau_relu. Here one such t-batch (gradient norm ~8e3) holds ~95% of
         # the gradient error: a float32 (FFMA) emulation of the path reaches 1.3e-3,
-        # the 3xTF32 tensor-core form ~1e-2. The mixed bar of this path (1e-5 value,
+        # the float16-split tensor-core form ~1e-2. The mixed bar of this path (1e-5 value,
         # 1e-4 gradient) is held on the headline workload.
         assert rel(v[idx], ov) < 1e-4, rel(v[idx], ov)
         assert rel(X.grad[idx], og) < 5e-2, rel(X.grad[idx], og)
