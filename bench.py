@@ -221,16 +221,19 @@ def run_ours(args) -> None:
     out = (torch.empty(b, dtype=torch.float64, device=device),
            torch.empty(b, Q, DIM, dtype=torch.float64, device=device),
            torch.empty(b, dtype=torch.int32, device=device))
-    step = lambda: acqf.value_and_grad_raw(Xd, True, check=False, out=out)  # noqa: E731
+    eager_step = lambda: acqf.value_and_grad_raw(Xd, True, check=False, out=out)  # noqa: E731
+    # the timed step: the whole call replayed from a CUDA graph (captured on the first call)
+    step = lambda: acqf.graphed_value_and_grad(Xd, True, check=False)  # noqa: E731
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     for _ in range(max(args.warmup, 3)):
+        eager_step()
         step()
     torch.cuda.synchronize(device)
     if args.profile:
         torch.cuda.profiler.start()
         for _ in range(args.steps):
             flush.zero_()
-            step()
+            eager_step()
         torch.cuda.synchronize(device)
         torch.cuda.profiler.stop()
         print(json.dumps({"profile_steps": args.steps, "b": b, "status_ok": int(out[2].max().item()) == 0}))
@@ -239,18 +242,24 @@ def run_ours(args) -> None:
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(device)
-    launches0 = lib.bgb_launch_count()
     with ClockSampler(local) as clk:
         t_wall0 = time.perf_counter()
         step_ms = time_steps(step, args.steps, device, flush)
         t_wall = time.perf_counter() - t_wall0
-    launches = lib.bgb_launch_count() - launches0
+    # graph replays bypass the host-side counter: each replay runs the launches
+    # recorded when the call was captured
+    launches = acqf.graph_launches(b, Q) * args.steps
     torch.cuda.synchronize(device)
+    launches0 = lib.bgb_launch_count()
+    eager_ms = time_steps(eager_step, max(3, min(args.steps, 5)), device, flush)
+    eager_launches_per_step = (lib.bgb_launch_count() - launches0) / len(eager_ms)
     total_ms = replicas.max_over_ranks(sum(step_ms), device)
     if world > 1:
         torch.distributed.barrier()
-    status_ok = int(out[2].max().item()) == 0
+    graph_status = acqf._graphs[(b, Q, True, bool(acqf.use_tensor_cores))]["out"][2]
+    status_ok = int(out[2].max().item()) == 0 and int(graph_status.max().item()) == 0
     value = replicas.evals_per_second(world, b, args.steps, total_ms)
+    eager_value = replicas.evals_per_second(1, b, len(eager_ms), sum(eager_ms))
 
     # roofline of the cross-covariance GEMMs, timed live per stage
     import ctypes
@@ -288,6 +297,8 @@ def run_ours(args) -> None:
     Xh = w.X.clone().pin_memory()
     vh = torch.empty(b, dtype=torch.float64).pin_memory()
     gh = torch.empty(b, Q, DIM, dtype=torch.float64).pin_memory()
+
+    acqf.use_cuda_graphs = True
 
     def e2e_step():
         X = Xh.to(device, non_blocking=True).requires_grad_(True)
@@ -353,7 +364,10 @@ def run_ours(args) -> None:
                                 "f64 accumulations", "l2": "flushed before each step (256 MB write)",
                    "parallelism": f"replicas, weak scaling over t-batches x{world}"},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
-        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "gpu_launches": int(launches), "launch_mode": "CUDA graph replay of the whole call",
+        "launches_per_step": acqf.graph_launches(b, Q),
+        "eager_evals_per_s": round(eager_value, 1),
+        "eager_launches_per_step": eager_launches_per_step, "clocks": clk.summary(),
         "stage_ms": {k: round(v, 4) for k, v in zip(names, st)},
         "fp64_gpu_evals_per_s": round(fp64_evals, 1),
         "speedup_vs_fp64_gpu": round(value / world / fp64_evals, 2),

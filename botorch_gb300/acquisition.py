@@ -67,8 +67,13 @@ class _MCAcquisition:
         self._ws = nat.Workspace(self.device)
         self._Z: dict[int, Tensor] = {}
         self._structs: dict = {}  # (q, tensor cores) -> (BgbAcq, its Z tensor, {b: workspace bytes})
+        self._graphs: dict = {}   # (b, q, need_grad, tensor cores) -> captured call
         self.check_status = True
         self.use_tensor_cores = True  # mixed path: tcgen05 GEMMs (False: FFMA GEMMs)
+        # forward through CUDA graphs captured per (b, q): for loops that call with
+        # a fixed shape (the restarts of an optimiser); each shape keeps its own
+        # workspace while captured
+        self.use_cuda_graphs = False
         self.X_pending: Tensor | None = None
 
     # -------------------------------------------------------------- override
@@ -100,7 +105,12 @@ class _MCAcquisition:
             raise ValueError(f"expected d={self.model.d}, got {d}")
         Xd = Xf.detach().reshape(-1, q, d).to(self.device, torch.float64).contiguous()
         b = Xd.shape[0]
-        value, grad = self.value_and_grad_raw(Xd, need_grad)
+        if self.use_cuda_graphs and b > 0:
+            value, grad = self.graphed_value_and_grad(Xd, need_grad)
+            value = value.clone()  # the graph's buffers are overwritten by the next replay
+            grad = grad.clone() if grad is not None else None
+        else:
+            value, grad = self.value_and_grad_raw(Xd, need_grad)
         value = value.reshape(batch_shape).to(X.dtype)
         if grad is not None:
             grad = grad[:, : X.shape[-2], :]  # pending points (appended last) carry no gradient
@@ -108,7 +118,7 @@ class _MCAcquisition:
         return value, grad
 
     def value_and_grad_raw(self, Xd: Tensor, need_grad: bool, check: bool | None = None,
-                           out: tuple | None = None):
+                           out: tuple | None = None, ws: "nat.Workspace | None" = None):
         """Native call on a contiguous float64 ``b x q x d`` device tensor."""
         lib = nat.lib()
         b, q, d = Xd.shape
@@ -124,7 +134,7 @@ class _MCAcquisition:
             value, grad, status = out
         if b not in ws_bytes:
             ws_bytes[b] = lib.bgb_acq_workspace_bytes(ctypes.byref(acq), b)
-        wp, wb = self._ws.get(ws_bytes[b])
+        wp, wb = (ws or self._ws).get(ws_bytes[b])
         stream = nat.stream_handle(self.device)
         if need_grad:
             rc = lib.bgb_acq_forward_backward(ctypes.byref(acq), nat.ptr(Xd), b, nat.ptr(value),
@@ -134,14 +144,69 @@ class _MCAcquisition:
                                      nat.ptr(status), wp, wb, stream)
         nat.check(rc, type(self).__name__)
         if (self.check_status if check is None else check):
-            worst = int(status.max().item()) if b > 0 else 0
-            if worst == nat.BGB_NOT_PSD:
-                raise NotPSDError("q x q posterior covariance not positive definite after jitter")
-            if worst == nat.BGB_NAN:
-                raise NanError("Samples contain nans or infs.")
-            if worst == nat.BGB_DEVICE_TIMEOUT:
-                raise RuntimeError("a bounded wait in a tensor-core GEMM expired")
+            self._raise_for_status(status)
         return value, grad
+
+    @staticmethod
+    def _raise_for_status(status: Tensor) -> None:
+        worst = int(status.max().item()) if status.numel() > 0 else 0
+        if worst == nat.BGB_NOT_PSD:
+            raise NotPSDError("q x q posterior covariance not positive definite after jitter")
+        if worst == nat.BGB_NAN:
+            raise NanError("Samples contain nans or infs.")
+        if worst == nat.BGB_DEVICE_TIMEOUT:
+            raise RuntimeError("a bounded wait in a tensor-core GEMM expired")
+
+    def graphed_value_and_grad(self, Xd: Tensor, need_grad: bool = True,
+                               check: bool | None = None) -> tuple[Tensor, Tensor | None]:
+        """``value_and_grad_raw`` replayed from a CUDA graph.
+
+        The first call for a (b, q, need_grad) shape runs the call once to set up
+        the library's state, then captures it into a CUDA graph with its own
+        input, output and workspace buffers; later calls copy ``Xd`` into the
+        captured input and replay the graph (one launch for the whole call).
+        The returned tensors are the graph's output buffers: the next replay for
+        the same shape overwrites them. A new baseline or pending points give new
+        base samples and a new capture.
+        """
+        b, q, d = Xd.shape
+        key = (b, q, bool(need_grad), bool(self.use_tensor_cores))
+        entry = self._graphs.get(key)
+        acq, _ = self._call_struct(q)
+        if entry is not None and entry["acq"] is not acq:
+            entry = None  # the call struct changed: capture again
+        if entry is None:
+            dev = self.device
+            Xs = Xd.detach().clone()
+            out = (torch.empty(b, dtype=torch.float64, device=dev),
+                   torch.empty(b, q, d, dtype=torch.float64, device=dev) if need_grad else None,
+                   torch.empty(b, dtype=torch.int32, device=dev))
+            ws = nat.Workspace(dev)
+            side = torch.cuda.Stream(dev)
+            side.wait_stream(torch.cuda.current_stream(dev))
+            with torch.cuda.stream(side):
+                self.value_and_grad_raw(Xs, need_grad, check=False, out=out, ws=ws)
+            torch.cuda.current_stream(dev).wait_stream(side)
+            torch.cuda.synchronize(dev)
+            lib = nat.lib()
+            graph = torch.cuda.CUDAGraph()
+            n0 = lib.bgb_launch_count()
+            with torch.cuda.graph(graph):
+                self.value_and_grad_raw(Xs, need_grad, check=False, out=out, ws=ws)
+            entry = dict(graph=graph, X=Xs, out=out, ws=ws, acq=acq,
+                         launches=lib.bgb_launch_count() - n0)
+            self._graphs[key] = entry
+        entry["X"].copy_(Xd)
+        entry["graph"].replay()
+        value, grad, status = entry["out"]
+        if (self.check_status if check is None else check):
+            self._raise_for_status(status)
+        return value, grad
+
+    def graph_launches(self, b: int, q: int, need_grad: bool = True) -> int:
+        """Kernel launches of this library inside the captured graph for one shape."""
+        entry = self._graphs.get((b, q, bool(need_grad), bool(self.use_tensor_cores)))
+        return 0 if entry is None else int(entry["launches"])
 
     def _call_struct(self, q: int):
         """The call struct for q points, rebuilt only when its base samples change
