@@ -56,6 +56,9 @@ def parse():
                    help="only warm up and run --steps mixed-precision steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     p.add_argument("--simt", action="store_true", help="FFMA GEMMs instead of tcgen05")
+    p.add_argument("--profile-fit", action="store_true",
+                   help="only build the model (training-side fit and operands) between "
+                        "cudaProfilerStart/Stop, then exit")
     return p.parse_args()
 
 
@@ -213,6 +216,16 @@ def run_ours(args) -> None:
     b = args.b
     w = T.qlognei_branin(n=N_TRAIN, b=b, q=Q, d=DIM, seed=0)
     w.X = replicas.rank_candidates(w.X, rank)  # weak scaling: every rank its own candidates
+    if args.profile_fit:
+        make_model(device, w)  # warm-up: library load, first-use attributes
+        torch.cuda.synchronize(device)
+        torch.cuda.profiler.start()
+        m = make_model(device, w)
+        m.operands("mixed")
+        torch.cuda.synchronize(device)
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_fit": True, "n": N_TRAIN, "jitter": m.train_jitter}))
+        return
     model = make_model(device, w)
     acqf = make_acqf(model, w, "mixed")
     acqf.check_status = False

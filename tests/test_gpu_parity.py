@@ -291,3 +291,28 @@ def test_headline_fp64_matches_oracle(cuda_lib):
     v.sum().backward()
     ov, og = fixture("qlognei_branin_value")[: len(sel)], fixture("qlognei_branin_grad")[: len(sel)]
     assert rel(v[sel], ov) < 1e-9 and rel(X.grad[sel], og) < 1e-9
+
+
+def test_large_n_precision_config(cuda_lib, capsys):
+    """Precision configuration at n=8192 (d=20, q=8, 512 samples): the mixed path
+    (float16-split tensor-core GEMMs) against the float64 GPU path, which the
+    other tests hold to 1e-9 of the oracle. Errors reported per output."""
+    w = T.qlognei_branin(n=8192, b=64, q=8, d=20)
+    gm = gpu_model(w)
+    res = {}
+    for precision in ("fp64", "mixed"):
+        torch.manual_seed(0)
+        a = qLogNoisyExpectedImprovement(gm, w.train_X, sampler=SobolQMCNormalSampler(
+            torch.Size([512]), seed=0), precision=precision)
+        X = w.X.to(DEV).requires_grad_(True)
+        v = a(X)
+        v.sum().backward()
+        res[precision] = (v.detach().cpu(), X.grad.cpu())
+    (v64, g64), (vm, gm_) = res["fp64"], res["mixed"]
+    ev, eg = rel(vm, v64), rel(gm_, g64)
+    per_value = ((vm - v64).abs() / v64.abs()).max().item()
+    per_grad = ((gm_ - g64).norm(dim=(1, 2)) / g64.norm(dim=(1, 2))).max().item()
+    with capsys.disabled():
+        print(f"\nn=8192 mixed vs fp64: value {ev:.2e} (max per t-batch {per_value:.2e}), "
+              f"grad {eg:.2e} (max per t-batch {per_grad:.2e})")
+    assert ev < 1e-5 and eg < 1e-4, (ev, eg)
