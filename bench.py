@@ -56,6 +56,10 @@ def parse():
                    help="only warm up and run --steps mixed-precision steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     p.add_argument("--simt", action="store_true", help="FFMA GEMMs instead of tcgen05")
+    p.add_argument("--config", default="headline", choices=["headline", "many_gps"],
+                   help="many_gps: 64 GPs of uneven size in one tuned CUDA-graph launch "
+                        "(prints its own JSON line)")
+    p.add_argument("--streams", type=int, default=8, help="streams of the many-GP graph")
     p.add_argument("--profile-fit", action="store_true",
                    help="only build the model (training-side fit and operands) between "
                         "cudaProfilerStart/Stop, then exit")
@@ -269,7 +273,7 @@ def run_ours(args) -> None:
     total_ms = replicas.max_over_ranks(sum(step_ms), device)
     if world > 1:
         torch.distributed.barrier()
-    graph_status = acqf._graphs[(b, Q, True, bool(acqf.use_tensor_cores))]["out"][2]
+    graph_status = acqf._graphs[(b, Q, True, bool(acqf.use_tensor_cores), 0)]["out"][2]
     status_ok = int(out[2].max().item()) == 0 and int(graph_status.max().item()) == 0
     value = replicas.evals_per_second(world, b, args.steps, total_ms)
     eager_value = replicas.evals_per_second(1, b, len(eager_ms), sum(eager_ms))
@@ -391,6 +395,82 @@ def run_ours(args) -> None:
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------- many GPs
+MANY_METRIC = ("qLogNEI value+grad evals/sec, 64 GPs (n ~ logU[100,4000], d ~ U{4..30}), "
+               "256 restarts x q=2, S=256, one CUDA-graph launch")
+
+
+def run_many_gps(args) -> None:
+    from botorch_gb300 import SobolQMCNormalSampler, qLogNoisyExpectedImprovement
+    from botorch_gb300 import testing as T
+    from botorch_gb300.batched import Autotuner, ModelBatch, apply_schedule
+
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    works = T.many_gps(64, seed=0)
+    t0 = time.perf_counter()
+    acqfs, Xs = [], []
+    for w in works:
+        m = make_model(device, w)
+        torch.manual_seed(0)
+        acqfs.append(qLogNoisyExpectedImprovement(m, w.train_X, sampler=SobolQMCNormalSampler(
+            torch.Size([w.n_samples]), seed=w.seed), precision="mixed"))
+        Xs.append(w.X.to(device).contiguous())
+    init_s = time.perf_counter() - t0
+    evals = sum(x.shape[0] for x in Xs)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    def timed(fn, steps):
+        times = []
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        return times
+
+    # eager: one model after the other, library-default schedule
+    for a in acqfs:
+        apply_schedule(a, (True, 0))
+
+    def eager():
+        for a, x in zip(acqfs, Xs):
+            a.value_and_grad_raw(x, True, check=False)
+
+    for _ in range(max(args.warmup, 3)):
+        eager()
+    eager_ms = timed(eager, args.steps)
+    tuner = Autotuner()
+    mb = ModelBatch(acqfs, [tuple(x.shape) for x in Xs], n_streams=args.streams, tuner=tuner)
+    for _ in range(max(args.warmup, 3)):
+        mb.value_and_grad(Xs, check=False)
+    graph_ms = timed(lambda: mb.value_and_grad(Xs, check=False), args.steps)
+    status_ok = all(int(o[2].max().item()) == 0 for o in mb.out)
+    choices = {}
+    for key, sched in tuner.choice.items():
+        label = f"{'tcgen05' if sched[0] else 'ffma'}/adj{sched[1] or 16}"
+        choices[label] = choices.get(label, 0) + 1
+    line = {
+        "metric": MANY_METRIC, "value": round(evals * args.steps / (sum(graph_ms) / 1e3), 1),
+        "unit": "evals/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(sum(graph_ms) / len(graph_ms), 4), "higher_is_better": True,
+        "dtype": "f16-split+f32+f64", "data": "synthetic (seeded RFF GP draws)",
+        "config": {"workload": "many_gps_64", "models": len(acqfs),
+                   "n": sorted(int(a.model.n) for a in acqfs),
+                   "restarts_per_model": 256, "q": 2, "mc_samples": 256,
+                   "l2": "flushed before each step (256 MB write)", "streams": mb.n_streams},
+        "eager_sequential_evals_per_s": round(evals * args.steps / (sum(eager_ms) / 1e3), 1),
+        "gpu_launches": int(mb.launches * args.steps), "launches_per_step": int(mb.launches),
+        "schedule_buckets": len(tuner.choice), "schedule_choices": choices,
+        "init_s": round(init_s, 2), "status_ok": status_ok,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- reference arm
 def run_reference(args) -> None:
     world, rank, _ = dist_info()
@@ -434,6 +514,8 @@ def main() -> None:
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "many_gps":
+        run_many_gps(args)
     else:
         run_ours(args)
 

@@ -19,6 +19,8 @@ BGB_NOT_PSD = 1
 BGB_NAN = 2
 BGB_DEVICE_TIMEOUT = 3
 BGB_FLAG_SIMT = 1
+BGB_FLAG_ADJ_CTAS_SHIFT = 8
+BGB_FLAG_ADJ_CTAS_MASK = 0xFF00
 BGB_ERR_ARG = -1
 BGB_ERR_WORKSPACE = -2
 BGB_ERR_CUDA = -3

@@ -74,6 +74,8 @@ class _MCAcquisition:
         # a fixed shape (the restarts of an optimiser); each shape keeps its own
         # workspace while captured
         self.use_cuda_graphs = False
+        # schedule knob: CTAs per SM the adjoint contraction aims for (0: library default)
+        self.adjoint_ctas_per_sm = 0
         self.X_pending: Tensor | None = None
 
     # -------------------------------------------------------------- override
@@ -170,7 +172,7 @@ class _MCAcquisition:
         base samples and a new capture.
         """
         b, q, d = Xd.shape
-        key = (b, q, bool(need_grad), bool(self.use_tensor_cores))
+        key = (b, q, bool(need_grad), bool(self.use_tensor_cores), int(self.adjoint_ctas_per_sm))
         entry = self._graphs.get(key)
         acq, _ = self._call_struct(q)
         if entry is not None and entry["acq"] is not acq:
@@ -205,16 +207,18 @@ class _MCAcquisition:
 
     def graph_launches(self, b: int, q: int, need_grad: bool = True) -> int:
         """Kernel launches of this library inside the captured graph for one shape."""
-        entry = self._graphs.get((b, q, bool(need_grad), bool(self.use_tensor_cores)))
+        entry = self._graphs.get((b, q, bool(need_grad), bool(self.use_tensor_cores),
+                                  int(self.adjoint_ctas_per_sm)))
         return 0 if entry is None else int(entry["launches"])
 
     def _call_struct(self, q: int):
         """The call struct for q points, rebuilt only when its base samples change
         (a new baseline or pending points) or the GEMM form is switched."""
-        key = (q, bool(self.use_tensor_cores))
+        key = (q, bool(self.use_tensor_cores), int(self.adjoint_ctas_per_sm))
         hit = self._structs.get(key)
         if hit is None or hit[1] is not self._Z.get(q):
             acq = self._acq_struct(q)
+            acq.flags |= (int(self.adjoint_ctas_per_sm) << nat.BGB_FLAG_ADJ_CTAS_SHIFT) & nat.BGB_FLAG_ADJ_CTAS_MASK
             hit = (acq, self._Z.get(q), {})
             self._structs[key] = hit
         return hit[0], hit[2]

@@ -42,6 +42,7 @@ struct QBatchArgs {
     float* z32;             // mixed: Z in float32 (S x (r+q))
     float* bf32;            // mixed: best_f per sample as float (hi, lo) pairs (S x 2)
     double beta_absmax;     // max |beta| (row-scale bound of the float16 adjoint operand)
+    int adj_ctas_per_sm;    // adjoint slab split target (0: default)
     float* hmul;            // tensor cores: b*q inverse row scales of the float16 H
 };
 

@@ -163,6 +163,7 @@ void fill_qargs(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa) 
     qa->Z = a->Z;
     qa->best_f = a->best_f;
     qa->beta_absmax = a->beta_absmax;
+    qa->adj_ctas_per_sm = (a->flags & BGB_FLAG_ADJ_CTAS_MASK) >> BGB_FLAG_ADJ_CTAS_SHIFT;
 }
 
 int valid_acq(const bgb_acq_t* a) {

@@ -1640,8 +1640,8 @@ int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T
     const int64_t rows = a.b * a.q;
     if (rows <= 0) return BGB_OK;
     const int64_t row_blocks = ceil_div(rows, kAdjRows);
-    // slabs: about four waves of four CTAs per SM, slabs of whole chunks, partials
-    // within part_cap
+    // slabs: a.adj_ctas_per_sm CTAs per SM (default 16: about four waves of four
+    // resident CTAs), slabs of whole chunks, partials within part_cap
     static int num_sms = 0;
     if (num_sms == 0) {
         int dev = 0, v = 0;
@@ -1650,7 +1650,8 @@ int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T
         num_sms = v > 0 ? v : 1;
     }
     const int64_t chunks = ceil_div(a.n, kAdjChunk);
-    int64_t nslab = ceil_div((int64_t)num_sms * 16, row_blocks);
+    const int64_t per_sm = a.adj_ctas_per_sm > 0 ? a.adj_ctas_per_sm : 16;
+    int64_t nslab = ceil_div((int64_t)num_sms * per_sm, row_blocks);
     if (nslab > chunks) nslab = chunks;
     if (nslab > 65535) nslab = 65535;
     if (part == nullptr || part_cap <= 0) nslab = 1;

@@ -16,6 +16,10 @@ the reference). The generators are:
   n=4096 is the headline point, n=8192 the large-n precision case.
 * ``rff_draw``: y = sqrt(2/F) sum_i w_i cos(omega_i . x + beta_i) + noise,
   the random-feature GP draw of the many-model and optimisation workloads.
+* ``many_gps``: independent problems of uneven size, n ~ log-uniform [100, 4000]
+  and d ~ uniform {4..30} per model, X ~ U[0,1]^d, y = an RFF draw (1024
+  features, lengthscale 0.3) + N(0, 0.01^2); Matern-5/2 with lengthscale 0.3,
+  outputscale 1, noise 1e-4; qLogNEI on 256 restarts x q=2 with 256 samples.
 """
 
 from __future__ import annotations
@@ -97,3 +101,22 @@ def rff_draw(X: Tensor, n_features: int, lengthscale: Tensor, g: torch.Generator
     w = torch.randn(n_features, generator=g, dtype=torch.float64)
     f = math.sqrt(2.0 / n_features) * torch.cos(X @ omega.T + beta) @ w
     return f + noise_std * torch.randn(X.shape[0], generator=g, dtype=torch.float64)
+
+
+def many_gps(n_models: int = 64, restarts: int = 256, q: int = 2, n_samples: int = 256,
+             seed: int = 0, n_range: tuple[int, int] = (100, 4000),
+             d_range: tuple[int, int] = (4, 30)) -> list[Workload]:
+    g = torch.Generator().manual_seed(seed)
+    out = []
+    lo, hi = math.log(n_range[0]), math.log(n_range[1])
+    for m in range(n_models):
+        n = int(round(math.exp(lo + (hi - lo) * float(torch.rand(1, generator=g, dtype=torch.float64)))))
+        d = int(torch.randint(d_range[0], d_range[1] + 1, (1,), generator=g))
+        X = torch.rand(n, d, generator=g, dtype=torch.float64)
+        ls = torch.full((d,), 0.3, dtype=torch.float64)
+        y = rff_draw(X, 1024, ls, g)
+        Xc = torch.rand(restarts, q, d, generator=g, dtype=torch.float64)
+        out.append(Workload(f"many_gps_{m}_n{n}_d{d}", X, y.unsqueeze(-1), ls, 1.0, 1e-4, 0.0,
+                            "matern52", Xc, n_samples, seed + m, "qLogNEI"))
+    return out
+

@@ -56,6 +56,10 @@ extern "C" {
 
 /* bgb_acq_t.flags */
 #define BGB_FLAG_SIMT 1        /* MIXED: use the FFMA GEMM even when tensor-core operands are set */
+/* bits 8-15: CTAs per SM the adjoint contraction aims for when it splits the
+ * training points into slabs (0: 16); a schedule knob for autotuners */
+#define BGB_FLAG_ADJ_CTAS_SHIFT 8
+#define BGB_FLAG_ADJ_CTAS_MASK 0xFF00
 
 /* An exact GP with fixed hyperparameters (SingleTaskGP, gp_regression.py:108-214).
  * Hyperparameters live in the standardised outcome space; y_mean / y_std
