@@ -56,9 +56,11 @@ def parse():
                    help="only warm up and run --steps mixed-precision steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     p.add_argument("--simt", action="store_true", help="FFMA GEMMs instead of tcgen05")
-    p.add_argument("--config", default="headline", choices=["headline", "many_gps"],
-                   help="many_gps: 64 GPs of uneven size in one tuned CUDA-graph launch "
-                        "(prints its own JSON line)")
+    p.add_argument("--config", default="headline", choices=["headline", "many_gps", "optimize"],
+                   help="many_gps: 64 GPs of uneven size in one tuned CUDA-graph launch; "
+                        "optimize: one full acquisition optimisation step (d=50, 65536 raw "
+                        "q-batches -> 64 restarts x q=16 -> L-BFGS-B); each prints its own line")
+    p.add_argument("--maxiter", type=int, default=100, help="L-BFGS-B iterations (optimize)")
     p.add_argument("--streams", type=int, default=8, help="streams of the many-GP graph")
     p.add_argument("--profile-fit", action="store_true",
                    help="only build the model (training-side fit and operands) between "
@@ -471,6 +473,68 @@ def run_many_gps(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- optimisation step
+OPT_METRIC = ("qLogNEI acquisition optimisation step, d=50, n=4096, 65536 raw q-batches -> "
+              "64 restarts x q=16, 1024 samples, L-BFGS-B")
+
+
+def run_optimize(args) -> None:
+    from botorch_gb300 import SobolQMCNormalSampler, qLogNoisyExpectedImprovement
+    from botorch_gb300 import testing as T
+    from botorch_gb300.optim import (draw_sobol_samples, evaluate_raw, gen_candidates_scipy,
+                                     initialize_q_batch)
+
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    w = T.optimization_step()
+    n, d = w.train_X.shape
+    q, restarts, raw = w.extra["q"], w.extra["restarts"], w.extra["raw_samples"]
+    t0 = time.perf_counter()
+    model = make_model(device, w)
+    acqfs = {}
+    for precision in ("mixed", "fp64"):
+        torch.manual_seed(0)
+        acqfs[precision] = qLogNoisyExpectedImprovement(model, w.train_X, sampler=SobolQMCNormalSampler(
+            torch.Size([w.n_samples]), seed=w.seed), precision=precision)
+    acqf = acqfs["mixed"]
+    torch.cuda.synchronize(device)
+    init_s = time.perf_counter() - t0
+    bounds = torch.stack([torch.zeros(d), torch.ones(d)]).double()
+    # warm-up of the shapes used below (library set-up, graph capture)
+    evaluate_raw(acqf, draw_sobol_samples(bounds, 4096, q, seed=1), 4096)
+    acqf.graphed_value_and_grad(torch.rand(restarts, q, d, dtype=torch.float64, device=device), True)
+    torch.cuda.synchronize(device)
+    t1 = time.perf_counter()
+    X_raw = draw_sobol_samples(bounds, raw, q, seed=0)
+    v_raw = evaluate_raw(acqf, X_raw, 4096)
+    torch.cuda.synchronize(device)
+    t2 = time.perf_counter()
+    X0, _ = initialize_q_batch(X_raw.to(device), v_raw, restarts, eta=1.0,
+                               generator=torch.Generator(device=device).manual_seed(0))
+    X, v = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": args.maxiter})
+    torch.cuda.synchronize(device)
+    t3 = time.perf_counter()
+    info = gen_candidates_scipy.last_info
+    v64, _ = acqfs["fp64"].value_and_grad_raw(X.contiguous(), False)
+    err = float((v - v64).norm() / v64.norm())
+    line = {
+        "metric": OPT_METRIC, "value": round(t3 - t1, 4), "unit": "s", "n_gpus": 1,
+        "higher_is_better": False, "dtype": "f16-split+f32+f64", "data": "synthetic (seeded RFF GP draw)",
+        "config": {"workload": w.name, "n": n, "d": d, "q": q, "restarts": restarts,
+                   "raw_samples": raw, "mc_samples": w.n_samples, "baseline_points_r": acqf.r,
+                   "maxiter": args.maxiter},
+        "raw_eval_s": round(t2 - t1, 4), "raw_evals_per_s": round(raw / (t2 - t1), 1),
+        "lbfgsb_s": round(t3 - t2, 4), "lbfgsb_iterations": info["nit"],
+        "objective_evaluations": info["nfev"],
+        "ms_per_objective_evaluation": round(1e3 * (t3 - t2) / max(info["nfev"], 1), 3),
+        "restart_sum_start": -info["f0"], "restart_sum_final": -info["f"],
+        "best_value": float(v.max()), "best_value_raw": float(v_raw.max()),
+        "final_values_rel_err_vs_fp64": err, "init_s": round(init_s, 2),
+        "launches_per_objective_evaluation": acqf.graph_launches(restarts, q),
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- reference arm
 def run_reference(args) -> None:
     world, rank, _ = dist_info()
@@ -516,6 +580,8 @@ def main() -> None:
         run_reference(args)
     elif args.config == "many_gps":
         run_many_gps(args)
+    elif args.config == "optimize":
+        run_optimize(args)
     else:
         run_ours(args)
 

@@ -1,0 +1,160 @@
+"""Acquisition optimisation around the CUDA acquisition path.
+
+The caller side of the path: raw-sample initialisation and multi-start
+L-BFGS-B on the acquisition value and its gradient, with the reference's
+argument meanings.
+
+* ``draw_sobol_samples``: scrambled Sobol q-batches in a box
+  (botorch/utils/sampling.py:74-111).
+* ``initialize_q_batch``: Boltzmann selection of restart points from the raw
+  samples, keeping the best raw sample (botorch/optim/initializers.py:959-1042,
+  botorch/utils/sampling.py:1084-1115).
+* ``gen_candidates_scipy``: L-BFGS-B on the restarts, aggregated into one
+  problem whose objective is minus the sum of the acquisition values (the
+  reference's aggregated mode, botorch/generation/gen.py:305-395). Each objective
+  call copies x to the device, evaluates value + gradient of every restart in
+  one call (a CUDA graph replay at fixed shape) and copies both back through
+  pinned host buffers (the f / grad wrapper of botorch/generation/gen.py:423-487).
+* ``optimize_acqf``: raw samples -> restarts -> L-BFGS-B -> the best restart
+  (botorch/optim/optimize.py:619, ``return_best_only=True``).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+from torch import Tensor
+
+
+def draw_sobol_samples(bounds: Tensor, n: int, q: int, seed: int | None = None) -> Tensor:
+    """``n x q x d`` scrambled-Sobol points in the box ``bounds`` (2 x d)."""
+    d = bounds.shape[-1]
+    engine = torch.quasirandom.SobolEngine(q * d, scramble=True, seed=seed)
+    raw = engine.draw(n, dtype=bounds.dtype).view(n, q, d).to(bounds.device)
+    lo, hi = bounds[0], bounds[1]
+    return lo + (hi - lo) * raw
+
+
+def _standardize(y: Tensor) -> Tensor:
+    s = y.std()
+    s = s if s >= 1e-9 else torch.ones_like(s)
+    return (y - y.mean()) / s
+
+
+def initialize_q_batch(X: Tensor, acq_vals: Tensor, n: int, eta: float = 1.0,
+                       generator: torch.Generator | None = None) -> tuple[Tensor, Tensor]:
+    """Pick ``n`` of the ``b`` raw q-batches ``X`` (b x q x d) without replacement with
+    probability proportional to exp(eta * standardised value), always keeping the
+    best one. Equal or non-finite values: a random choice."""
+    b = X.shape[0]
+    if n > b:
+        raise RuntimeError(f"n ({n}) cannot be larger than the number of provided samples ({b})")
+    if n == b:
+        return X, acq_vals
+    ystd = acq_vals.std()
+    if ystd == 0 or not torch.isfinite(ystd):
+        idx = torch.randperm(b, device=X.device, generator=generator)[:n]
+        return X[idx], acq_vals[idx]
+    z = _standardize(acq_vals)
+    weights = torch.exp(eta * z)
+    while torch.isinf(weights).any():
+        eta *= 0.5
+        weights = torch.exp(eta * z)
+    idx = torch.multinomial(weights, n, replacement=False, generator=generator)
+    best = torch.argmax(acq_vals)
+    if not bool((idx == best).any()):
+        idx[-1] = best
+    return X[idx], acq_vals[idx]
+
+
+def evaluate_raw(acqf, X: Tensor, batch_limit: int = 4096) -> Tensor:
+    """Acquisition values (no gradient) of ``b x q x d`` raw q-batches, ``batch_limit``
+    q-batches per call."""
+    out = []
+    Xd = X.to(acqf.device, torch.float64)
+    for i in range(0, X.shape[0], batch_limit):
+        v, _ = acqf.value_and_grad_raw(Xd[i:i + batch_limit].contiguous(), False)
+        out.append(v.clone())
+    return torch.cat(out)
+
+
+class _Objective:
+    """f(x) = -sum_i acq(X_i) and its gradient for L-BFGS-B, x the flattened restarts.
+
+    The restarts are evaluated in one call per objective evaluation; x and the
+    gradient cross the host boundary through pinned buffers."""
+
+    def __init__(self, acqf, shape: tuple[int, int, int], use_graph: bool = True) -> None:
+        self.acqf = acqf
+        self.shape = shape
+        self.use_graph = use_graph
+        self.host_x = torch.empty(shape, dtype=torch.float64).pin_memory()
+        self.host_v = torch.empty(shape[0], dtype=torch.float64).pin_memory()
+        self.host_g = torch.empty(shape, dtype=torch.float64).pin_memory()
+        self.dev_x = torch.empty(shape, dtype=torch.float64, device=acqf.device)
+        self.calls = 0
+
+    def __call__(self, x: np.ndarray) -> tuple[float, np.ndarray]:
+        if np.isnan(x).any():
+            raise RuntimeError(f"{int(np.isnan(x).sum())} elements of x are NaN")
+        self.host_x.numpy().reshape(-1)[:] = x
+        self.dev_x.copy_(self.host_x, non_blocking=True)
+        if self.use_graph:
+            v, g = self.acqf.graphed_value_and_grad(self.dev_x, True)
+        else:
+            v, g = self.acqf.value_and_grad_raw(self.dev_x, True)
+        self.host_v.copy_(v, non_blocking=True)
+        self.host_g.copy_(g, non_blocking=True)
+        torch.cuda.current_stream(self.acqf.device).synchronize()
+        self.calls += 1
+        gn = self.host_g.numpy().reshape(-1)
+        if np.isnan(gn).any():
+            raise RuntimeError(f"{int(np.isnan(gn).sum())} elements of the gradient are NaN")
+        return -float(self.host_v.numpy().sum()), -gn.astype(np.float64, copy=True)
+
+
+def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower_bounds: float | Tensor,
+                         upper_bounds: float | Tensor, options: dict | None = None,
+                         use_graph: bool = True) -> tuple[Tensor, Tensor]:
+    """L-BFGS-B from the ``b x q x d`` initial conditions on the box; returns the
+    candidates and their acquisition values."""
+    from scipy.optimize import minimize
+
+    options = dict(options or {})
+    maxiter = int(options.pop("maxiter", 2000))
+    X0 = initial_conditions.detach().to(torch.float64)
+    b, q, d = X0.shape
+    lo = torch.as_tensor(lower_bounds, dtype=torch.float64).expand(d).cpu().numpy()
+    hi = torch.as_tensor(upper_bounds, dtype=torch.float64).expand(d).cpu().numpy()
+    x0 = np.clip(X0.cpu().numpy(), lo, hi).reshape(-1)
+    bounds = list(zip(np.tile(lo, b * q), np.tile(hi, b * q)))
+    obj = _Objective(acquisition_function, (b, q, d), use_graph)
+    f0 = obj(x0)[0]
+    res = minimize(obj, x0, method="L-BFGS-B", jac=True, bounds=bounds,
+                   options={"maxiter": maxiter, **options})
+    X = torch.from_numpy(np.clip(res.x.reshape(b, q, d), lo, hi)).to(acquisition_function.device)
+    v, _ = acquisition_function.value_and_grad_raw(X.contiguous(), False)
+    info = {"nit": int(res.nit), "nfev": int(obj.calls), "message": str(res.message),
+            "f0": f0, "f": float(res.fun)}
+    gen_candidates_scipy.last_info = info
+    return X, v.clone()
+
+
+def optimize_acqf(acq_function, bounds: Tensor, q: int, num_restarts: int, raw_samples: int,
+                  options: dict | None = None, seed: int | None = None,
+                  use_graph: bool = True) -> tuple[Tensor, Tensor]:
+    """Raw samples -> Boltzmann-selected restarts -> L-BFGS-B -> the best restart.
+
+    options: ``batch_limit`` (raw-sample evaluation chunk, 4096), ``eta`` (1.0),
+    ``maxiter`` (2000) and further L-BFGS-B options."""
+    options = dict(options or {})
+    batch_limit = int(options.pop("batch_limit", 4096))
+    eta = float(options.pop("eta", 1.0))
+    bounds = bounds.to(torch.float64)
+    X_raw = draw_sobol_samples(bounds.cpu(), raw_samples, q, seed=seed)
+    v_raw = evaluate_raw(acq_function, X_raw, batch_limit)
+    g = None if seed is None else torch.Generator(device=v_raw.device).manual_seed(seed)
+    X0, _ = initialize_q_batch(X_raw.to(v_raw.device), v_raw, num_restarts, eta=eta, generator=g)
+    X, v = gen_candidates_scipy(X0, acq_function, bounds[0], bounds[1], options, use_graph)
+    best = int(torch.argmax(v))
+    return X[best], v[best]

@@ -16,6 +16,10 @@ the reference). The generators are:
   n=4096 is the headline point, n=8192 the large-n precision case.
 * ``rff_draw``: y = sqrt(2/F) sum_i w_i cos(omega_i . x + beta_i) + noise,
   the random-feature GP draw of the many-model and optimisation workloads.
+* ``optimization_step``: d=50, n=4096, X ~ U[0,1]^50, y = an RFF draw (2048
+  features, ARD lengthscales ~ U[0.1, 2.0]) + N(0, 0.01^2); Matern-5/2 with those
+  lengthscales, outputscale 1, noise 1e-4; qLogNEI with 1024 samples, optimised
+  from 65536 raw q-batches of q=16 over 64 restarts.
 * ``many_gps``: independent problems of uneven size, n ~ log-uniform [100, 4000]
   and d ~ uniform {4..30} per model, X ~ U[0,1]^d, y = an RFF draw (1024
   features, lengthscale 0.3) + N(0, 0.01^2); Matern-5/2 with lengthscale 0.3,
@@ -119,4 +123,14 @@ def many_gps(n_models: int = 64, restarts: int = 256, q: int = 2, n_samples: int
         out.append(Workload(f"many_gps_{m}_n{n}_d{d}", X, y.unsqueeze(-1), ls, 1.0, 1e-4, 0.0,
                             "matern52", Xc, n_samples, seed + m, "qLogNEI"))
     return out
+
+
+def optimization_step(n: int = 4096, d: int = 50, seed: int = 0) -> Workload:
+    g = torch.Generator().manual_seed(seed)
+    X = torch.rand(n, d, generator=g, dtype=torch.float64)
+    ls = 0.1 + 1.9 * torch.rand(d, generator=g, dtype=torch.float64)
+    y = rff_draw(X, 2048, ls, g)
+    return Workload(f"optimize_d{d}_n{n}", X, y.unsqueeze(-1), ls, 1.0, 1e-4, 0.0, "matern52",
+                    torch.empty(0, 16, d, dtype=torch.float64), 1024, seed, "qLogNEI",
+                    extra={"raw_samples": 65536, "restarts": 64, "q": 16})
 
