@@ -167,8 +167,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     int* fail = reinterpret_cast<int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    // tile order: consecutive CTAs share the A row-block (all n-tiles of one m-tile)
-    const int m_tile = blockIdx.x / n_tiles, n_tile = blockIdx.x % n_tiles;
+    // tile order: consecutive CTAs share the A row-block (all n-tiles of one m-tile),
+    // and within it the longest k range comes first (KB_UPPER: the last column
+    // blocks, KB_LOWER: the first), so the final wave holds the short tiles
+    const int m_tile = blockIdx.x / n_tiles;
+    const int n_idx = blockIdx.x % n_tiles;
+    const int n_tile = (kmode == KB_UPPER) ? n_tiles - 1 - n_idx : n_idx;
     const int m0 = m_tile * TC_BM, n0 = n_tile * TC_BN;
     int kbeg = 0, kend = K;
     if (kmode == KB_UPPER) kend = min(K, n0 + TC_BN);
