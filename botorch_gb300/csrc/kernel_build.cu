@@ -28,11 +28,11 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
     int same, TOut* __restrict__ K, int64_t ldk, __half* __restrict__ K16,
     __half* __restrict__ K16_lo, float k16_scale, const float* __restrict__ Z1T, int64_t ldz1,
     const float* __restrict__ Z2T, int64_t ldz2) {
-    __shared__ TAcc s1[KB_DCHUNK][KB_TILE + 1];
+    __shared__ __align__(16) TAcc s1[KB_DCHUNK][KB_TILE];
     __shared__ __align__(16) TAcc s2[KB_DCHUNK][KB_TILE];
-    // thread (tx, ty): rows ty + 16 u, columns 4 tx + v (u, v < 4): the column
-    // coordinates are one 16-byte shared load per k and the outputs are
-    // vector stores of 4 consecutive entries
+    // thread (tx, ty): rows 4 ty + u, columns 4 tx + v (u, v < 4): the row and
+    // column coordinates are 16-byte shared loads per k (broadcast within a
+    // half-warp) and the outputs are vector stores of 4 consecutive entries
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int64_t row0 = (int64_t)blockIdx.y * KB_TILE, col0 = (int64_t)blockIdx.x * KB_TILE;
     TAcc acc[4][4];
@@ -67,10 +67,12 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
 #pragma unroll 4
             for (int kk = 0; kk < kc; ++kk) {
                 const float4 bv = *reinterpret_cast<const float4*>(&s2[kk][4 * tx]);
+                const float4 av = *reinterpret_cast<const float4*>(&s1[kk][4 * ty]);
                 const float2 b01 = make_float2(bv.x, bv.y), b23 = make_float2(bv.z, bv.w);
+                const float avs[4] = {av.x, av.y, av.z, av.w};
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const float au = s1[kk][ty + 16 * u];
+                    const float au = avs[u];
                     const float2 a2 = make_float2(au, au);
                     const float2 d01 = __ffma2_rn(b01, m1, a2);
                     const float2 d23 = __ffma2_rn(b23, m1, a2);
@@ -83,7 +85,7 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
             for (int kk = 0; kk < kc; ++kk) {
                 TAcc a[4], b[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) a[u] = s1[kk][ty + 16 * u];
+                for (int u = 0; u < 4; ++u) a[u] = s1[kk][4 * ty + u];
                 const double2 b01 = *reinterpret_cast<const double2*>(&s2[kk][4 * tx]);
                 const double2 b23 = *reinterpret_cast<const double2*>(&s2[kk][4 * tx + 2]);
                 b[0] = b01.x; b[1] = b01.y; b[2] = b23.x; b[3] = b23.y;
@@ -111,7 +113,7 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
     const bool full = (j0 + 3 < n2) && (ldk % 4) == 0;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        const int64_t i = row0 + ty + 16 * u;
+        const int64_t i = row0 + 4 * ty + u;
         if (i >= m) continue;
         TAcc val[4];
 #pragma unroll

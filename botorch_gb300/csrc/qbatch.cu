@@ -771,6 +771,7 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
 // storing it, and accumulates d[bl, br] = sum_s dY_s z_s^T per chunk of samples
 // (float32 within a chunk, float64 across chunks).
 constexpr int kBsThreads = 128;
+constexpr int kDyLd = kSampleChunk + 1;  // row stride of the reverse-pass dY tile
 
 __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
     s = a + b;
@@ -807,8 +808,9 @@ __device__ __forceinline__ void sample_u(const float* __restrict__ LfT, const fl
 // psd_safe_cholesky of the q x q matrix M (float64, row-major) into scr: plain,
 // then jitter j * 10^t (t < max_tries) added to M's diagonal. Returns 0,
 // BGB_NOT_PSD or BGB_NAN. Run by the 32 lanes of one warp: each column step
-// computes its pivot in every lane (one reciprocal per column) and lane i
-// updates row i, which spreads the float64 work over the warp.
+// computes its pivot in every lane (one reciprocal square root per column: the
+// pivot is v rsqrt(v)) and lane i updates row i, which spreads the float64 work
+// over the warp.
 __device__ int psd_chol_warp(double* M, double* scr, int q, int max_tries, double jitter, int lane) {
     bool has_nan = false;
     for (int p = lane; p < q * q; p += 32) has_nan |= isnan(M[p]);
@@ -828,7 +830,7 @@ __device__ int psd_chol_warp(double* M, double* scr, int q, int max_tries, doubl
             double v = scr[j * q + j];
             for (int k = 0; k < j; ++k) v -= scr[j * q + k] * scr[j * q + k];
             if (!(v > 0.0)) { ok = false; break; }
-            const double djj = sqrt(v), rj = 1.0 / djj;
+            const double rj = rsqrt(v), djj = v * rj;  // one reciprocal square root
             __syncwarp();
             if (lane == j) scr[j * q + j] = djj;
             if (lane > j && lane < q) {
@@ -859,7 +861,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     double* scr = gA + q * q;        // max(q*q, q*r)
     float* Lf = reinterpret_cast<float*>(scr + (q * q > q * r ? q * q : q * r));  // D x QMAX (k-major)
     float* tS = Lf + D * QMAX;       // S
-    float* dY = tS + S;              // q x kSampleChunk
+    float* dY = tS + S;              // q x kDyLd
     __shared__ float s_muh[QMAX], s_mul[QMAX];
     __shared__ double s_dmu[QMAX], s_rd[QMAX];
     __shared__ int s_status;
@@ -1061,20 +1063,20 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
             }
 #pragma unroll
             for (int i = 0; i < QMAX; ++i)
-                if (i < q) dY[i * kSampleChunk + ls] = g[i];  // point-major: no bank conflicts
+                if (i < q) dY[i * kDyLd + ls] = g[i];  // point-major, padded: no bank conflicts
         }
         __syncthreads();
         for (int p = tid; p < q * D; p += kBsThreads) {
             const int i = p / D, k = p % D;
             if (k >= r + i + 1) continue;  // the upper part of br stays zero
             float cs = 0.f;
-            const float* dyi = dY + i * kSampleChunk;
+            const float* dyi = dY + i * kDyLd;
             for (int ls = 0; ls < sc; ++ls) cs = fmaf(dyi[ls], z32[(int64_t)(s0 + ls) * D + k], cs);
             dLq[p] += (double)cs;
         }
         for (int i = tid; i < q; i += kBsThreads) {
             float cs = 0.f;
-            const float* dyi = dY + i * kSampleChunk;
+            const float* dyi = dY + i * kDyLd;
             for (int ls = 0; ls < sc; ++ls) cs += dyi[ls];
             s_dmu[i] += (double)cs;
         }
@@ -1135,6 +1137,24 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     }
     for (int p = tid; p < q * q; p += kBsThreads) a.gqq[bidx * q * q + p] = sy2 * gA[p];
     for (int i = tid; i < q; i += kBsThreads) a.gmu[bidx * q + i] = sy * s_dmu[i];
+    if (a.hmul == nullptr) return;
+    // power-of-two row scales of H = gmu beta^T - 2 Gqq V - Gqb Vb for its float16
+    // split, from |H[i,c]| <= |gmu_i| max|beta| + sqrt(outputscale) (sum_j 2|Gqq_ij| +
+    // sum_k |Gqb_ik|) (rows of V and Vb have 2-norm <= sqrt(outputscale))
+    __syncthreads();
+    for (int i = tid; i < q; i += kBsThreads) {
+        double sv = 0.0;
+        for (int j = 0; j < q; ++j) sv += 2.0 * fabs(a.gqq[(bidx * q + i) * q + j]);
+        for (int k = 0; k < r; ++k) sv += fabs(a.gqb[(bidx * q + i) * r + k]);
+        const double bound = fabs(a.gmu[bidx * q + i]) * a.beta_absmax + sqrt(a.outputscale) * sv;
+        float sc = 1.f;
+        if (bound > 0.0 && !isinf(bound)) {
+            int e;
+            frexp(bound, &e);
+            sc = ldexpf(1.f, 14 - e);
+        }
+        a.hmul[bidx * q + i] = 1.f / sc;
+    }
 }
 
 __global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
@@ -1157,12 +1177,12 @@ __global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
 // layout allows, else E = 1), so every seed read from shared memory feeds E
 // columns; QM >= q bounds the register arrays.
 // H16 set (float32 only): H is written as the float16 split of s_i H[i,:] for
-// the tensor-core adjoint GEMM, s_i a power of two from the bound
+// the tensor-core adjoint GEMM, with 1 / s_i in a.hmul: the power of two that
+// the batch step derived from the bound
 //   |H[i,c]| <= |gmu_i| max|beta| + sqrt(outputscale) (sum_j 2|Gqq[i,j]| + sum_k |Gqb[i,k]|)
-// (every row of V and Vb has 2-norm <= sqrt(outputscale) since V V^T <= K(X,X)),
-// and hmul[i] = 1 / s_i.
+// (every row of V and Vb has 2-norm <= sqrt(outputscale) since V V^T <= K(X,X)).
 template <typename T, int QM, int E>
-__global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __restrict__ V,
+__global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T* __restrict__ V,
                                                        int64_t ldv, const T* __restrict__ Vb,
                                                        const T* __restrict__ beta,
                                                        T* __restrict__ H, __half* __restrict__ H16,
@@ -1178,21 +1198,8 @@ __global__ void __launch_bounds__(256) mix_rows_kernel(QBatchArgs a, const T* __
     for (int p = threadIdx.x; p < q * r; p += blockDim.x) gqb[p] = (T)(-a.gqb[bidx * q * r + p]);
     for (int p = threadIdx.x; p < q; p += blockDim.x) gm[p] = (T)a.gmu[bidx * q + p];
     __syncthreads();
-    if (H16 != nullptr) {
-        for (int i = threadIdx.x; i < q; i += blockDim.x) {
-            float bound = fabsf((float)gm[i]) * (float)a.beta_absmax, sv = 0.f;
-            for (int j = 0; j < q; ++j) sv += fabsf((float)gq[i * q + j]);
-            for (int k = 0; k < r; ++k) sv += fabsf((float)gqb[i * r + k]);
-            bound += sqrtf((float)a.outputscale) * sv;
-            float sc = 1.f;
-            if (bound > 0.f && !isinf(bound)) {
-                int e;
-                frexpf(bound, &e);
-                sc = ldexpf(1.f, 14 - e);
-            }
-            hs[i] = sc;
-            if (blockIdx.x == 0) a.hmul[rbase + i] = 1.f / sc;
-        }
+    if (H16 != nullptr) {  // row scales written by the batch step (a.hmul = 1 / scale)
+        for (int i = threadIdx.x; i < q; i += blockDim.x) hs[i] = 1.f / a.hmul[rbase + i];
         __syncthreads();
     }
     const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * E;
@@ -1332,6 +1339,26 @@ __device__ __forceinline__ void adjoint_finish_row(const QBatchArgs& a, int64_t 
         if (k < d) a.grad[row * d + k] = 2.0 * a.outputscale * a.inv_ls[k] * (double)gx[k];
 }
 
+// d kappa / d r2 in float32 with the fast intrinsics (rsqrtf, __expf: a few ulp,
+// far inside the gradient's error budget), for the adjoint sweep; same branches
+// as dkappa_dr2.
+__device__ __forceinline__ float dkappa_dr2_fast(int kind, float r2) {
+    if (kind == BGB_KERNEL_RBF) return -0.5f * __expf(-0.5f * r2);
+    const bool live = r2 > (float)kMinSqDist;
+    const float rr = live ? r2 : (float)kMinSqDist;
+    const float rho = rr * rsqrtf(rr);
+    if (kind == BGB_KERNEL_MATERN52) {
+        const float sv = 2.2360679774997896964f * rho;
+        const float e = __expf(-sv);
+        return live ? (-5.f / 6.f) * (1.f + sv) * e : (5.f / 3.f) * e;
+    }
+    if (kind == BGB_KERNEL_MATERN32) {
+        const float sv = 1.7320508075688772935f * rho;
+        return live ? -1.5f * __expf(-sv) : 0.f;
+    }
+    return live ? -__fdividef(__expf(-rho), 2.f * rho) : 0.f;
+}
+
 template <typename T, int DMAX, bool FINISH>
 __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
                                                            int64_t ldd, const T* __restrict__ XsT,
@@ -1399,7 +1426,7 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
                     r2v = __ffma2_rn(df2[2 * v], df2[2 * v], r2v);
                     r2v = __ffma2_rn(df2[2 * v + 1], df2[2 * v + 1], r2v);
                 }
-                const float coef = dk * dkappa_dr2<float>(kind, r2v.x + r2v.y);
+                const float coef = dk * dkappa_dr2_fast(kind, r2v.x + r2v.y);
                 const float2 coef2 = make_float2(coef, coef);
 #pragma unroll
                 for (int v = 0; v < DMAX / 2; ++v) g2[v] = __ffma2_rn(coef2, df2[v], g2[v]);
@@ -1518,7 +1545,7 @@ size_t batch_step_f32_smem_bytes(int q, int r, int S) {
     const int D = r + q;
     const int qmax = q <= 4 ? 4 : q <= 8 ? 8 : q <= 16 ? 16 : 32;
     return sizeof(double) * (size_t)(2 * q * q + 2 * q * D + (q * q > q * r ? q * q : q * r)) +
-           sizeof(float) * (size_t)(D * qmax + S + kSampleChunk * q);
+           sizeof(float) * (size_t)(D * qmax + S + kDyLd * q);
 }
 
 int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bool mixed) {
