@@ -1202,9 +1202,12 @@ __global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T*
         for (int i = threadIdx.x; i < q; i += blockDim.x) hs[i] = 1.f / a.hmul[rbase + i];
         __syncthreads();
     }
-    const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * E;
-    if (c0 >= n) return;
     using VT = typename Vec16<T>::type;
+    // column groups of blockDim.x * E, strided over grid.x
+    for (int64_t cg = (int64_t)blockIdx.x * blockDim.x * E; cg < n;
+         cg += (int64_t)gridDim.x * blockDim.x * E) {
+    const int64_t c0 = cg + (int64_t)threadIdx.x * E;
+    if (c0 >= n) continue;
     T v[QM][E], bc[E];
 #pragma unroll
     for (int j = 0; j < QM; ++j) {
@@ -1280,6 +1283,7 @@ __global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T*
         } else {
             H[off] = h[0];
         }
+    }
     }
 }
 
@@ -1521,6 +1525,20 @@ __global__ void posterior_out_kernel(QBatchArgs a, double* mean, double* covar) 
 
 }  // namespace
 
+// SMs of the current device (queried once, 152 on a GB300; 1 if the query fails)
+int sm_count() {
+    static int num_sms = 0;
+    if (num_sms == 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            num_sms = v;
+        else
+            num_sms = 1;
+    }
+    return num_sms;
+}
+
 template <typename T>
 int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc,
                         cudaStream_t stream) {
@@ -1632,14 +1650,21 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
     const bool vec = (a.n % E == 0) && (ldv % E == 0) && (ld % E == 0) && al(V, 16) &&
                      al(beta, 16) && (a.r == 0 || al(Vb, 16)) &&
                      (H16 != nullptr ? (al(H16, 8) && al(H16_lo, 8)) : al(H, 16));
+    // column groups per t-batch: enough CTAs for ~6 per SM, each CTA loads its
+    // t-batch's seeds once and strides over the rest
+    auto groups = [&](int64_t per) {
+        const int64_t all = ceil_div(a.n, per);
+        const int64_t want = ceil_div((int64_t)sm_count() * 6, a.b);
+        return (unsigned)(want < 1 ? 1 : (want > all ? all : want));
+    };
 #define BGB_MIX(QM)                                                                              \
     do {                                                                                        \
         if (vec) {                                                                              \
-            dim3 grid((unsigned)ceil_div(a.n, 256 * E), (unsigned)a.b);                         \
+            dim3 grid(groups(256 * E), (unsigned)a.b);                                          \
             mix_rows_kernel<T, QM, E><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H16,   \
                                                                    H16_lo, ld);                 \
         } else {                                                                                \
-            dim3 grid((unsigned)ceil_div(a.n, 256), (unsigned)a.b);                             \
+            dim3 grid(groups(256), (unsigned)a.b);                                              \
             mix_rows_kernel<T, QM, 1><<<grid, 256, smem, stream>>>(a, V, ldv, Vb, beta, H, H16,   \
                                                                    H16_lo, ld);                 \
         }                                                                                       \
@@ -1669,13 +1694,7 @@ int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T
     const int64_t row_blocks = ceil_div(rows, kAdjRows);
     // slabs: a.adj_ctas_per_sm CTAs per SM (default 16: about four waves of four
     // resident CTAs), slabs of whole chunks, partials within part_cap
-    static int num_sms = 0;
-    if (num_sms == 0) {
-        int dev = 0, v = 0;
-        BGB_CUDA_TRY(cudaGetDevice(&dev));
-        BGB_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-        num_sms = v > 0 ? v : 1;
-    }
+    const int num_sms = sm_count();
     const int64_t chunks = ceil_div(a.n, kAdjChunk);
     const int64_t per_sm = a.adj_ctas_per_sm > 0 ? a.adj_ctas_per_sm : 16;
     int64_t nslab = ceil_div((int64_t)num_sms * per_sm, row_blocks);
