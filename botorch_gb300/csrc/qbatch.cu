@@ -1364,7 +1364,7 @@ __device__ __forceinline__ float dkappa_dr2_fast(int kind, float r2) {
 }
 
 template <typename T, int DMAX, bool FINISH>
-__global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
+__global__ void __launch_bounds__(kAdjRows, (sizeof(T) == 4 && DMAX <= 24) ? 5 : 1) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
                                                            int64_t ldd, const T* __restrict__ XsT,
                                                            int64_t slab, T* __restrict__ part) {
     using VT = typename Vec16<T>::type;
@@ -1414,23 +1414,23 @@ __global__ void __launch_bounds__(kAdjRows) adjoint_kernel(QBatchArgs a, const T
         if constexpr (sizeof(T) == 4) {
             // each thread streams its own row of D from global memory (16-byte
             // loads along the row; L1 serves the rest of each line), and the pair
-            // arithmetic runs on packed float32 pairs (even, odd coordinate): the
-            // same correctly rounded operations as the scalar form below
+            // arithmetic runs on packed float32 pairs of coordinates
             const float2 m1 = make_float2(-1.f, -1.f);
             const float* drow = reinterpret_cast<const float*>(Dm) + row * ldd + c0;
             auto pair = [&](float dk, int c) {
                 const float4* xc = reinterpret_cast<const float4*>(Xc + c * DMAX);
                 float2 df2[DMAX / 2];
-                float2 r2v = make_float2(0.f, 0.f);
+                // two independent packed chains (k mod 4 in {0, 1} and {2, 3})
+                float2 r2a = make_float2(0.f, 0.f), r2b = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int v = 0; v < DMAX / 4; ++v) {
                     const float4 x4 = xc[v];
                     df2[2 * v] = __ffma2_rn(make_float2(x4.x, x4.y), m1, zx2[2 * v]);
                     df2[2 * v + 1] = __ffma2_rn(make_float2(x4.z, x4.w), m1, zx2[2 * v + 1]);
-                    r2v = __ffma2_rn(df2[2 * v], df2[2 * v], r2v);
-                    r2v = __ffma2_rn(df2[2 * v + 1], df2[2 * v + 1], r2v);
+                    r2a = __ffma2_rn(df2[2 * v], df2[2 * v], r2a);
+                    r2b = __ffma2_rn(df2[2 * v + 1], df2[2 * v + 1], r2b);
                 }
-                const float coef = dk * dkappa_dr2_fast(kind, r2v.x + r2v.y);
+                const float coef = dk * dkappa_dr2_fast(kind, (r2a.x + r2a.y) + (r2b.x + r2b.y));
                 const float2 coef2 = make_float2(coef, coef);
 #pragma unroll
                 for (int v = 0; v < DMAX / 2; ++v) g2[v] = __ffma2_rn(coef2, df2[v], g2[v]);
