@@ -770,7 +770,7 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
 // rounding. The reverse pass recomputes each sample's forward rather than
 // storing it, and accumulates d[bl, br] = sum_s dY_s z_s^T per chunk of samples
 // (float32 within a chunk, float64 across chunks).
-constexpr int kBsThreads = 128;
+constexpr int kBsThreads = 64;
 constexpr int kDyLd = kSampleChunk + 1;  // row stride of the reverse-pass dY tile
 
 __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
