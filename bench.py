@@ -77,7 +77,7 @@ def dist_info():
 
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -93,7 +93,7 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.fh,
                 stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -261,10 +261,20 @@ def run_ours(args) -> None:
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(device)
+    def load_for(seconds: float) -> None:  # the same step, untimed, to hold the clocks under load
+        t_end = time.perf_counter() + seconds
+        while time.perf_counter() < t_end:
+            step()
+            torch.cuda.synchronize(device)
+
+    # the sampler window: 0.6 s of load, the timed steps, 0.3 s of load (the timed
+    # region alone is shorter than the sampling period)
     with ClockSampler(local) as clk:
+        load_for(0.6)
         t_wall0 = time.perf_counter()
         step_ms = time_steps(step, args.steps, device, flush)
         t_wall = time.perf_counter() - t_wall0
+        load_for(0.3)
     # graph replays bypass the host-side counter: each replay runs the launches
     # recorded when the call was captured
     launches = acqf.graph_launches(b, Q) * args.steps
@@ -386,7 +396,8 @@ def run_ours(args) -> None:
         "gpu_launches": int(launches), "launch_mode": "CUDA graph replay of the whole call",
         "launches_per_step": acqf.graph_launches(b, Q),
         "eager_evals_per_s": round(eager_value, 1),
-        "eager_launches_per_step": eager_launches_per_step, "clocks": clk.summary(),
+        "eager_launches_per_step": eager_launches_per_step,
+        "clocks": {**clk.summary(), "window": "0.6 s load, timed steps, 0.3 s load; 100 ms sampling"},
         "stage_ms": {k: round(v, 4) for k, v in zip(names, st)},
         "fp64_gpu_evals_per_s": round(fp64_evals, 1),
         "speedup_vs_fp64_gpu": round(value / world / fp64_evals, 2),
