@@ -195,7 +195,8 @@ class _MCAcquisition:
             n0 = lib.bgb_launch_count()
             with torch.cuda.graph(graph):
                 self.value_and_grad_raw(Xs, need_grad, check=False, out=out, ws=ws)
-            entry = dict(graph=graph, X=Xs, out=out, ws=ws, acq=acq,
+            # keep the base samples the captured struct points to alive with the graph
+            entry = dict(graph=graph, X=Xs, out=out, ws=ws, acq=acq, Z=self._Z.get(q),
                          launches=lib.bgb_launch_count() - n0)
             self._graphs[key] = entry
         entry["X"].copy_(Xd)

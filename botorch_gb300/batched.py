@@ -151,6 +151,15 @@ class ModelBatch:
                 main.wait_stream(s)
         self.launches = lib.bgb_launch_count() - n0
         self.graph = graph
+        # the call structs (and the base samples they point to) the graph was captured with
+        self.structs = [a._call_struct(s[1])[0] for a, s in zip(self.acqfs, self.shapes)]
+        self.keep = [a._Z.get(s[1]) for a, s in zip(self.acqfs, self.shapes)]
+
+    def _stale(self) -> bool:
+        """A problem's call struct changed (new baseline or pending points): its graph
+        would read released buffers, so it has to be captured again."""
+        return any(a._call_struct(s[1])[0] is not st
+                   for a, s, st in zip(self.acqfs, self.shapes, self.structs))
 
     def value_and_grad(self, Xs: list[Tensor], check: bool = True) -> list[tuple[Tensor, Tensor]]:
         if len(Xs) != len(self.acqfs):
@@ -158,7 +167,7 @@ class ModelBatch:
         for x, s in zip(Xs, self.shapes):
             if tuple(x.shape) != s:
                 raise ValueError(f"candidate shape {tuple(x.shape)} differs from the captured {s}")
-        if self.graph is None:
+        if self.graph is None or self._stale():
             self._capture(Xs)
         else:
             for dst, x in zip(self.X, Xs):

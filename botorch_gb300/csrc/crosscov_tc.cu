@@ -426,11 +426,14 @@ int tc_gemm_f16x3(int64_t M, int64_t N, int64_t K, const __half* A_hi, const __h
     if (!make_map(&maps.a_hi, A_hi, M, K, lda, TC_BM) || !make_map(&maps.a_lo, A_lo, M, K, lda, TC_BM) ||
         !make_map(&maps.b_hi, B_hi, N, K, ldbs, TC_BN) || !make_map(&maps.b_lo, B_lo, N, K, ldbs, TC_BN))
         return BGB_ERR_UNSUPPORTED;
-    static bool attr_set = false;
-    if (!attr_set) {
+    // the shared-memory opt-in is a per-device function attribute
+    static bool attr_set[64] = {};
+    int dev = 0;
+    BGB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
         BGB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)TC_SMEM));
-        attr_set = true;
+        if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
     const int m_tiles = (int)ceil_div(M, TC_BM), n_tiles = (int)ceil_div(N, TC_BN);
     tc_gemm_kernel<<<(unsigned)(m_tiles * n_tiles), TC_THREADS, TC_SMEM, stream>>>(

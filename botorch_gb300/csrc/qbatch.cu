@@ -1525,18 +1525,16 @@ __global__ void posterior_out_kernel(QBatchArgs a, double* mean, double* covar) 
 
 }  // namespace
 
-// SMs of the current device (queried once, 152 on a GB300; 1 if the query fails)
+// SMs of the current device (queried once per device, 152 on a GB300; 1 if the
+// query fails)
 int sm_count() {
-    static int num_sms = 0;
-    if (num_sms == 0) {
-        int dev = 0, v = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
-            num_sms = v;
-        else
-            num_sms = 1;
-    }
-    return num_sms;
+    static int num_sms[64] = {};
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (dev >= 0 && dev < 64 && num_sms[dev] > 0) return num_sms[dev];
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+    if (dev >= 0 && dev < 64) num_sms[dev] = v;
+    return v;
 }
 
 template <typename T>
