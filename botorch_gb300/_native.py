@@ -80,6 +80,9 @@ _SIGNATURES = {
     "bgb_gp_fit_workspace_bytes": (c_size, [c_i64]),
     "bgb_gp_operands": (c_i32, [ctypes.POINTER(BgbGP), c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp,
                                 c_vp, c_vp, c_vp]),
+    "bgb_gp_mll": (c_i32, [ctypes.POINTER(BgbGP), c_vp, c_vp, c_vp, c_vp,
+                           ctypes.POINTER(ctypes.c_double), c_vp, c_size, c_vp]),
+    "bgb_gp_mll_workspace_bytes": (c_size, [c_i64, c_i32]),
     "bgb_gp_tc_operands": (c_i32, [ctypes.POINTER(BgbGP), c_vp, c_i64, c_vp, c_vp, c_vp, c_vp,
                                    c_vp, c_vp, c_vp]),
     "bgb_crosscov_gemm_f16x3": (c_i32, [c_i64, c_i64, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64,

@@ -58,6 +58,15 @@ int gemm_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const
 int transpose_f64(const double* src, int64_t rows, int64_t cols, int64_t lds, double* dst,
                   int64_t ldd, cudaStream_t stream);
 
+// mll.cu ---------------------------------------------------------------------
+// Exact MLL of y under the GP and its gradient (float64, from L, L^-1, alpha):
+// out_host[0] = mll / n, [1 + k] = -s sum W kappa' dz_k^2 / n (to be scaled by
+// 1 / l_k), [1 + d] outputscale, [2 + d] noise, [3 + d] mean-constant gradient.
+size_t mll_workspace_bytes(int64_t n, int d);
+int gp_mll(const double* X, int64_t n, int d, const double* inv_ls, double outputscale, int kind,
+           double mean_constant, const double* y, const double* L, const double* Linv,
+           const double* alpha, double* out_host, void* ws, size_t ws_bytes, cudaStream_t st);
+
 // crosscov_tc.cu ------------------------------------------------------------
 bool tc_gemm_available();
 // C = diag(row_mul) A op(B) diag(col_mul) on tcgen05 tensor cores from float16

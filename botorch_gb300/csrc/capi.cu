@@ -606,6 +606,25 @@ int bgb_baseline_operands(const bgb_gp_t* gp, const double* Linv, const double* 
     return BGB_OK;
 }
 
+size_t bgb_gp_mll_workspace_bytes(int64_t n, int32_t d) { return mll_workspace_bytes(n, d); }
+
+int bgb_gp_mll(const bgb_gp_t* gp, const double* y, const double* L, const double* Linv,
+               const double* alpha, double* out_host, void* workspace, size_t workspace_bytes,
+               void* stream) {
+    if (!valid_gp(gp) || y == nullptr || L == nullptr || Linv == nullptr || alpha == nullptr ||
+        out_host == nullptr)
+        return BGB_ERR_ARG;
+    if (gp->d > 64) return BGB_ERR_UNSUPPORTED;
+    cudaStream_t st = as_stream(stream);
+    int rc = gp_mll(gp->train_X, gp->n, gp->d, gp->inv_lengthscale, gp->outputscale, gp->kernel,
+                    gp->mean_constant, y, L, Linv, alpha, out_host, workspace, workspace_bytes, st);
+    if (rc) return rc;
+    double il[64];
+    BGB_CUDA_TRY(cudaMemcpy(il, gp->inv_lengthscale, sizeof(double) * gp->d, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < gp->d; ++k) out_host[1 + k] *= il[k];  // d r2 / d l_k = -2 dz_k^2 / l_k
+    return BGB_OK;
+}
+
 size_t bgb_acq_workspace_bytes(const bgb_acq_t* acq, int64_t b) {
     if (acq == nullptr || b <= 0) return 0;
     return acq_ws_layout(acq, b, nullptr, nullptr, nullptr, nullptr, nullptr);

@@ -172,6 +172,19 @@ int bgb_gp_fit(const bgb_gp_t* gp, const double* y, double noise, int32_t max_tr
                void* workspace, size_t workspace_bytes, void* stream);
 size_t bgb_gp_fit_workspace_bytes(int64_t n);
 
+/* (a3) Exact marginal log-likelihood of the standardised training targets y (n)
+ * and its gradient w.r.t. the hyperparameters, float64, from the training cache
+ * of bgb_gp_fit (L, Linv, alpha): out_host (host, d + 4 doubles) = [mll / n,
+ * d/d lengthscale_k (d values), d/d outputscale, d/d noise, d/d mean_constant],
+ * per data point like gpytorch's ExactMarginalLogLikelihood. Replaces the loss
+ * that fit_gpytorch_mll minimises (botorch/fit.py:76 with
+ * botorch/optim/closures/model_closures.py:117-143; no priors). d <= 64.
+ * Synchronises `stream`. */
+int bgb_gp_mll(const bgb_gp_t* gp, const double* y, const double* L, const double* Linv,
+               const double* alpha, double* out_host, void* workspace, size_t workspace_bytes,
+               void* stream);
+size_t bgb_gp_mll_workspace_bytes(int64_t n, int32_t d);
+
 /* (c) Model-level operands: B = Linv^T (n x ldb, ldb >= n) in float64 and
  * float32 (B32 may be NULL), float32 copies of Linv and beta (may be NULL), and
  * the training inputs scaled by 1 / lengthscale, Xs (d x n, k-major) in
