@@ -142,6 +142,23 @@ class SingleTaskGP:
                          train_X=nat.ptr(self.train_inputs[0]),
                          inv_lengthscale=nat.ptr(self.inv_lengthscale))
 
+    def set_hyperparameters(self, lengthscale=None, outputscale: float | None = None,
+                            noise: float | None = None, mean_constant: float | None = None) -> None:
+        """New hyperparameter values (standardised outcome space) and a refit of the
+        training cache; operands built for acquisition functions are dropped, so
+        acquisition functions are built after fitting, as in the reference."""
+        if lengthscale is not None:
+            ls = torch.as_tensor(lengthscale, dtype=torch.float64).reshape(-1)
+            self.lengthscale = (ls.expand(self.d) if ls.numel() == 1 else ls).clone().cpu()
+            self.inv_lengthscale = (1.0 / self.lengthscale).to(self.device, torch.float64).contiguous()
+        if outputscale is not None:
+            self.outputscale = float(outputscale)
+        if noise is not None:
+            self.noise = float(noise)
+        if mean_constant is not None:
+            self.mean_constant = float(mean_constant)
+        self._fit()
+
     def _fit(self) -> None:
         lib = nat.lib()
         n, dev = self.n, self.device
