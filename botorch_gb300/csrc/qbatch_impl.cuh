@@ -19,6 +19,13 @@
 //                 contracted with d K(X, Xt) / d X while recomputing
 //                 the scaled distances to Xt instead of storing K(X, Xt); plus the
 //                 K(X, X) and K(X, Xb) terms.
+//
+// This file holds the kernels and their launchers. It is compiled as several
+// translation units (qbatch_*.cu), each defining one BGB_QB_* selector, so
+// that the launchers and the kernel instantiations they pull in are split
+// over parallel compiler processes.
+#pragma once
+
 #include <math.h>
 
 #include "bgb_common.cuh"
@@ -26,6 +33,9 @@
 #include "bgb_qbatch.cuh"
 
 namespace bgb {
+
+// SMs of the current device (defined in the statistics translation unit)
+int sm_count();
 
 namespace {
 
@@ -474,6 +484,7 @@ __device__ int chol_small(double* A, int q) {
 //                          t S | dY SC*q | scratch q*q
 constexpr int kSampleChunk = 128;
 
+#if defined(BGB_QB_STEP)
 // The float64 path's step (the mixed path's is batch_step_f32_kernel).
 __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backward) {
     extern __shared__ double sm[];
@@ -757,6 +768,7 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     for (int p = tid; p < q * q; p += blockDim.x) a.gqq[bidx * q * q + p] = sy2 * gA[p];
     for (int i = tid; i < q; i += blockDim.x) a.gmu[bidx * q + i] = sy * dmu[i];
 }
+#endif  // BGB_QB_STEP
 
 // ---------------------------------------------------------------- batch_step (mixed)
 // Per-t-batch step of the mixed path. float64 for the q x q algebra: the
@@ -1157,6 +1169,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     }
 }
 
+#if defined(BGB_QB_STEP)
 __global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
                                     const double* __restrict__ best_f, int S, int qei,
                                     float* __restrict__ z32, float* __restrict__ bf32) {
@@ -1169,6 +1182,7 @@ __global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
         bf32[2 * idx + 1] = (float)(bf - (double)h);
     }
 }
+#endif  // BGB_QB_STEP
 
 // ---------------------------------------------------------------- mix_rows
 // H[row i of t-batch] = gmu_i beta - 2 sum_j Gqq[i,j] V[j,:] - sum_k Gqb[i,k] Vb[k,:]
@@ -1228,9 +1242,7 @@ __global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T*
         bc[0] = beta[c0];
     }
     // one output row at a time (the Vb rows are re-read from L1 per row)
-#pragma unroll
-    for (int i = 0; i < QM; ++i) {
-        if (i >= q) break;
+    auto row = [&](int i) {
         T h[E];
         const T gmi = gm[i];
 #pragma unroll
@@ -1272,7 +1284,7 @@ __global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T*
                     H16_lo[off + e] = ll[e];
                 }
             }
-            continue;
+            return;
         }
         if constexpr (E > 1) {
             VT o;
@@ -1283,6 +1295,18 @@ __global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T*
         } else {
             H[off] = h[0];
         }
+    };
+    if constexpr (QM <= 8) {
+#pragma unroll
+        for (int i = 0; i < QM; ++i) {
+            if (i >= q) break;
+            row(i);
+        }
+    } else {
+        // rolled: a fully unrolled QM x QM body beyond q = 8 gains nothing and
+        // is slow to compile
+#pragma unroll 1
+        for (int i = 0; i < q; ++i) row(i);
     }
     }
 }
@@ -1515,6 +1539,7 @@ __global__ void __launch_bounds__(128) adjoint_finalize_kernel(QBatchArgs a, con
     adjoint_finish_row<T, DMAX>(a, row, gx);
 }
 
+#if defined(BGB_QB_STATS)
 __global__ void posterior_out_kernel(QBatchArgs a, double* mean, double* covar) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = a.q;
@@ -1522,9 +1547,11 @@ __global__ void posterior_out_kernel(QBatchArgs a, double* mean, double* covar) 
     covar[idx] = a.y_std * a.y_std * a.sig[idx];
     if (idx < a.b * q) mean[idx] = a.y_mean + a.y_std * a.mu[idx];
 }
+#endif  // BGB_QB_STATS
 
 }  // namespace
 
+#if defined(BGB_QB_STATS)
 // SMs of the current device (queried once per device, 152 on a GB300; 1 if the
 // query fails)
 int sm_count() {
@@ -1550,7 +1577,9 @@ int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
+#endif  // BGB_QB_STATS
 
+#if defined(BGB_QB_STEP)
 size_t batch_step_smem_bytes(int q, int r, int S) {
     const int D = r + q;
     return sizeof(double) * (size_t)(2 * q * D + 2 * q * q + 2 * q + S + kSampleChunk * q +
@@ -1601,7 +1630,9 @@ int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bo
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
+#endif  // BGB_QB_STEP
 
+#if defined(BGB_QB_STATS)
 template <typename T>
 int launch_qstats(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb,
                   cudaStream_t stream) {
@@ -1634,6 +1665,9 @@ int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta,
     return BGB_OK;
 }
 
+#endif  // BGB_QB_STATS
+
+#if defined(BGB_QB_MIX)
 template <typename T>
 int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, const T* beta, T* H,
                     cudaStream_t stream, __half* H16, __half* H16_lo, int64_t ldh) {
@@ -1675,7 +1709,9 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
+#endif  // BGB_QB_MIX
 
+#if defined(BGB_QB_ADJ_F64) || defined(BGB_QB_ADJ_F32)
 template <typename T, int DMAX>
 size_t adjoint_smem_bytes() {
     // float32 rows stream D from global memory; float64 stages its D tile
@@ -1743,6 +1779,9 @@ int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T
     return BGB_OK;
 }
 
+#endif  // BGB_QB_ADJ_*
+
+#if defined(BGB_QB_STATS)
 int launch_posterior_out(const QBatchArgs& a, double* mean, double* covar, cudaStream_t stream) {
     const int64_t tot = a.b * a.q * a.q;
     if (tot <= 0) return BGB_OK;
@@ -1763,14 +1802,21 @@ template int launch_row_dots<double>(const QBatchArgs&, const double*, int64_t, 
                                      const double*, double*, cudaStream_t);
 template int launch_row_dots<float>(const QBatchArgs&, const float*, int64_t, const float*,
                                     const float*, float*, cudaStream_t);
+#endif  // BGB_QB_STATS
+#if defined(BGB_QB_MIX)
 template int launch_mix_rows<double>(const QBatchArgs&, const double*, int64_t, const double*,
                                      const double*, double*, cudaStream_t, __half*, __half*,
                                      int64_t);
 template int launch_mix_rows<float>(const QBatchArgs&, const float*, int64_t, const float*,
                                     const float*, float*, cudaStream_t, __half*, __half*, int64_t);
+#endif  // BGB_QB_MIX
+#if defined(BGB_QB_ADJ_F64)
 template int launch_adjoint<double>(const QBatchArgs&, const double*, int64_t, const double*,
                                     double*, int64_t, cudaStream_t);
+#endif
+#if defined(BGB_QB_ADJ_F32)
 template int launch_adjoint<float>(const QBatchArgs&, const float*, int64_t, const float*,
                                    float*, int64_t, cudaStream_t);
+#endif
 
 }  // namespace bgb
