@@ -56,7 +56,7 @@ def parse():
                    help="only warm up and run --steps mixed-precision steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     p.add_argument("--simt", action="store_true", help="FFMA GEMMs instead of tcgen05")
-    p.add_argument("--config", default="headline", choices=["headline", "many_gps", "optimize"],
+    p.add_argument("--config", default="headline", choices=["headline", "many_gps", "optimize", "log_areas"],
                    help="many_gps: 64 GPs of uneven size in one tuned CUDA-graph launch; "
                         "optimize: one full acquisition optimisation step (d=50, 65536 raw "
                         "q-batches -> 64 restarts x q=16 -> L-BFGS-B); each prints its own line")
@@ -546,6 +546,167 @@ def run_optimize(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- fused log-areas (qLogEHVI)
+LA_METRIC = ("qLogEHVI fused log-areas forward+backward, (sample-batch, cell, subset) areas/s, "
+             "m=2, q=4, 64 cells, 32768 sample-batches")
+
+
+def _la_step_fns(w, go):
+    from botorch_gb300 import logei_fused as lf
+
+    def step():
+        for obj, g in zip(w.obj_subsets, go):
+            lf.forward(obj, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
+            lf.backward(g, obj, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
+    return step
+
+
+def la_cpu_baseline(w, threads: int, sample_batches: int) -> tuple[float, str]:
+    """The C restatement of the reference kernel (oracle) on `threads` host threads:
+    forward + backward of every subset size over the first `sample_batches` rows."""
+    from oracle import log_areas as ola
+
+    cpu = [o[:sample_batches].cpu() for o in w.obj_subsets]
+    cl, cu = w.cell_lower.cpu(), w.cell_upper.cpu()
+    gos = [torch.ones(sample_batches, w.nc, o.shape[1], dtype=o.dtype) for o in cpu]
+    ola.forward(cpu[0][:8], cl, cu, w.tau_relu, w.tau_max)  # load / build
+    t0 = time.perf_counter()
+    for o, g in zip(cpu, gos):
+        ola.forward(o, cl, cu, w.tau_relu, w.tau_max, threads=threads)
+        ola.backward(g, o, cl, cu, w.tau_relu, w.tau_max, threads=threads)
+    dt = time.perf_counter() - t0
+    areas = sample_batches * w.nc * sum(int(o.shape[1]) for o in cpu)
+    return areas / dt, f"{sample_batches} of {w.B} sample-batches, all subset sizes, fwd+bwd"
+
+
+def run_log_areas(args) -> None:
+    from botorch_gb300 import _native as nat
+    from botorch_gb300 import logei_fused as lf
+    from botorch_gb300.testing import log_areas_workload
+
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    lib = nat.lib()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+    res = {}
+    for tag, dtype in (("f64", torch.float64), ("f32", torch.float32)):
+        w = log_areas_workload(dtype=dtype, device=device)
+        g = torch.Generator().manual_seed(1)
+        go = [torch.randn(w.B, w.nc, o.shape[1], generator=g, dtype=torch.float64).to(device, dtype)
+              for o in w.obj_subsets]
+        step = _la_step_fns(w, go)
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize(device)
+        n0 = lib.bgb_launch_count()
+        with ClockSampler(0) as clk:
+            ms = time_steps(step, args.steps, device, flush)
+        launches = lib.bgb_launch_count() - n0
+        # per-kernel times (forward and backward of the largest subset size, i = 2)
+        obj2, go2 = w.obj_subsets[1], go[1]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        flush.zero_()
+        ev[0].record(stream)
+        lf.forward(obj2, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
+        ev[1].record(stream)
+        lf.backward(go2, obj2, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
+        ev[2].record(stream)
+        torch.cuda.synchronize(device)
+        # end to end: host objective samples in (pinned), areas and gradients out (pinned)
+        h_obj = [o.cpu().pin_memory() for o in w.obj_subsets]
+        h_go = [x.cpu().pin_memory() for x in go]
+        h_out = [torch.empty(w.B, w.nc, o.shape[1], dtype=dtype).pin_memory() for o in w.obj_subsets]
+        h_grad = [torch.empty(o.shape, dtype=dtype).pin_memory() for o in w.obj_subsets]
+
+        def e2e_step():
+            for ho, hg, hout, hgr in zip(h_obj, h_go, h_out, h_grad):
+                o = ho.to(device, non_blocking=True)
+                gg = hg.to(device, non_blocking=True)
+                hout.copy_(lf.forward(o, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max), non_blocking=True)
+                hgr.copy_(lf.backward(gg, o, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max), non_blocking=True)
+            torch.cuda.current_stream(device).synchronize()
+
+        e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        h2d = sum(x.numel() * x.element_size() for x in h_obj + h_go)
+        d2h = sum(x.numel() * x.element_size() for x in h_out + h_grad)
+        mean_ms = sum(ms) / len(ms)
+        # algorithmic bytes: objective samples and cells read once, areas written (forward);
+        # grad_out read, gradient written (backward)
+        bytes_step = sum(o.numel() * o.element_size() * 2 + x.numel() * x.element_size() * 2
+                         for o, x in zip(w.obj_subsets, go))
+        res[tag] = {"areas_per_s": w.areas_per_step() / (mean_ms / 1e3), "ms_per_step": mean_ms,
+                    "fwd_ms_i2": ev[0].elapsed_time(ev[1]), "bwd_ms_i2": ev[1].elapsed_time(ev[2]),
+                    "e2e_areas_per_s": w.areas_per_step() / e2e_s, "h2d": h2d, "d2h": d2h,
+                    "launches": launches, "clocks": clk.summary(), "bytes_step": bytes_step,
+                    "log_fatplus_per_step": 2 * w.B * w.nc * w.m * sum(int(o.shape[1] * o.shape[2])
+                                                                        for o in w.obj_subsets)}
+        w_cpu = w
+    peaks = measured_peaks()
+    r = res["f64"]
+    achieved_gbs = r["bytes_step"] / (r["ms_per_step"] / 1e3) / 1e9
+    threads = os.cpu_count() or 1
+    cpu_value, cpu_sample = (None, None)
+    if not args.no_cpu_baseline:
+        w64 = log_areas_workload(dtype=torch.float64)
+        cpu_value, cpu_sample = la_cpu_baseline(w64, threads, 2048)
+    line = {
+        "metric": LA_METRIC, "value": round(r["areas_per_s"], 1), "unit": "areas/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms_per_step"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded objective samples, 63-point front)",
+        "config": {"workload": "log_areas_m2_q4_nc64_B32768", "B": w_cpu.B, "q": 4, "m": 2, "cells": 64,
+                   "areas_per_step": w_cpu.areas_per_step(), "l2": "flushed before each step (256 MB write)"},
+        "e2e": {"value": round(r["e2e_areas_per_s"], 1), "unit": "areas/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"]},
+        "roofline": {"bound": "fp64 pipe (transcendentals); hbm shown", "achieved": round(achieved_gbs, 1),
+                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": round(achieved_gbs / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None,
+                     "traffic": None},
+        "log_fatplus_evals_per_s": round(r["log_fatplus_per_step"] / (r["ms_per_step"] / 1e3), 1),
+        "kernel_ms_subset2": {"forward": round(r["fwd_ms_i2"], 4), "backward": round(r["bwd_ms_i2"], 4)},
+        "f32": {"value": round(res["f32"]["areas_per_s"], 1), "ms_per_step": round(res["f32"]["ms_per_step"], 4),
+                "e2e": round(res["f32"]["e2e_areas_per_s"], 1),
+                "kernel_ms_subset2": {"forward": round(res["f32"]["fwd_ms_i2"], 4),
+                                      "backward": round(res["f32"]["bwd_ms_i2"], 4)}},
+        "cpu_baseline": None if cpu_value is None else {
+            "value": round(cpu_value, 1), "unit": "areas/s", "cores": threads, "kind": "port",
+            "sample": cpu_sample + " (C restatement of the reference kernel, bit-exact to it on x86-64)"},
+        "gpu_launches": int(r["launches"]), "clocks": r["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_log_areas_reference(args) -> None:
+    """Reference arm of the log-areas benchmark: the reference kernel's C restatement
+    (bit-exact to botorch/csrc/logei_fused.cpp where that compiles) on all host cores."""
+    world, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from botorch_gb300.testing import log_areas_workload
+
+    w = log_areas_workload(dtype=torch.float64)
+    threads = os.cpu_count() or 1
+    sample = 1024
+    for _ in range(max(args.warmup, 1)):
+        la_cpu_baseline(w, threads, 256)
+    vals = [la_cpu_baseline(w, threads, sample) for _ in range(args.steps)]
+    value = statistics.median(v for v, _ in vals)
+    line = {"metric": LA_METRIC, "value": round(value, 1), "unit": "areas/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded objective samples, 63-point front)",
+            "impl": "reference",
+            "config": {"workload": "log_areas_m2_q4_nc64_B32768", "B": w.B, "q": 4, "m": 2, "cells": 64},
+            "cpu_baseline": {"value": round(value, 1), "unit": "areas/s", "cores": threads, "kind": "port",
+                             "sample": vals[0][1]},
+            "e2e": {"value": round(value, 1), "unit": "areas/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- reference arm
 def run_reference(args) -> None:
     world, rank, _ = dist_info()
@@ -587,8 +748,12 @@ def run_reference(args) -> None:
 
 def main() -> None:
     args = parse()
-    if args.impl == "reference":
+    if args.impl == "reference" and args.config == "log_areas":
+        run_log_areas_reference(args)
+    elif args.impl == "reference":
         run_reference(args)
+    elif args.config == "log_areas":
+        run_log_areas(args)
     elif args.config == "many_gps":
         run_many_gps(args)
     elif args.config == "optimize":

@@ -113,6 +113,14 @@ _SIGNATURES = {
                                                c_vp]),
     "bgb_acq_forward_backward_noalloc": (c_i32, [ctypes.POINTER(BgbAcq), c_vp, c_i64, c_vp, c_vp,
                                                  c_vp, c_vp]),
+    "bgb_log_areas_forward": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64, c_i64,
+                                      c_f64, c_f64, c_vp, c_vp]),
+    "bgb_log_areas_forward_f32": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64,
+                                          c_i64, c_f64, c_f64, c_vp, c_vp]),
+    "bgb_log_areas_backward": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64,
+                                       c_i64, c_f64, c_f64, c_vp, c_vp]),
+    "bgb_log_areas_backward_f32": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp,
+                                           c_i64, c_i64, c_f64, c_f64, c_vp, c_vp]),
     "bgb_launch_count": (ctypes.c_ulonglong, []),
 }
 

@@ -1,0 +1,115 @@
+"""Fused log-areas of qLogEHVI / qLogNEHVI on the GPU.
+
+Drop-in for the reference's fused CPU extension (the module-level ``_C`` of
+botorch/acquisition/multi_objective/logei.py:59-104, built from
+botorch/csrc/logei_fused.cpp): ``forward`` and ``backward`` take the same
+arguments, check them the same way and return the same shapes, for CUDA
+tensors. ``FusedLogAreas`` mirrors the reference's ``_FusedLogAreas``
+autograd function (logei.py:107-165).
+
+    forward(obj_subsets, cell_lower, cell_upper, tau_relu, tau_max)
+        obj_subsets (B, n_sub, i, m), cells (nc, m) or (B, nc, m) -> (B, nc, n_sub)
+    backward(grad_output, obj_subsets, cell_lower, cell_upper, tau_relu, tau_max)
+        -> gradient w.r.t. obj_subsets, (B, n_sub, i, m)
+
+float64 and float32 inputs compute in their own type, as the reference's
+AT_DISPATCH_FLOATING_TYPES. There is no CPU path: CPU tensors raise.
+"""
+
+from __future__ import annotations
+
+import torch
+from torch import Tensor
+
+from botorch_gb300 import _native as nat
+
+MAX_I = 32  # largest subset size (the reference's _FUSED_MAX_I / MAX_I)
+MAX_M = 8   # largest number of objectives (the reference's MAX_M)
+
+
+def _prepare(obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor):
+    obj = obj_subsets.contiguous()
+    cl = cell_lower.contiguous()
+    cu = cell_upper.contiguous()
+    if obj.dim() != 4:
+        raise RuntimeError("obj_subsets must be 4-D")
+    if not ((cl.dim() == 2 or cl.dim() == 3) and cl.dim() == cu.dim()):
+        raise RuntimeError("cell bounds must be 2-D or 3-D")
+    B, n_sub, isz, m = obj.shape
+    if isz > MAX_I or m > MAX_M:
+        raise RuntimeError("subset_size or m too large")
+    if obj.dtype not in (torch.float64, torch.float32):
+        raise RuntimeError(f"fused log-areas: unsupported dtype {obj.dtype}")
+    if obj.device.type != "cuda":
+        raise RuntimeError("fused log-areas: the inputs must be CUDA tensors (no CPU path)")
+    if cl.dtype != obj.dtype or cu.dtype != obj.dtype or cl.device != obj.device or cu.device != obj.device:
+        raise RuntimeError("fused log-areas: cell bounds must match obj_subsets in dtype and device")
+    if cl.shape != cu.shape or cl.shape[-1] != m:
+        raise RuntimeError("fused log-areas: cell bounds must be (..., num_cells, m) and of equal shape")
+    B_cells = cl.shape[0] if cl.dim() == 3 else 1
+    nc = cl.shape[-2]
+    if cl.dim() == 3 and B_cells != B:
+        raise RuntimeError("fused log-areas: batched cell bounds need one batch per obj_subsets batch")
+    return obj, cl, cu, (B, n_sub, isz, m, B_cells, nc)
+
+
+def forward(obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor, tau_relu: float,
+            tau_max: float) -> Tensor:
+    """Log areas (B, nc, n_sub) of every cell and q-subset (logei_fused.cpp:184-264)."""
+    obj, cl, cu, (B, n_sub, isz, m, B_cells, nc) = _prepare(obj_subsets, cell_lower, cell_upper)
+    out = torch.empty(B, nc, n_sub, dtype=obj.dtype, device=obj.device)
+    fn = nat.lib().bgb_log_areas_forward if obj.dtype == torch.float64 else nat.lib().bgb_log_areas_forward_f32
+    with torch.cuda.device(obj.device):
+        rc = fn(obj.data_ptr(), B, n_sub, isz, m, cl.data_ptr(), cu.data_ptr(), B_cells, nc,
+                float(tau_relu), float(tau_max), out.data_ptr(), nat.stream_handle(obj.device))
+    nat.check(rc, "bgb_log_areas_forward")
+    return out
+
+
+def backward(grad_output: Tensor, obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor,
+             tau_relu: float, tau_max: float) -> Tensor:
+    """Gradient of sum(grad_output * forward(...)) w.r.t. obj_subsets (logei_fused.cpp:266-374)."""
+    obj, cl, cu, (B, n_sub, isz, m, B_cells, nc) = _prepare(obj_subsets, cell_lower, cell_upper)
+    go = grad_output.contiguous()
+    if tuple(go.shape) != (B, nc, n_sub) or go.dtype != obj.dtype or go.device != obj.device:
+        raise RuntimeError("fused log-areas: grad_output must be (B, num_cells, n_sub) like the forward output")
+    g_obj = torch.empty_like(obj)
+    fn = (nat.lib().bgb_log_areas_backward if obj.dtype == torch.float64
+          else nat.lib().bgb_log_areas_backward_f32)
+    with torch.cuda.device(obj.device):
+        rc = fn(go.data_ptr(), obj.data_ptr(), B, n_sub, isz, m, cl.data_ptr(), cu.data_ptr(),
+                B_cells, nc, float(tau_relu), float(tau_max), g_obj.data_ptr(),
+                nat.stream_handle(obj.device))
+    nat.check(rc, "bgb_log_areas_backward")
+    return g_obj
+
+
+class FusedLogAreas(torch.autograd.Function):
+    """Autograd wrapper with the reference's ``_FusedLogAreas`` contract:
+    ``obj_subsets`` (*batch, n_sub, i, m) and cell bounds (nc, m) or
+    (*batch, nc, m) -> (*batch, nc, n_sub); only ``obj_subsets`` gets a gradient."""
+
+    @staticmethod
+    def forward(ctx, obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor, tau_relu: float,
+                tau_max: float) -> Tensor:
+        batch_shape = obj_subsets.shape[:-3]
+        B = max(1, int(torch.Size(batch_shape).numel()))
+        obj_flat = obj_subsets.reshape(B, *obj_subsets.shape[-3:])
+        nc, m_cells = cell_lower.shape[-2], cell_lower.shape[-1]
+        if cell_lower.ndim > 2:
+            cell_lower = cell_lower.reshape(-1, nc, m_cells)
+            cell_upper = cell_upper.reshape(-1, nc, m_cells)
+        result = forward(obj_flat, cell_lower, cell_upper, tau_relu, tau_max)
+        ctx.save_for_backward(obj_flat, cell_lower, cell_upper)
+        ctx.tau_relu = tau_relu
+        ctx.tau_max = tau_max
+        ctx.orig_shape = obj_subsets.shape
+        return result.reshape(*batch_shape, result.shape[-2], result.shape[-1])
+
+    @staticmethod
+    def backward(ctx, grad_output: Tensor):
+        obj_flat, cell_lower, cell_upper = ctx.saved_tensors
+        B = obj_flat.shape[0]
+        grad_flat = grad_output.reshape(B, *grad_output.shape[-2:])
+        grad_obj = backward(grad_flat, obj_flat, cell_lower, cell_upper, ctx.tau_relu, ctx.tau_max)
+        return grad_obj.reshape(ctx.orig_shape), None, None, None, None

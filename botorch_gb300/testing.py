@@ -20,6 +20,12 @@ the reference). The generators are:
   features, ARD lengthscales ~ U[0.1, 2.0]) + N(0, 0.01^2); Matern-5/2 with those
   lengthscales, outputscale 1, noise 1e-4; qLogNEI with 1024 samples, optimised
   from 65536 raw q-batches of q=16 over 64 restarts.
+* ``log_areas_workload``: the inner loop of qLogEHVI with m=2 objectives and
+  q=4 candidates: objective samples N(0.5, 0.3^2) for 128 MC samples x 256
+  restarts (B = 32768 sample-batches), their q-subsets of sizes 1..4, and the
+  64 cells of the non-dominated region of a 63-point front on
+  y2 = 1 - y1^2 above the reference point (-0.1, -0.1) (the outer cells
+  unbounded above).
 * ``many_gps``: independent problems of uneven size, n ~ log-uniform [100, 4000]
   and d ~ uniform {4..30} per model, X ~ U[0,1]^d, y = an RFF draw (1024
   features, lengthscale 0.3) + N(0, 0.01^2); Matern-5/2 with lengthscale 0.3,
@@ -134,3 +140,48 @@ def optimization_step(n: int = 4096, d: int = 50, seed: int = 0) -> Workload:
                     torch.empty(0, 16, d, dtype=torch.float64), 1024, seed, "qLogNEI",
                     extra={"raw_samples": 65536, "restarts": 64, "q": 16})
 
+
+
+@dataclass
+class LogAreasWorkload:
+    B: int                      # sample-batches (MC samples x restarts)
+    q: int
+    m: int
+    obj_subsets: list           # [i = 1..q] (B, C(q, i), i, m)
+    cell_lower: Tensor          # (nc, m)
+    cell_upper: Tensor
+    tau_relu: float = 1e-6      # the reference's TAU_RELU (botorch/acquisition/logei.py:67)
+    tau_max: float = 1e-2       # the reference's TAU_MAX
+
+    @property
+    def nc(self) -> int:
+        return int(self.cell_lower.shape[0])
+
+    def areas_per_step(self) -> int:
+        """(sample-batch, cell, subset) log areas of one pass over all subset sizes."""
+        return self.B * self.nc * sum(int(o.shape[1]) for o in self.obj_subsets)
+
+
+def log_areas_workload(mc: int = 128, restarts: int = 256, q: int = 4, n_pareto: int = 63,
+                       seed: int = 0, dtype: torch.dtype = torch.float64,
+                       device: torch.device | str = "cpu") -> LogAreasWorkload:
+    import itertools
+
+    g = torch.Generator().manual_seed(seed)
+    B = mc * restarts
+    Y = 0.5 + 0.3 * torch.randn(B, q, 2, generator=g, dtype=torch.float64)
+    subsets = []
+    for i in range(1, q + 1):
+        idx = torch.tensor(list(itertools.combinations(range(q), i)), dtype=torch.long)  # C(q,i) x i
+        subsets.append(Y[:, idx.reshape(-1)].reshape(B, idx.shape[0], i, 2))
+    y1 = torch.sort(torch.rand(n_pareto, generator=g, dtype=torch.float64)).values
+    y2 = 1.0 - y1 ** 2
+    ref = -0.1
+    inf = float("inf")
+    # cell k spans y1 in [x_k, x_{k+1}) above the front: x_0 = ref, x_k = y1_{k-1}
+    xs = torch.cat([torch.tensor([ref], dtype=torch.float64), y1])
+    lower = torch.stack([xs, torch.cat([y2, torch.tensor([ref], dtype=torch.float64)])], dim=-1)
+    upper = torch.stack([torch.cat([y1, torch.tensor([inf], dtype=torch.float64)]),
+                         torch.full((n_pareto + 1,), inf, dtype=torch.float64)], dim=-1)
+    cast = lambda t: t.to(device=device, dtype=dtype).contiguous()  # noqa: E731
+    return LogAreasWorkload(B, q, 2, [cast(o) for o in subsets], cast(lower), cast(upper))

@@ -323,6 +323,36 @@ int bgb_acq_forward_backward_timed(const bgb_acq_t* acq, const double* X, int64_
 int bgb_acq_forward_backward_noalloc(const bgb_acq_t* acq, const double* X, int64_t b,
                                      double* value, double* grad, int32_t* status, void* stream);
 
+/* ---- Fused log-areas of qLogEHVI / qLogNEHVI (the inner loop of
+ * _compute_log_qehvi, botorch/acquisition/multi_objective/logei.py:272-392).
+ * Replace the reference's CPU extension botorch/csrc/logei_fused.cpp:
+ * bgb_log_areas_forward  <- fused_log_areas_forward  (logei_fused.cpp:184-264),
+ * bgb_log_areas_backward <- fused_log_areas_backward (logei_fused.cpp:266-374).
+ * All pointers are device pointers to contiguous row-major arrays:
+ *   obj       (B, n_sub, isz, m)  objective values of the q-subsets of size isz
+ *   cell_lower, cell_upper (B_cells, nc, m), B_cells == 1 (shared cells) or B
+ *   out       (B, nc, n_sub)      log area of each cell and subset
+ *   grad_out  (B, nc, n_sub), grad_obj (B, n_sub, isz, m)
+ * Limits as the reference's: 1 <= isz <= 32, 1 <= m <= 8 (larger returns
+ * BGB_ERR_UNSUPPORTED); tau_relu, tau_max > 0. Empty B, n_sub or nc is a no-op
+ * (grad_obj is zero-filled when nc == 0). The *_f32 forms compute in float
+ * with the reference's float clamp of the upper bounds (1e8; 1e10 in double). */
+int bgb_log_areas_forward(const double* obj, int64_t B, int64_t n_sub, int64_t isz, int64_t m,
+                          const double* cell_lower, const double* cell_upper, int64_t B_cells,
+                          int64_t nc, double tau_relu, double tau_max, double* out, void* stream);
+int bgb_log_areas_forward_f32(const float* obj, int64_t B, int64_t n_sub, int64_t isz, int64_t m,
+                              const float* cell_lower, const float* cell_upper, int64_t B_cells,
+                              int64_t nc, double tau_relu, double tau_max, float* out,
+                              void* stream);
+int bgb_log_areas_backward(const double* grad_out, const double* obj, int64_t B, int64_t n_sub,
+                           int64_t isz, int64_t m, const double* cell_lower,
+                           const double* cell_upper, int64_t B_cells, int64_t nc, double tau_relu,
+                           double tau_max, double* grad_obj, void* stream);
+int bgb_log_areas_backward_f32(const float* grad_out, const float* obj, int64_t B, int64_t n_sub,
+                               int64_t isz, int64_t m, const float* cell_lower,
+                               const float* cell_upper, int64_t B_cells, int64_t nc,
+                               double tau_relu, double tau_max, float* grad_obj, void* stream);
+
 /* Number of kernel launches this library has issued in the process so far.
  * Measurement aid; no reference counterpart. */
 unsigned long long bgb_launch_count(void);
