@@ -552,13 +552,20 @@ LA_METRIC = ("qLogEHVI fused log-areas forward+backward, (sample-batch, cell, su
 
 
 def _la_step_fns(w, go):
+    """(step through the Jacobian route that FusedLogAreas takes under autograd,
+    step through the reference extension's forward / backward contract)"""
     from botorch_gb300 import logei_fused as lf
 
-    def step():
+    def step_jac():
+        for obj, g in zip(w.obj_subsets, go):
+            _, jac = lf.forward_with_jacobian(obj, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
+            lf.backward_from_jacobian(g, jac)
+
+    def step_recompute():
         for obj, g in zip(w.obj_subsets, go):
             lf.forward(obj, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
             lf.backward(g, obj, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
-    return step
+    return step_jac, step_recompute
 
 
 def la_cpu_baseline(w, threads: int, sample_batches: int) -> tuple[float, str]:
@@ -595,36 +602,46 @@ def run_log_areas(args) -> None:
         g = torch.Generator().manual_seed(1)
         go = [torch.randn(w.B, w.nc, o.shape[1], generator=g, dtype=torch.float64).to(device, dtype)
               for o in w.obj_subsets]
-        step = _la_step_fns(w, go)
+        step, step_rc = _la_step_fns(w, go)
         for _ in range(max(args.warmup, 3)):
             step()
+            step_rc()
         torch.cuda.synchronize(device)
         n0 = lib.bgb_launch_count()
         with ClockSampler(0) as clk:
             ms = time_steps(step, args.steps, device, flush)
         launches = lib.bgb_launch_count() - n0
+        ms_rc = time_steps(step_rc, args.steps, device, flush)
         # per-kernel times (forward and backward of the largest subset size, i = 2)
         obj2, go2 = w.obj_subsets[1], go[1]
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
         flush.zero_()
         ev[0].record(stream)
         lf.forward(obj2, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
         ev[1].record(stream)
         lf.backward(go2, obj2, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
         ev[2].record(stream)
+        _, jac2 = lf.forward_with_jacobian(obj2, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
+        ev[3].record(stream)
+        lf.backward_from_jacobian(go2, jac2)
+        ev[4].record(stream)
         torch.cuda.synchronize(device)
+        jac_bytes2 = jac2.numel() * jac2.element_size()
+        del jac2
         # end to end: host objective samples in (pinned), areas and gradients out (pinned)
         h_obj = [o.cpu().pin_memory() for o in w.obj_subsets]
         h_go = [x.cpu().pin_memory() for x in go]
         h_out = [torch.empty(w.B, w.nc, o.shape[1], dtype=dtype).pin_memory() for o in w.obj_subsets]
         h_grad = [torch.empty(o.shape, dtype=dtype).pin_memory() for o in w.obj_subsets]
 
-        def e2e_step():
+        def e2e_step():  # through the autograd function, as the acquisition function calls it
             for ho, hg, hout, hgr in zip(h_obj, h_go, h_out, h_grad):
-                o = ho.to(device, non_blocking=True)
+                o = ho.to(device, non_blocking=True).requires_grad_(True)
                 gg = hg.to(device, non_blocking=True)
-                hout.copy_(lf.forward(o, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max), non_blocking=True)
-                hgr.copy_(lf.backward(gg, o, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max), non_blocking=True)
+                a = lf.FusedLogAreas.apply(o, w.cell_lower, w.cell_upper, w.tau_relu, w.tau_max)
+                (gr,) = torch.autograd.grad(a, o, gg)
+                hout.copy_(a.detach(), non_blocking=True)
+                hgr.copy_(gr, non_blocking=True)
             torch.cuda.current_stream(device).synchronize()
 
         e2e_step()
@@ -638,9 +655,13 @@ def run_log_areas(args) -> None:
         # algorithmic bytes: objective samples and cells read once, areas written (forward);
         # grad_out read, gradient written (backward)
         bytes_step = sum(o.numel() * o.element_size() * 2 + x.numel() * x.element_size() * 2
+                         + 2 * x.numel() * o.shape[2] * o.shape[3] * o.element_size()
                          for o, x in zip(w.obj_subsets, go))
         res[tag] = {"areas_per_s": w.areas_per_step() / (mean_ms / 1e3), "ms_per_step": mean_ms,
+                    "recompute_areas_per_s": w.areas_per_step() / (sum(ms_rc) / len(ms_rc) / 1e3),
                     "fwd_ms_i2": ev[0].elapsed_time(ev[1]), "bwd_ms_i2": ev[1].elapsed_time(ev[2]),
+                    "fwdjac_ms_i2": ev[2].elapsed_time(ev[3]), "bwdjac_ms_i2": ev[3].elapsed_time(ev[4]),
+                    "jac_bytes_i2": jac_bytes2,
                     "e2e_areas_per_s": w.areas_per_step() / e2e_s, "h2d": h2d, "d2h": d2h,
                     "launches": launches, "clocks": clk.summary(), "bytes_step": bytes_step,
                     "log_fatplus_per_step": 2 * w.B * w.nc * w.m * sum(int(o.shape[1] * o.shape[2])
@@ -667,12 +688,19 @@ def run_log_areas(args) -> None:
                      "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                      "frac": round(achieved_gbs / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None,
                      "traffic": None},
-        "log_fatplus_evals_per_s": round(r["log_fatplus_per_step"] / (r["ms_per_step"] / 1e3), 1),
-        "kernel_ms_subset2": {"forward": round(r["fwd_ms_i2"], 4), "backward": round(r["bwd_ms_i2"], 4)},
+        "route": "Jacobian kept by the forward, backward = HBM contraction (FusedLogAreas under autograd)",
+        "recompute_route_areas_per_s": round(r["recompute_areas_per_s"], 1),
+        "kernel_ms_subset2": {"forward": round(r["fwd_ms_i2"], 4), "backward": round(r["bwd_ms_i2"], 4),
+                              "forward_jacobian": round(r["fwdjac_ms_i2"], 4),
+                              "backward_from_jacobian": round(r["bwdjac_ms_i2"], 4),
+                              "jacobian_bytes": r["jac_bytes_i2"]},
         "f32": {"value": round(res["f32"]["areas_per_s"], 1), "ms_per_step": round(res["f32"]["ms_per_step"], 4),
+                "recompute_route_areas_per_s": round(res["f32"]["recompute_areas_per_s"], 1),
                 "e2e": round(res["f32"]["e2e_areas_per_s"], 1),
                 "kernel_ms_subset2": {"forward": round(res["f32"]["fwd_ms_i2"], 4),
-                                      "backward": round(res["f32"]["bwd_ms_i2"], 4)}},
+                                      "backward": round(res["f32"]["bwd_ms_i2"], 4),
+                                      "forward_jacobian": round(res["f32"]["fwdjac_ms_i2"], 4),
+                                      "backward_from_jacobian": round(res["f32"]["bwdjac_ms_i2"], 4)}},
         "cpu_baseline": None if cpu_value is None else {
             "value": round(cpu_value, 1), "unit": "areas/s", "cores": threads, "kind": "port",
             "sample": cpu_sample + " (C restatement of the reference kernel, bit-exact to it on x86-64)"},

@@ -121,6 +121,14 @@ _SIGNATURES = {
                                        c_i64, c_f64, c_f64, c_vp, c_vp]),
     "bgb_log_areas_backward_f32": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp,
                                            c_i64, c_i64, c_f64, c_f64, c_vp, c_vp]),
+    "bgb_log_areas_forward_jac": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64,
+                                          c_i64, c_f64, c_f64, c_vp, c_vp, c_vp]),
+    "bgb_log_areas_forward_jac_f32": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64,
+                                              c_i64, c_f64, c_f64, c_vp, c_vp, c_vp]),
+    "bgb_log_areas_backward_jac": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp,
+                                           c_vp]),
+    "bgb_log_areas_backward_jac_f32": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp,
+                                               c_vp]),
     "bgb_launch_count": (ctypes.c_ulonglong, []),
 }
 

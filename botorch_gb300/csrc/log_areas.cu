@@ -41,24 +41,33 @@ template <> struct LaMath<double> {
     static __device__ __forceinline__ double log_(double x) { return log(x); }
     static __device__ __forceinline__ double log1p_(double x) { return log1p(x); }
     static constexpr double kClamp = 1e10;
+    static constexpr double kExpZero = -750.0;  // exp(y) rounds to +0 below this
+    static constexpr double kSigOne = 38.0;     // 1 + exp(-y) rounds to 1 above this
 };
 template <> struct LaMath<float> {
     static __device__ __forceinline__ float exp_(float x) { return expf(x); }
     static __device__ __forceinline__ float log_(float x) { return logf(x); }
     static __device__ __forceinline__ float log1p_(float x) { return log1pf(x); }
     static constexpr float kClamp = 1e8f;
+    static constexpr float kExpZero = -105.f;
+    static constexpr float kSigOne = 18.f;
 };
 
+// The exp calls are skipped where their result is exactly what the rounded
+// arithmetic gives anyway (exp underflowing to +0, 1 + exp(-y) rounding to
+// 1): the values are unchanged and most elements, far from the cell corners
+// (|y| = |x| / tau_relu >> 20), need no exp at all.
 template <typename T>
 __device__ __forceinline__ T la_softplus(T y) {
     if (y > T(20)) return y;
-    if (y < T(-20)) return LaMath<T>::exp_(y);
+    if (y < T(-20)) return y < LaMath<T>::kExpZero ? T(0) : LaMath<T>::exp_(y);
     return LaMath<T>::log1p_(LaMath<T>::exp_(y));
 }
 
 template <typename T>
 __device__ __forceinline__ T la_sigmoid(T y) {
-    if (y >= T(0)) return T(1) / (T(1) + LaMath<T>::exp_(-y));
+    if (y >= T(0)) return y > LaMath<T>::kSigOne ? T(1) : T(1) / (T(1) + LaMath<T>::exp_(-y));
+    if (y < LaMath<T>::kExpZero) return T(0);
     const T e = LaMath<T>::exp_(y);
     return e / (T(1) + e);
 }
@@ -170,6 +179,102 @@ __global__ void __launch_bounds__(kLaThreads) log_areas_forward_kernel(
             area += la_fatmin2(lim, lcl, tau_max, inv_max, (T*)nullptr);
         }
         out[idx] = area;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forward that also keeps the Jacobian of each area with respect to its
+// subset's objective values: jac[b][c][s][j][k] = d out[b][c][s] / d obj[b][s][j][k]
+// (the pair fatmin's weight x the subset fatmin's weight x d log_fatplus / dx).
+// Same thread layout as the forward; each thread writes its i m entries
+// contiguously, so a warp writes one contiguous run.
+template <typename T, int IM>
+__global__ void __launch_bounds__(kLaThreads) log_areas_forward_jac_kernel(
+    const T* __restrict__ obj, int64_t B, int64_t n_sub, int isz, int m,
+    const T* __restrict__ lower, const T* __restrict__ upper, int64_t B_cells, int64_t nc,
+    T tau_relu, T tau_max, T* __restrict__ out, T* __restrict__ jac) {
+    const int64_t total = B * nc * n_sub;
+    const T inv_relu = T(1) / tau_relu, inv_max = T(1) / tau_max;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = idx % n_sub;
+        const int64_t bc = idx / n_sub;
+        const int64_t c = bc % nc, b = bc / nc;
+        const int64_t cb = B_cells == 1 ? 0 : b;
+        const T* o = obj + (b * n_sub + s) * isz * m;
+        const T* lo = lower + (cb * nc + c) * m;
+        const T* up = upper + (cb * nc + c) * m;
+        T* J = jac + idx * isz * m;
+        T area = T(0);
+        for (int k = 0; k < m; ++k) {
+            const T lk = lo[k];
+            const T lcl = LaMath<T>::log_(la_min_clamp(up[k]) - lk);
+            T li[IM], lg[IM];
+            T mn = T(0);
+            int ami = 0;
+#pragma unroll
+            for (int j = 0; j < IM; ++j) {
+                if (j < isz) {
+                    la_log_fatplus_grad(o[j * m + k] - lk, tau_relu, inv_relu, li[j], lg[j]);
+                    if (j == 0 || li[j] < mn) {
+                        mn = li[j];
+                        ami = j;
+                    }
+                }
+            }
+            if (isz == 1 || mn < T(-1e29)) {
+                const T lim = isz == 1 ? li[0] : mn;
+                T g2;
+                area += la_fatmin2(lim, lcl, tau_max, inv_max, &g2);
+#pragma unroll
+                for (int j = 0; j < IM; ++j)
+                    if (j < isz) J[j * m + k] = j == ami ? g2 * lg[j] : T(0);
+            } else {
+                T S = T(0), S_pd = T(0);
+#pragma unroll
+                for (int j = 0; j < IM; ++j) {
+                    if (j < isz) {
+                        const T z = (li[j] - mn) * inv_max;
+                        S += la_pareto(z);
+                        li[j] = la_pareto_deriv(z);  // li[j] now holds pareto'(z_j)
+                        S_pd += li[j];
+                    }
+                }
+                const T lim = mn - tau_max * LaMath<T>::log_(S);
+                T g2;
+                area += la_fatmin2(lim, lcl, tau_max, inv_max, &g2);
+#pragma unroll
+                for (int j = 0; j < IM; ++j) {
+                    if (j < isz) {
+                        const T w = j == ami ? T(1) + (S_pd + T(1)) / S : -li[j] / S;
+                        J[j * m + k] = g2 * w * lg[j];
+                    }
+                }
+            }
+        }
+        out[idx] = area;
+    }
+}
+
+// g_obj[b][s][e] = sum_c g_out[b][c][s] jac[b][c][s][e], e = (j, k): one thread
+// per (b, s, e), e fastest, so consecutive threads read consecutive Jacobian
+// entries of one cell; cells in order.
+template <typename T>
+__global__ void __launch_bounds__(kLaThreads) log_areas_backward_jac_kernel(
+    const T* __restrict__ g_out, const T* __restrict__ jac, int64_t B, int64_t n_sub, int im,
+    int64_t nc, T* __restrict__ g_obj) {
+    const int64_t total = B * n_sub * im;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t % im;
+        const int64_t bs = t / im;
+        const int64_t s = bs % n_sub, b = bs / n_sub;
+        const T* J = jac + (b * nc * n_sub + s) * im + e;  // cell 0
+        const T* go = g_out + b * nc * n_sub + s;
+        const int64_t cstride = n_sub * im;
+        T acc = T(0);
+        for (int64_t c = 0; c < nc; ++c) acc = fma(go[c * n_sub], J[c * cstride], acc);
+        g_obj[t] = acc;
     }
 }
 
@@ -347,6 +452,55 @@ int log_areas_backward(const T* g_out, const T* obj, int64_t B, int64_t n_sub, i
     return BGB_OK;
 }
 
+template <typename T>
+int log_areas_forward_jac(const T* obj, int64_t B, int64_t n_sub, int64_t isz, int64_t m,
+                          const T* lower, const T* upper, int64_t B_cells, int64_t nc,
+                          double tau_relu, double tau_max, T* out, T* jac, cudaStream_t st) {
+    int rc = la_check(B, n_sub, isz, m, B_cells, nc, tau_relu, tau_max);
+    if (rc) return rc;
+    const int64_t total = B * nc * n_sub;
+    if (total == 0) return BGB_OK;
+    if (!obj || !lower || !upper || !out || !jac) return BGB_ERR_ARG;
+    const int64_t want = (total + kLaThreads - 1) / kLaThreads;
+    const int64_t cap = (int64_t)sm_count_la() * 32;
+    const unsigned grid = (unsigned)(want < cap ? want : cap);
+#define BGB_LA_FJ(IM)                                                                           \
+    log_areas_forward_jac_kernel<T, IM><<<grid, kLaThreads, 0, st>>>(                           \
+        obj, B, n_sub, (int)isz, (int)m, lower, upper, B_cells, nc, (T)tau_relu, (T)tau_max,    \
+        out, jac)
+    switch (la_bucket(isz)) {
+        case 4: BGB_LA_FJ(4); break;
+        case 8: BGB_LA_FJ(8); break;
+        case 16: BGB_LA_FJ(16); break;
+        default: BGB_LA_FJ(32); break;
+    }
+#undef BGB_LA_FJ
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+template <typename T>
+int log_areas_backward_jac(const T* g_out, const T* jac, int64_t B, int64_t n_sub, int64_t isz,
+                           int64_t m, int64_t nc, T* g_obj, cudaStream_t st) {
+    if (B < 0 || n_sub < 0 || nc < 0 || isz < 1 || m < 1) return BGB_ERR_ARG;
+    if (isz > kLaMaxI || m > kLaMaxM) return BGB_ERR_UNSUPPORTED;
+    const int64_t total = B * n_sub * isz * m;
+    if (total == 0) return BGB_OK;
+    if (!g_obj) return BGB_ERR_ARG;
+    if (nc == 0) {
+        BGB_CUDA_TRY(cudaMemsetAsync(g_obj, 0, sizeof(T) * (size_t)total, st));
+        return BGB_OK;
+    }
+    if (!g_out || !jac) return BGB_ERR_ARG;
+    const int64_t want = (total + kLaThreads - 1) / kLaThreads;
+    const int64_t cap = (int64_t)sm_count_la() * 32;
+    const unsigned grid = (unsigned)(want < cap ? want : cap);
+    log_areas_backward_jac_kernel<T><<<grid, kLaThreads, 0, st>>>(g_out, jac, B, n_sub,
+                                                                   (int)(isz * m), nc, g_obj);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
 }  // namespace
 
 }  // namespace bgb
@@ -386,6 +540,38 @@ int bgb_log_areas_backward_f32(const float* grad_out, const float* obj, int64_t 
     return bgb::log_areas_backward<float>(grad_out, obj, B, n_sub, isz, m, cell_lower, cell_upper,
                                           B_cells, nc, tau_relu, tau_max, grad_obj,
                                           static_cast<cudaStream_t>(stream));
+}
+
+int bgb_log_areas_forward_jac(const double* obj, int64_t B, int64_t n_sub, int64_t isz, int64_t m,
+                              const double* cell_lower, const double* cell_upper, int64_t B_cells,
+                              int64_t nc, double tau_relu, double tau_max, double* out,
+                              double* jac, void* stream) {
+    return bgb::log_areas_forward_jac<double>(obj, B, n_sub, isz, m, cell_lower, cell_upper,
+                                              B_cells, nc, tau_relu, tau_max, out, jac,
+                                              static_cast<cudaStream_t>(stream));
+}
+
+int bgb_log_areas_forward_jac_f32(const float* obj, int64_t B, int64_t n_sub, int64_t isz,
+                                  int64_t m, const float* cell_lower, const float* cell_upper,
+                                  int64_t B_cells, int64_t nc, double tau_relu, double tau_max,
+                                  float* out, float* jac, void* stream) {
+    return bgb::log_areas_forward_jac<float>(obj, B, n_sub, isz, m, cell_lower, cell_upper,
+                                             B_cells, nc, tau_relu, tau_max, out, jac,
+                                             static_cast<cudaStream_t>(stream));
+}
+
+int bgb_log_areas_backward_jac(const double* grad_out, const double* jac, int64_t B,
+                               int64_t n_sub, int64_t isz, int64_t m, int64_t nc,
+                               double* grad_obj, void* stream) {
+    return bgb::log_areas_backward_jac<double>(grad_out, jac, B, n_sub, isz, m, nc, grad_obj,
+                                               static_cast<cudaStream_t>(stream));
+}
+
+int bgb_log_areas_backward_jac_f32(const float* grad_out, const float* jac, int64_t B,
+                                   int64_t n_sub, int64_t isz, int64_t m, int64_t nc,
+                                   float* grad_obj, void* stream) {
+    return bgb::log_areas_backward_jac<float>(grad_out, jac, B, n_sub, isz, m, nc, grad_obj,
+                                              static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

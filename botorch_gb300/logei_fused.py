@@ -14,6 +14,13 @@ autograd function (logei.py:107-165).
 
 float64 and float32 inputs compute in their own type, as the reference's
 AT_DISPATCH_FLOATING_TYPES. There is no CPU path: CPU tensors raise.
+
+``FusedLogAreas`` differs from the reference in one respect: when the input
+needs a gradient and the Jacobian fits ``JACOBIAN_BUDGET_BYTES``, its forward
+also keeps d area / d obj (``forward_with_jacobian``) and its backward is
+the contraction of grad_output with it (``backward_from_jacobian``), instead
+of recomputing the forward quantities. On GB300 the recomputation is bound
+by the float64 pipe while the Jacobian costs 8 i m bytes of HBM per area.
 """
 
 from __future__ import annotations
@@ -25,6 +32,7 @@ from botorch_gb300 import _native as nat
 
 MAX_I = 32  # largest subset size (the reference's _FUSED_MAX_I / MAX_I)
 MAX_M = 8   # largest number of objectives (the reference's MAX_M)
+JACOBIAN_BUDGET_BYTES = 8 << 30  # largest Jacobian FusedLogAreas keeps for its backward
 
 
 def _prepare(obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor):
@@ -84,6 +92,43 @@ def backward(grad_output: Tensor, obj_subsets: Tensor, cell_lower: Tensor, cell_
     return g_obj
 
 
+def forward_with_jacobian(obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor, tau_relu: float,
+                          tau_max: float) -> tuple[Tensor, Tensor]:
+    """``forward`` plus the Jacobian (B, nc, n_sub, i, m) of every area with respect to
+    its subset's objective values."""
+    obj, cl, cu, (B, n_sub, isz, m, B_cells, nc) = _prepare(obj_subsets, cell_lower, cell_upper)
+    out = torch.empty(B, nc, n_sub, dtype=obj.dtype, device=obj.device)
+    jac = torch.empty(B, nc, n_sub, isz, m, dtype=obj.dtype, device=obj.device)
+    fn = (nat.lib().bgb_log_areas_forward_jac if obj.dtype == torch.float64
+          else nat.lib().bgb_log_areas_forward_jac_f32)
+    with torch.cuda.device(obj.device):
+        rc = fn(obj.data_ptr(), B, n_sub, isz, m, cl.data_ptr(), cu.data_ptr(), B_cells, nc,
+                float(tau_relu), float(tau_max), out.data_ptr(), jac.data_ptr(),
+                nat.stream_handle(obj.device))
+    nat.check(rc, "bgb_log_areas_forward_jac")
+    return out, jac
+
+
+def backward_from_jacobian(grad_output: Tensor, jac: Tensor) -> Tensor:
+    """Gradient w.r.t. obj_subsets (B, n_sub, i, m) from the Jacobian of
+    ``forward_with_jacobian``: sum over cells of grad_output x Jacobian."""
+    if jac.dim() != 5:
+        raise RuntimeError("fused log-areas: the Jacobian must be (B, num_cells, n_sub, i, m)")
+    B, nc, n_sub, isz, m = jac.shape
+    go = grad_output.contiguous()
+    if tuple(go.shape) != (B, nc, n_sub) or go.dtype != jac.dtype or go.device != jac.device:
+        raise RuntimeError("fused log-areas: grad_output must be (B, num_cells, n_sub) like the forward output")
+    jac = jac.contiguous()
+    g_obj = torch.empty(B, n_sub, isz, m, dtype=jac.dtype, device=jac.device)
+    fn = (nat.lib().bgb_log_areas_backward_jac if jac.dtype == torch.float64
+          else nat.lib().bgb_log_areas_backward_jac_f32)
+    with torch.cuda.device(jac.device):
+        rc = fn(go.data_ptr(), jac.data_ptr(), B, n_sub, isz, m, nc, g_obj.data_ptr(),
+                nat.stream_handle(jac.device))
+    nat.check(rc, "bgb_log_areas_backward_jac")
+    return g_obj
+
+
 class FusedLogAreas(torch.autograd.Function):
     """Autograd wrapper with the reference's ``_FusedLogAreas`` contract:
     ``obj_subsets`` (*batch, n_sub, i, m) and cell bounds (nc, m) or
@@ -99,8 +144,16 @@ class FusedLogAreas(torch.autograd.Function):
         if cell_lower.ndim > 2:
             cell_lower = cell_lower.reshape(-1, nc, m_cells)
             cell_upper = cell_upper.reshape(-1, nc, m_cells)
-        result = forward(obj_flat, cell_lower, cell_upper, tau_relu, tau_max)
-        ctx.save_for_backward(obj_flat, cell_lower, cell_upper)
+        n_sub, isz, m = obj_flat.shape[-3:]
+        jac_bytes = B * nc * n_sub * isz * m * obj_flat.element_size()
+        if ctx.needs_input_grad[0] and jac_bytes <= JACOBIAN_BUDGET_BYTES:
+            result, jac = forward_with_jacobian(obj_flat, cell_lower, cell_upper, tau_relu, tau_max)
+            ctx.save_for_backward(jac)
+            ctx.with_jacobian = True
+        else:
+            result = forward(obj_flat, cell_lower, cell_upper, tau_relu, tau_max)
+            ctx.save_for_backward(obj_flat, cell_lower, cell_upper)
+            ctx.with_jacobian = False
         ctx.tau_relu = tau_relu
         ctx.tau_max = tau_max
         ctx.orig_shape = obj_subsets.shape
@@ -108,6 +161,11 @@ class FusedLogAreas(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, grad_output: Tensor):
+        if ctx.with_jacobian:
+            (jac,) = ctx.saved_tensors
+            grad_flat = grad_output.reshape(jac.shape[0], *grad_output.shape[-2:])
+            grad_obj = backward_from_jacobian(grad_flat, jac)
+            return grad_obj.reshape(ctx.orig_shape), None, None, None, None
         obj_flat, cell_lower, cell_upper = ctx.saved_tensors
         B = obj_flat.shape[0]
         grad_flat = grad_output.reshape(B, *grad_output.shape[-2:])

@@ -353,6 +353,29 @@ int bgb_log_areas_backward_f32(const float* grad_out, const float* obj, int64_t 
                                const float* cell_upper, int64_t B_cells, int64_t nc,
                                double tau_relu, double tau_max, float* grad_obj, void* stream);
 
+/* Forward that also keeps the Jacobian of every area with respect to its
+ * subset's objective values, and the backward as a contraction with it (no
+ * counterpart in the reference, which recomputes in its backward; here the
+ * recomputation is FP64-bound and the contraction HBM-bound):
+ *   jac      (B, nc, n_sub, isz, m): d out[b][c][s] / d obj[b][s][j][k]
+ *   grad_obj[b][s][j][k] = sum_c grad_out[b][c][s] jac[b][c][s][j][k]
+ * out equals bgb_log_areas_forward's; grad_obj equals bgb_log_areas_backward's
+ * up to rounding. */
+int bgb_log_areas_forward_jac(const double* obj, int64_t B, int64_t n_sub, int64_t isz, int64_t m,
+                              const double* cell_lower, const double* cell_upper, int64_t B_cells,
+                              int64_t nc, double tau_relu, double tau_max, double* out,
+                              double* jac, void* stream);
+int bgb_log_areas_forward_jac_f32(const float* obj, int64_t B, int64_t n_sub, int64_t isz,
+                                  int64_t m, const float* cell_lower, const float* cell_upper,
+                                  int64_t B_cells, int64_t nc, double tau_relu, double tau_max,
+                                  float* out, float* jac, void* stream);
+int bgb_log_areas_backward_jac(const double* grad_out, const double* jac, int64_t B,
+                               int64_t n_sub, int64_t isz, int64_t m, int64_t nc,
+                               double* grad_obj, void* stream);
+int bgb_log_areas_backward_jac_f32(const float* grad_out, const float* jac, int64_t B,
+                                   int64_t n_sub, int64_t isz, int64_t m, int64_t nc,
+                                   float* grad_obj, void* stream);
+
 /* Number of kernel launches this library has issued in the process so far.
  * Measurement aid; no reference counterpart. */
 unsigned long long bgb_launch_count(void);

@@ -162,3 +162,44 @@ def test_benchmark_size_rows_against_oracle(cuda_lib, dtype):
         ev, eg = _exact(sub, cl, cu, gsub)
         _assert_close(v[rows.to(DEV)], rv, TOL[dtype], f"i={obj.shape[2]} value", ev)
         _assert_close(gr[rows.to(DEV)], rg, TOL[dtype], f"i={obj.shape[2]} grad", eg)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_jacobian_route_matches_recompute_route(cuda_lib, dtype):
+    """forward_with_jacobian's areas equal forward's, and the Jacobian contraction
+    equals the recomputing backward (float64 1e-12; float32 held to the float64
+    oracle as above)."""
+    g = torch.Generator().manual_seed(23)
+    for B, n_sub, isz, m, nc, batched in [(9, 4, 1, 2, 5, False), (7, 6, 2, 2, 40, True),
+                                          (4, 10, 5, 3, 3, False), (2, 1, 17, 2, 33, True),
+                                          (2, 1, 32, 8, 4, False)]:
+        obj, lo, up, go = _random_case(g, B, n_sub, isz, m, nc, batched, dtype)
+        od, ld, ud, gd = obj.to(DEV), lo.to(DEV), up.to(DEV), go.to(DEV)
+        v, jac = lf.forward_with_jacobian(od, ld, ud, 1e-6, 1e-2)
+        assert jac.shape == (B, nc, n_sub, isz, m)
+        v0 = lf.forward(od, ld, ud, 1e-6, 1e-2)
+        torch.testing.assert_close(v, v0, atol=0, rtol=1e-14 if dtype == torch.float64 else 1e-6)
+        gj = lf.backward_from_jacobian(gd, jac)
+        rg = ola.backward(go, obj, lo, up, 1e-6, 1e-2)
+        _, eg = _exact(obj, lo, up, go)
+        _assert_close(gj, rg, TOL[dtype], f"{dtype} B={B} i={isz} m={m} nc={nc} jacobian grad", eg)
+
+
+def test_autograd_routes(cuda_lib, monkeypatch):
+    """FusedLogAreas keeps the Jacobian when the input needs a gradient and it fits the
+    budget, and recomputes otherwise; both give the same gradient."""
+    g = torch.Generator().manual_seed(31)
+    obj, lo, up, _ = _random_case(g, 6, 6, 2, 2, 12, False, torch.float64)
+    w = torch.randn(6, 12, 6, generator=g, dtype=torch.float64).to(DEV)
+    grads = []
+    for budget in (lf.JACOBIAN_BUDGET_BYTES, 0):
+        monkeypatch.setattr(lf, "JACOBIAN_BUDGET_BYTES", budget)
+        x = obj.to(DEV).requires_grad_(True)
+        out = lf.FusedLogAreas.apply(x, lo.to(DEV), up.to(DEV), 1e-6, 1e-2)
+        assert out.grad_fn is not None
+        (out * w).sum().backward()
+        grads.append(x.grad.clone())
+    torch.testing.assert_close(grads[0], grads[1], atol=0, rtol=1e-12)
+    with torch.no_grad():  # no gradient wanted: the plain forward
+        v = lf.FusedLogAreas.apply(obj.to(DEV), lo.to(DEV), up.to(DEV), 1e-6, 1e-2)
+    torch.testing.assert_close(v, lf.forward(obj.to(DEV), lo.to(DEV), up.to(DEV), 1e-6, 1e-2), atol=0, rtol=0)
