@@ -107,10 +107,14 @@ template <typename T>
 __device__ __forceinline__ T la_pareto(T z) {
     return T(2) / (T(2) + T(2) * z + z * z);
 }
+// value and derivative from one reciprocal: 2 RN(1/d) is RN(2/d) exactly, so
+// the value is unchanged; the derivative moves by a few ulps
 template <typename T>
-__device__ __forceinline__ T la_pareto_deriv(T z) {
+__device__ __forceinline__ void la_pareto_vd(T z, T& val, T& deriv) {
     const T d = T(2) + T(2) * z + z * z;
-    return T(-2) * (T(2) + T(2) * z) / (d * d);
+    const T r = T(1) / d;
+    val = T(2) * r;
+    deriv = T(-2) * (T(2) + T(2) * z) * r * r;
 }
 
 // fatmin of two values and d/d(first)
@@ -124,14 +128,14 @@ __device__ __forceinline__ T la_fatmin2(T a, T b, T tau, T inv_tau, T* ga) {
     }
     const T other = a_min ? b : a;
     const T z = (other - mn) * inv_tau;
-    const T S = T(1) + la_pareto(z);  // pareto(0) = 1
-    if (ga) {
-        const T pd = la_pareto_deriv(z);
-        // sum of the derivatives (pareto'(0) = -1 for the minimum);
-        // d/d(min) = 1 + (S_pd - pareto'(0)) / S, d/d(other) = -pd / S
-        const T S_pd = T(-1) + pd;
-        *ga = a_min ? T(1) + (S_pd + T(1)) / S : -pd / S;
-    }
+    if (!ga) return mn - tau * LaMath<T>::log_(T(1) + la_pareto(z));  // pareto(0) = 1
+    T pv, pd;
+    la_pareto_vd(z, pv, pd);
+    const T S = T(1) + pv;
+    // sum of the derivatives (pareto'(0) = -1 for the minimum);
+    // d/d(min) = 1 + (S_pd - pareto'(0)) / S, d/d(other) = -pd / S
+    const T S_pd = T(-1) + pd;
+    *ga = a_min ? T(1) + (S_pd + T(1)) / S : -pd / S;
     return mn - tau * LaMath<T>::log_(S);
 }
 
@@ -234,19 +238,20 @@ __global__ void __launch_bounds__(kLaThreads) log_areas_forward_jac_kernel(
 #pragma unroll
                 for (int j = 0; j < IM; ++j) {
                     if (j < isz) {
-                        const T z = (li[j] - mn) * inv_max;
-                        S += la_pareto(z);
-                        li[j] = la_pareto_deriv(z);  // li[j] now holds pareto'(z_j)
+                        T pv;
+                        la_pareto_vd((li[j] - mn) * inv_max, pv, li[j]);  // li[j] <- pareto'(z_j)
+                        S += pv;
                         S_pd += li[j];
                     }
                 }
                 const T lim = mn - tau_max * LaMath<T>::log_(S);
                 T g2;
                 area += la_fatmin2(lim, lcl, tau_max, inv_max, &g2);
+                const T inv_S = T(1) / S;
 #pragma unroll
                 for (int j = 0; j < IM; ++j) {
                     if (j < isz) {
-                        const T w = j == ami ? T(1) + (S_pd + T(1)) / S : -li[j] / S;
+                        const T w = j == ami ? T(1) + (S_pd + T(1)) * inv_S : -li[j] * inv_S;
                         J[j * m + k] = g2 * w * lg[j];
                     }
                 }
@@ -273,6 +278,7 @@ __global__ void __launch_bounds__(kLaThreads) log_areas_backward_jac_kernel(
         const T* go = g_out + b * nc * n_sub + s;
         const int64_t cstride = n_sub * im;
         T acc = T(0);
+#pragma unroll 8
         for (int64_t c = 0; c < nc; ++c) acc = fma(go[c * n_sub], J[c * cstride], acc);
         g_obj[t] = acc;
     }
@@ -330,9 +336,9 @@ __global__ void __launch_bounds__(kLaThreads) log_areas_backward_kernel(
 #pragma unroll
                 for (int j = 0; j < IM; ++j) {
                     if (j < isz) {
-                        const T z = (li[j] - mn) * inv_max;
-                        S += la_pareto(z);
-                        li[j] = la_pareto_deriv(z);  // li[j] now holds pareto'(z_j)
+                        T pv;
+                        la_pareto_vd((li[j] - mn) * inv_max, pv, li[j]);  // li[j] <- pareto'(z_j)
+                        S += pv;
                         S_pd += li[j];
                     }
                 }
@@ -340,11 +346,12 @@ __global__ void __launch_bounds__(kLaThreads) log_areas_backward_kernel(
                 T g2;
                 la_fatmin2(lim, lcl, tau_max, inv_max, &g2);
                 const T gl = go * g2;
+                const T inv_S = T(1) / S;
 #pragma unroll
                 for (int j = 0; j < IM; ++j) {
                     if (j < isz) {
                         // pareto'(0) = -1
-                        const T w = j == ami ? T(1) + (S_pd + T(1)) / S : -li[j] / S;
+                        const T w = j == ami ? T(1) + (S_pd + T(1)) * inv_S : -li[j] * inv_S;
                         g[j] += gl * w * lg[j];
                     }
                 }
