@@ -9,12 +9,16 @@ argument meanings.
 * ``initialize_q_batch``: Boltzmann selection of restart points from the raw
   samples, keeping the best raw sample (botorch/optim/initializers.py:959-1042,
   botorch/utils/sampling.py:1084-1115).
-* ``gen_candidates_scipy``: L-BFGS-B on the restarts, aggregated into one
-  problem whose objective is minus the sum of the acquisition values (the
-  reference's aggregated mode, botorch/generation/gen.py:305-395). Each objective
-  call copies x to the device, evaluates value + gradient of every restart in
-  one call (a CUDA graph replay at fixed shape) and copies both back through
-  pinned host buffers (the f / grad wrapper of botorch/generation/gen.py:423-487).
+* ``gen_candidates_scipy``: L-BFGS-B on the restarts. By default, as the
+  reference's fast path (botorch/generation/gen.py:226-247 with
+  botorch/optim/batched_lbfgs_b.py), every restart runs its own L-BFGS-B on
+  minus its own value, with the objectives of all restarts evaluated in one
+  call per round; with ``use_parallel_mode=False`` the restarts are aggregated
+  into one problem whose objective is minus the sum of the values (the
+  reference's aggregated mode, gen.py:249-395). Each evaluation copies the
+  points to the device, evaluates value + gradient of every restart in one
+  call (a CUDA graph replay at fixed shape) and copies both back through
+  pinned host buffers (the f / grad wrapper of gen.py:423-487).
 * ``optimize_acqf``: raw samples -> restarts -> L-BFGS-B -> the best restart
   (botorch/optim/optimize.py:619, ``return_best_only=True``).
 """
@@ -113,11 +117,160 @@ class _Objective:
         return -float(self.host_v.numpy().sum()), -gn.astype(np.float64, copy=True)
 
 
+class _RestartRounds:
+    """Batched objective for restarts that each run their own L-BFGS-B.
+
+    Every restart's optimiser runs in its own host thread and hands its point
+    to ``evaluate``. The threads pass a baton, so that exactly one of them, or
+    the serving thread, runs at a time (no contention for the interpreter
+    lock): a restart that has handed in its point wakes the next restart
+    waiting for the last round's result (or starts the next thread that has
+    not begun); the last one wakes the serving thread (``serve``), which
+    evaluates all b points in one call (a CUDA graph replay at fixed shape,
+    through pinned buffers; only this thread touches the GPU) and wakes the
+    first restart. Rows of restarts that have finished keep their last point
+    and their values are ignored. The value of a t-batch does not depend on
+    the other rows, so each restart's path is that of its own run alone.
+    (The reference reaches the same per-restart semantics by stepping scipy's
+    internal L-BFGS-B routine for every restart in one loop,
+    botorch/optim/batched_lbfgs_b.py:169-636.)"""
+
+    def __init__(self, acqf, shape: tuple[int, int, int], use_graph: bool = True) -> None:
+        import collections
+        import threading
+
+        self.acqf = acqf
+        self.use_graph = use_graph
+        self.cuda = torch.device(acqf.device).type == "cuda"
+        b = shape[0]
+
+        def host(*sz):
+            t = torch.empty(sz, dtype=torch.float64)
+            return t.pin_memory() if self.cuda else t
+
+        self.host_x, self.host_v, self.host_g = host(*shape), host(b), host(*shape)
+        self.dev_x = torch.empty(shape, dtype=torch.float64, device=acqf.device)
+        self.sems = [threading.Semaphore(0) for _ in range(b)]
+        self.server = threading.Semaphore(0)
+        self.unstarted: collections.deque = collections.deque()
+        self.queue: collections.deque = collections.deque()
+        self.active = b
+        self.pending: list[int] = []
+        self.calls = 0
+        self.error: BaseException | None = None
+        self.fv = np.zeros(b)
+        self.fg = np.zeros((b, shape[1] * shape[2]))
+
+    def _next(self) -> None:
+        """Hand the baton on: a thread not yet started, else the next restart
+        waiting for its result, else the serving thread."""
+        if self.unstarted:
+            self.unstarted.popleft().start()
+        elif self.queue:
+            self.sems[self.queue.popleft()].release()
+        else:
+            self.server.release()
+
+    def _run(self) -> None:
+        """One batched evaluation (serving thread)."""
+        try:
+            self.dev_x.copy_(self.host_x, non_blocking=True)
+            if self.use_graph and self.cuda:
+                v, g = self.acqf.graphed_value_and_grad(self.dev_x, True)
+            else:
+                v, g = self.acqf.value_and_grad_raw(self.dev_x, True)
+            self.host_v.copy_(v, non_blocking=True)
+            self.host_g.copy_(g, non_blocking=True)
+            if self.cuda:
+                torch.cuda.current_stream(self.dev_x.device).synchronize()
+            self.fv = -self.host_v.numpy().copy()
+            self.fg = -self.host_g.numpy().reshape(self.fv.shape[0], -1).copy()
+            self.calls += 1
+        except BaseException as e:  # handed to every waiting restart
+            self.error = e
+
+    def serve(self, threads) -> None:
+        """Run the restart threads and evaluate rounds until all have finished."""
+        self.unstarted.extend(threads)
+        self._next()
+        while True:
+            self.server.acquire()
+            if self.active == 0:
+                return
+            # every running restart has handed in its point
+            self.queue.extend(self.pending)
+            self.pending = []
+            self._run()
+            self._next()
+
+    def evaluate(self, i: int, x: np.ndarray) -> tuple[float, np.ndarray]:
+        """Restart i's objective (its own thread, holding the baton)."""
+        if np.isnan(x).any():
+            raise RuntimeError(f"{int(np.isnan(x).sum())} elements of x are NaN")
+        if self.error is not None:
+            raise RuntimeError("batched acquisition evaluation failed") from self.error
+        self.host_x.numpy()[i].reshape(-1)[:] = x
+        self.pending.append(i)
+        self._next()
+        self.sems[i].acquire()
+        if self.error is not None:
+            raise RuntimeError("batched acquisition evaluation failed") from self.error
+        f, g = float(self.fv[i]), self.fg[i].copy()
+        if np.isnan(g).any():
+            raise RuntimeError(f"{int(np.isnan(g).sum())} elements of the gradient are NaN")
+        return f, g
+
+    def done(self, i: int) -> None:
+        """Restart i has finished (holding the baton): the rounds no longer wait for it."""
+        self.active -= 1
+        self._next()
+
+
+def _per_restart_lbfgsb(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape, maxiter: int,
+                        options: dict, use_graph: bool):
+    """Each restart's own L-BFGS-B (scipy, one host thread each), objectives batched
+    per round on the calling thread. Returns the scipy results and the rounds."""
+    import threading
+
+    from scipy.optimize import minimize
+
+    b, q, d = shape
+    rounds = _RestartRounds(acqf, shape, use_graph)
+    bounds = list(zip(np.tile(lo, q), np.tile(hi, q)))
+    results: list = [None] * b
+    errors: list = [None] * b
+
+    def run(i: int) -> None:
+        try:
+            results[i] = minimize(lambda x: rounds.evaluate(i, x), x0[i], method="L-BFGS-B", jac=True,
+                                  bounds=bounds, options={"maxiter": maxiter, **options})
+        except BaseException as e:
+            errors[i] = e
+        finally:
+            rounds.done(i)
+
+    threads = [threading.Thread(target=run, args=(i,), daemon=True) for i in range(b)]
+    rounds.serve(threads)
+    for t in threads:
+        t.join()
+    for e in errors:
+        if e is not None:
+            raise e
+    return results, rounds.calls
+
+
 def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower_bounds: float | Tensor,
                          upper_bounds: float | Tensor, options: dict | None = None,
-                         use_graph: bool = True) -> tuple[Tensor, Tensor]:
+                         use_graph: bool = True,
+                         use_parallel_mode: bool | None = None) -> tuple[Tensor, Tensor]:
     """L-BFGS-B from the ``b x q x d`` initial conditions on the box; returns the
-    candidates and their acquisition values."""
+    candidates and their acquisition values.
+
+    ``use_parallel_mode`` None or True (the reference's default fast path,
+    botorch/generation/gen.py:226-247): every restart runs its own L-BFGS-B on
+    minus its own value, with one batched evaluation per round. False: one
+    L-BFGS-B on minus the sum of all restarts' values (the reference's
+    aggregated mode, gen.py:249-395)."""
     from scipy.optimize import minimize
 
     options = dict(options or {})
@@ -127,6 +280,20 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
     lo = torch.as_tensor(lower_bounds, dtype=torch.float64).expand(d).cpu().numpy()
     hi = torch.as_tensor(upper_bounds, dtype=torch.float64).expand(d).cpu().numpy()
     x0 = np.clip(X0.cpu().numpy(), lo, hi).reshape(-1)
+    if use_parallel_mode is not False:
+        v0, _ = acquisition_function.value_and_grad_raw(
+            torch.from_numpy(x0.reshape(b, q, d)).to(acquisition_function.device), False)
+        f0 = -float(v0.sum())
+        results, calls = _per_restart_lbfgsb(acquisition_function, x0.reshape(b, -1), lo, hi, (b, q, d),
+                                             maxiter, options, use_graph)
+        xs = np.stack([r.x for r in results]).reshape(b, q, d)
+        X = torch.from_numpy(np.clip(xs, lo, hi)).to(acquisition_function.device)
+        v, _ = acquisition_function.value_and_grad_raw(X.contiguous(), False)
+        info = {"mode": "per-restart", "nit": max(int(r.nit) for r in results), "nfev": int(calls),
+                "nit_per_restart": [int(r.nit) for r in results],
+                "message": str(results[0].message), "f0": f0, "f": -float(v.sum())}
+        gen_candidates_scipy.last_info = info
+        return X, v.clone()
     bounds = list(zip(np.tile(lo, b * q), np.tile(hi, b * q)))
     obj = _Objective(acquisition_function, (b, q, d), use_graph)
     f0 = obj(x0)[0]
@@ -134,7 +301,7 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
                    options={"maxiter": maxiter, **options})
     X = torch.from_numpy(np.clip(res.x.reshape(b, q, d), lo, hi)).to(acquisition_function.device)
     v, _ = acquisition_function.value_and_grad_raw(X.contiguous(), False)
-    info = {"nit": int(res.nit), "nfev": int(obj.calls), "message": str(res.message),
+    info = {"mode": "aggregated", "nit": int(res.nit), "nfev": int(obj.calls), "message": str(res.message),
             "f0": f0, "f": float(res.fun)}
     gen_candidates_scipy.last_info = info
     return X, v.clone()
@@ -142,7 +309,7 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
 
 def optimize_acqf(acq_function, bounds: Tensor, q: int, num_restarts: int, raw_samples: int,
                   options: dict | None = None, seed: int | None = None,
-                  use_graph: bool = True) -> tuple[Tensor, Tensor]:
+                  use_graph: bool = True, use_parallel_mode: bool | None = None) -> tuple[Tensor, Tensor]:
     """Raw samples -> Boltzmann-selected restarts -> L-BFGS-B -> the best restart.
 
     options: ``batch_limit`` (raw-sample evaluation chunk, 4096), ``eta`` (1.0),
@@ -155,6 +322,7 @@ def optimize_acqf(acq_function, bounds: Tensor, q: int, num_restarts: int, raw_s
     v_raw = evaluate_raw(acq_function, X_raw, batch_limit)
     g = None if seed is None else torch.Generator(device=v_raw.device).manual_seed(seed)
     X0, _ = initialize_q_batch(X_raw.to(v_raw.device), v_raw, num_restarts, eta=eta, generator=g)
-    X, v = gen_candidates_scipy(X0, acq_function, bounds[0], bounds[1], options, use_graph)
+    X, v = gen_candidates_scipy(X0, acq_function, bounds[0], bounds[1], options, use_graph,
+                                use_parallel_mode)
     best = int(torch.argmax(v))
     return X[best], v[best]

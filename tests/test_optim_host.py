@@ -40,3 +40,62 @@ def test_initialize_q_batch_edge_cases():
     v = torch.tensor([0.0] * 7 + [1e6], dtype=torch.float64)
     Xs, vs = initialize_q_batch(X, v, 2, eta=1e4)
     assert float(vs.max()) == 1e6
+
+
+class _FakeAcqf:
+    """Independent concave objectives per t-batch on the CPU:
+    value_i = -sum (w_i (X_i - c)^2 + (X_i - c)^4), w_i anisotropic and uneven."""
+
+    device = torch.device("cpu")
+
+    def __init__(self, b, q, d, fail_at=None):
+        g = torch.Generator().manual_seed(4)
+        self.w = 0.5 + 20 * torch.rand(b, q, d, generator=g, dtype=torch.float64) ** 3
+        self.c = 0.2 + 0.6 * torch.rand(1, q, d, generator=g, dtype=torch.float64)
+        self.calls = 0
+        self.fail_at = fail_at
+
+    def value_and_grad_raw(self, X, need_grad, **kw):
+        self.calls += 1
+        if self.fail_at is not None and self.calls >= self.fail_at:
+            raise ValueError("planted failure")
+        return self.rows(X, self.w[:X.shape[0]], need_grad)
+
+    def rows(self, X, w, need_grad):
+        r = X - self.c
+        return -(w * r * r + r ** 4).sum((1, 2)), (-(2 * w * r + 4 * r ** 3) if need_grad else None)
+
+
+def test_per_restart_mode_equals_independent_runs():
+    """Each restart's own L-BFGS-B with batched rounds gives exactly the result of
+    running scipy on that restart alone (the rows do not interact)."""
+    import numpy as np
+    from scipy.optimize import minimize
+
+    from botorch_gb300.optim import gen_candidates_scipy
+
+    b, q, d = 7, 2, 3
+    acqf = _FakeAcqf(b, q, d)
+    X0 = torch.rand(b, q, d, generator=torch.Generator().manual_seed(9), dtype=torch.float64)
+    X, v = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 50})
+    info = gen_candidates_scipy.last_info
+    assert info["mode"] == "per-restart" and len(set(info["nit_per_restart"])) > 1
+    for i in range(b):
+        def f(x, i=i):  # restart i alone
+            vv, gg = acqf.rows(torch.from_numpy(x.reshape(1, q, d)), acqf.w[i:i + 1], True)
+            return -float(vv[0]), -gg.numpy().reshape(-1)
+        res = minimize(f, X0[i].numpy().reshape(-1), method="L-BFGS-B", jac=True,
+                       bounds=[(0.0, 1.0)] * (q * d), options={"maxiter": 50})
+        assert np.array_equal(res.x, X[i].numpy().reshape(-1)), i
+    assert torch.allclose(X, acqf.c.expand(b, q, d), atol=1e-3)
+    assert info["nfev"] >= max(info["nit_per_restart"])  # one round per evaluation of the slowest restart
+
+
+@pytest.mark.timeout(60)
+def test_per_restart_mode_raises_without_hanging():
+    from botorch_gb300.optim import gen_candidates_scipy
+
+    acqf = _FakeAcqf(5, 2, 2, fail_at=4)
+    X0 = torch.rand(5, 2, 2, dtype=torch.float64)
+    with pytest.raises(RuntimeError, match="batched acquisition evaluation failed"):
+        gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 50})
