@@ -253,7 +253,7 @@ __device__ __forceinline__ void add_pair(T& h, T& l, T bh, T bl) {
     l = l + bl + e;
 }
 
-constexpr int kQstatsThreads = 256;
+constexpr int kQstatsThreads = 128;  // 8 columns of 4 per thread at n = 4096: the tail reduction is paid per 128 threads
 
 // outputscale * kappa between row `ri` of X and row `rj` of X (rj >= 0) or
 // baseline point `kb` (rj < 0). Float path (T = float with a.zt set): float32
