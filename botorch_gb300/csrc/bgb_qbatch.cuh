@@ -59,7 +59,7 @@ int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta,
 template <typename T>
 int launch_sigma_reduce(const QBatchArgs& a, const T* P, const T* C, int64_t ldc,
                         cudaStream_t stream);
-// mixed: float32 evaluation of the per-sample smooth reductions (see qbatch.cu)
+// mixed: float32 evaluation of the per-sample smooth reductions (see qbatch_impl.cuh)
 int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bool mixed = false);
 size_t batch_step_smem_bytes(int q, int r, int S);
 // H (b*q x n) = gmu beta^T - 2 Gqq V - Gqb Vb per t-batch
