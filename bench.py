@@ -528,9 +528,10 @@ def run_optimize(args) -> None:
     info = gen_candidates_scipy.last_info
     v64, _ = acqfs["fp64"].value_and_grad_raw(X.contiguous(), False)
     err = float((v - v64).norm() / v64.norm())
-    # the reference's other mode on the same restarts: one L-BFGS-B on the summed objective
+    # the reference's other mode on the same restarts: each restart its own L-BFGS-B,
+    # one batched evaluation per round (host threads; cost varies with the host)
     t4 = time.perf_counter()
-    _, va = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": args.maxiter}, use_parallel_mode=False)
+    _, va = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": args.maxiter}, use_parallel_mode=True)
     torch.cuda.synchronize(device)
     t5 = time.perf_counter()
     info_a = gen_candidates_scipy.last_info
@@ -551,9 +552,10 @@ def run_optimize(args) -> None:
         "best_value": float(v.max()), "best_value_raw": float(v_raw.max()),
         "final_values_rel_err_vs_fp64": err, "init_s": round(init_s, 2),
         "launches_per_objective_evaluation": acqf.graph_launches(restarts, q),
-        "aggregated_mode": {"lbfgsb_s": round(t5 - t4, 4), "iterations": info_a["nit"],
-                            "objective_evaluations": info_a["nfev"], "restart_sum_final": float(va.sum()),
-                            "best_value": float(va.max())},
+        "per_restart_mode": {"lbfgsb_s": round(t5 - t4, 4), "iterations": info_a["nit"],
+                             "rounds": info_a["nfev"],
+                             "ms_per_round": round(1e3 * (t5 - t4) / max(info_a["nfev"], 1), 3),
+                             "restart_sum_final": float(va.sum()), "best_value": float(va.max())},
     }
     print(json.dumps(line), flush=True)
 

@@ -9,13 +9,17 @@ argument meanings.
 * ``initialize_q_batch``: Boltzmann selection of restart points from the raw
   samples, keeping the best raw sample (botorch/optim/initializers.py:959-1042,
   botorch/utils/sampling.py:1084-1115).
-* ``gen_candidates_scipy``: L-BFGS-B on the restarts. By default, as the
-  reference's fast path (botorch/generation/gen.py:226-247 with
-  botorch/optim/batched_lbfgs_b.py), every restart runs its own L-BFGS-B on
-  minus its own value, with the objectives of all restarts evaluated in one
-  call per round; with ``use_parallel_mode=False`` the restarts are aggregated
-  into one problem whose objective is minus the sum of the values (the
-  reference's aggregated mode, gen.py:249-395). Each evaluation copies the
+* ``gen_candidates_scipy``: L-BFGS-B on the restarts, in either of the
+  reference's two modes. By default the restarts are aggregated into one
+  problem whose objective is minus the sum of the values (the reference's
+  aggregated mode, gen.py:249-395). With ``use_parallel_mode=True`` every
+  restart runs its own L-BFGS-B on minus its own value, with the objectives
+  of all restarts evaluated in one call per round (the reference's fast
+  path, botorch/generation/gen.py:226-247 with botorch/optim/batched_lbfgs_b.py,
+  which the reference takes by default). Here that mode runs one scipy
+  optimiser per restart in its own host thread, and its cost per round
+  depends on the host's thread wake-up latency (15 ms and 130 ms per round of
+  64 restarts on two GPU hosts, same results), so it is not the default. Each evaluation copies the
   points to the device, evaluates value + gradient of every restart in one
   call (a CUDA graph replay at fixed shape) and copies both back through
   pinned host buffers (the f / grad wrapper of gen.py:423-487).
@@ -266,11 +270,11 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
     """L-BFGS-B from the ``b x q x d`` initial conditions on the box; returns the
     candidates and their acquisition values.
 
-    ``use_parallel_mode`` None or True (the reference's default fast path,
+    ``use_parallel_mode`` True (the reference's fast path,
     botorch/generation/gen.py:226-247): every restart runs its own L-BFGS-B on
-    minus its own value, with one batched evaluation per round. False: one
-    L-BFGS-B on minus the sum of all restarts' values (the reference's
-    aggregated mode, gen.py:249-395)."""
+    minus its own value, with one batched evaluation per round. None or False
+    (the default here): one L-BFGS-B on minus the sum of all restarts' values
+    (the reference's aggregated mode, gen.py:249-395)."""
     from scipy.optimize import minimize
 
     options = dict(options or {})
@@ -280,7 +284,7 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
     lo = torch.as_tensor(lower_bounds, dtype=torch.float64).expand(d).cpu().numpy()
     hi = torch.as_tensor(upper_bounds, dtype=torch.float64).expand(d).cpu().numpy()
     x0 = np.clip(X0.cpu().numpy(), lo, hi).reshape(-1)
-    if use_parallel_mode is not False:
+    if use_parallel_mode:
         v0, _ = acquisition_function.value_and_grad_raw(
             torch.from_numpy(x0.reshape(b, q, d)).to(acquisition_function.device), False)
         f0 = -float(v0.sum())

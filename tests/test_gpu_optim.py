@@ -40,8 +40,9 @@ def test_optimize_acqf_improves_and_agrees_with_fp64(cuda_lib):
 
 
 def test_per_restart_and_aggregated_modes(cuda_lib):
-    """The reference's default per-restart mode: every restart's own value does not
-    decrease; the aggregated mode decreases the summed objective; both stay in the box."""
+    """The per-restart mode (the reference's fast path): every restart's own value does
+    not decrease; the aggregated mode (the default here) decreases the summed
+    objective; both stay in the box."""
     w = T.qlognei_diff(b=1, q=2, n=128)
     gm = gpu_model(w)
     acqf = _acqf(gm, w, "mixed")
@@ -49,11 +50,11 @@ def test_per_restart_and_aggregated_modes(cuda_lib):
     X0 = draw_sobol_samples(torch.stack([torch.zeros(d), torch.ones(d)]).double(), 6, 2, seed=1).to(DEV)
     v0, _ = acqf.value_and_grad_raw(X0.contiguous(), False)
     v0 = v0.clone()
-    X, v = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 20})
+    X, v = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 20}, use_parallel_mode=True)
     info = gen_candidates_scipy.last_info
     assert info["mode"] == "per-restart" and len(info["nit_per_restart"]) == 6
     assert bool((v >= v0 - 1e-9).all()), (v, v0)
     assert bool(((X >= 0) & (X <= 1)).all())
-    Xa, va = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 20}, use_parallel_mode=False)
+    Xa, va = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 20})
     assert gen_candidates_scipy.last_info["mode"] == "aggregated"
     assert float(va.sum()) >= float(v0.sum()) - 1e-9

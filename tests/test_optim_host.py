@@ -77,7 +77,7 @@ def test_per_restart_mode_equals_independent_runs():
     b, q, d = 7, 2, 3
     acqf = _FakeAcqf(b, q, d)
     X0 = torch.rand(b, q, d, generator=torch.Generator().manual_seed(9), dtype=torch.float64)
-    X, v = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 50})
+    X, v = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 50}, use_parallel_mode=True)
     info = gen_candidates_scipy.last_info
     assert info["mode"] == "per-restart" and len(set(info["nit_per_restart"])) > 1
     for i in range(b):
@@ -98,4 +98,4 @@ def test_per_restart_mode_raises_without_hanging():
     acqf = _FakeAcqf(5, 2, 2, fail_at=4)
     X0 = torch.rand(5, 2, 2, dtype=torch.float64)
     with pytest.raises(RuntimeError, match="batched acquisition evaluation failed"):
-        gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 50})
+        gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 50}, use_parallel_mode=True)
