@@ -16,13 +16,19 @@ argument meanings.
   restart runs its own L-BFGS-B on minus its own value, with the objectives
   of all restarts evaluated in one call per round (the reference's fast
   path, botorch/generation/gen.py:226-247 with botorch/optim/batched_lbfgs_b.py,
-  which the reference takes by default). Here that mode runs one scipy
-  optimiser per restart in its own host thread, and its cost per round
-  depends on the host's thread wake-up latency (15 ms and 130 ms per round of
-  64 restarts on two GPU hosts, same results), so it is not the default. Each evaluation copies the
-  points to the device, evaluates value + gradient of every restart in one
-  call (a CUDA graph replay at fixed shape) and copies both back through
-  pinned host buffers (the f / grad wrapper of gen.py:423-487).
+  which the reference takes by default). That mode steps scipy's
+  reverse-communication L-BFGS-B routine for every restart on the calling
+  thread, as the reference does, where the installed scipy has the interface
+  this driver follows (>= 1.15) and reproduces scipy's own ``minimize`` bit
+  for bit in a self-test; otherwise it runs one scipy optimiser per restart
+  in its own host thread, whose cost per round depends on the host's thread
+  wake-up latency (15 ms and 130 ms per round of 64 restarts on two GPU
+  hosts, same results). Either way its host cost is one L-BFGS-B step per
+  restart per round, so the aggregated mode stays the default. Each
+  evaluation copies the points to the device, evaluates value + gradient of
+  every restart in one call (a CUDA graph replay at fixed shape) and copies
+  both back through pinned host buffers (the f / grad wrapper of
+  gen.py:423-487).
 * ``optimize_acqf``: raw samples -> restarts -> L-BFGS-B -> the best restart
   (botorch/optim/optimize.py:619, ``return_best_only=True``).
 """
@@ -230,6 +236,142 @@ class _RestartRounds:
         self._next()
 
 
+class _RCRestart:
+    """One restart's L-BFGS-B state for scipy's reverse-communication routine
+    ``setulb`` (scipy >= 1.15), advanced exactly as scipy's own driver loop
+    advances it (scipy.optimize._lbfgsb_py._minimize_lbfgsb): task 3 asks for
+    f and g at x, task 1 starts a new iteration, anything else stops."""
+
+    def __init__(self, setulb, int_dtype, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, opts: dict):
+        n = x0.size
+        self.setulb = setulb
+        self.m = int(opts.get("maxcor", 10))
+        self.factr = float(opts.get("ftol", 2.2204460492503131e-09)) / np.finfo(float).eps
+        self.pgtol = float(opts.get("gtol", 1e-5))
+        self.maxls = int(opts.get("maxls", 20))
+        self.maxiter = int(opts.get("maxiter", 15000))
+        self.maxfun = int(opts.get("maxfun", 15000))
+        self.nbd = np.zeros(n, dtype=int_dtype)
+        self.low = np.zeros(n, dtype=np.float64)
+        self.up = np.zeros(n, dtype=np.float64)
+        for i in range(n):  # scipy's bound codes: 0 none, 1 lower, 2 both, 3 upper
+            has_lo, has_up = not np.isinf(lo[i]), not np.isinf(hi[i])
+            if has_lo:
+                self.low[i] = lo[i]
+            if has_up:
+                self.up[i] = hi[i]
+            self.nbd[i] = {(False, False): 0, (True, False): 1, (True, True): 2, (False, True): 3}[has_lo, has_up]
+        self.x = np.clip(np.asarray(x0, dtype=np.float64), lo, hi)
+        self.f = np.array(0.0, dtype=np.float64)
+        self.g = np.zeros(n, dtype=np.float64)
+        m = self.m
+        self.wa = np.zeros(2 * m * n + 5 * n + 11 * m * m + 8 * m, np.float64)
+        self.iwa = np.zeros(3 * n, dtype=int_dtype)
+        self.task = np.zeros(2, dtype=int_dtype)
+        self.ln_task = np.zeros(2, dtype=int_dtype)
+        self.lsave = np.zeros(4, dtype=int_dtype)
+        self.isave = np.zeros(44, dtype=int_dtype)
+        self.dsave = np.zeros(29, dtype=np.float64)
+        self.nit = 0
+        self.nfev = 0
+
+    def advance(self) -> bool:
+        """Run the routine until it asks for f and g (True) or stops (False)."""
+        while True:
+            self.g = self.g.astype(np.float64)
+            self.setulb(self.m, self.x, self.low, self.up, self.nbd, self.f, self.g, self.factr,
+                        self.pgtol, self.wa, self.iwa, self.task, self.lsave, self.isave, self.dsave,
+                        self.maxls, self.ln_task)
+            if self.task[0] == 3:
+                return True
+            if self.task[0] == 1:
+                self.nit += 1
+                if self.nit >= self.maxiter:
+                    self.task[0], self.task[1] = 5, 504
+                elif self.nfev > self.maxfun:
+                    self.task[0], self.task[1] = 5, 502
+            else:
+                return False
+
+    def result(self) -> dict:
+        from scipy.optimize import _lbfgsb_py
+
+        msg = (_lbfgsb_py.status_messages[int(self.task[0])] + ": "
+               + _lbfgsb_py.task_messages[int(self.task[1])])
+        return {"x": self.x.copy(), "fun": float(self.f), "nit": self.nit, "nfev": self.nfev, "message": msg}
+
+
+_RC = {}
+
+
+def _lbfgsb_rc():
+    """(setulb, int dtype) of scipy's reverse-communication L-BFGS-B when it is the
+    interface this driver follows (scipy >= 1.15) and reproduces scipy's own
+    ``minimize`` bit for bit on a small bounded problem; else None (the per-restart
+    mode then runs one scipy optimiser per host thread)."""
+    if "rc" in _RC:
+        return _RC["rc"]
+    rc = None
+    try:
+        import scipy
+        from scipy.optimize import _lbfgsb, _lbfgsb_py, minimize
+
+        major, minor = (int(v) for v in scipy.__version__.split(".")[:2])
+        if (major, minor) >= (1, 15) and hasattr(_lbfgsb_py, "HAS_ILP64"):
+            cand = (_lbfgsb.setulb, np.int64 if _lbfgsb_py.HAS_ILP64 else np.int32)
+            w = np.array([3.0, 0.5, 7.0, 1.5])
+            c = np.array([0.3, 1.2, -0.4, 0.8])
+
+            def fg(x):
+                r = x - c
+                return float(np.sum(w * r * r + r ** 4)), 2 * w * r + 4 * r ** 3
+
+            lo, hi = np.array([0.0, 0.0, -1.0, 0.0]), np.array([1.0, 1.0, 1.0, 0.5])
+            x0 = np.array([0.9, 0.1, 0.5, 0.2])
+            ref = minimize(fg, x0, method="L-BFGS-B", jac=True, bounds=list(zip(lo, hi)),
+                           options={"maxiter": 30})
+            st = _RCRestart(*cand, x0, lo, hi, {"maxiter": 30})
+            while st.advance():
+                st.f, st.g = fg(st.x)
+                st.nfev += 1
+            if np.array_equal(st.x, ref.x) and st.nit == ref.nit:
+                rc = cand
+    except Exception:
+        rc = None
+    _RC["rc"] = rc
+    return rc
+
+
+def _per_restart_rc(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape, maxiter: int,
+                    options: dict, use_graph: bool, rc):
+    """Each restart's own L-BFGS-B through scipy's reverse-communication routine, all
+    restarts that need f and g evaluated in one call per round, on this thread (the
+    reference's batched driver, botorch/optim/batched_lbfgs_b.py:169-636, does the
+    same). Returns per-restart results and the rounds."""
+    b, q, d = shape
+    lo_r, hi_r = np.tile(lo, q), np.tile(hi, q)
+    opts = {**options, "maxiter": maxiter}
+    states = [_RCRestart(*rc, x0[i], lo_r, hi_r, opts) for i in range(b)]
+    rounds = _RestartRounds(acqf, shape, use_graph)
+    active = [i for i in range(b) if states[i].advance()]
+    while active:
+        for i in active:
+            if np.isnan(states[i].x).any():
+                raise RuntimeError(f"{int(np.isnan(states[i].x).sum())} elements of x are NaN")
+            rounds.host_x.numpy()[i].reshape(-1)[:] = states[i].x
+        rounds._run()
+        if rounds.error is not None:
+            raise RuntimeError("batched acquisition evaluation failed") from rounds.error
+        for i in active:
+            g = rounds.fg[i].copy()
+            if np.isnan(g).any():
+                raise RuntimeError(f"{int(np.isnan(g).sum())} elements of the gradient are NaN")
+            states[i].f, states[i].g = float(rounds.fv[i]), g
+            states[i].nfev += 1
+        active = [i for i in active if states[i].advance()]
+    return [s.result() for s in states], rounds.calls
+
+
 def _per_restart_lbfgsb(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape, maxiter: int,
                         options: dict, use_graph: bool):
     """Each restart's own L-BFGS-B (scipy, one host thread each), objectives batched
@@ -288,14 +430,20 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
         v0, _ = acquisition_function.value_and_grad_raw(
             torch.from_numpy(x0.reshape(b, q, d)).to(acquisition_function.device), False)
         f0 = -float(v0.sum())
-        results, calls = _per_restart_lbfgsb(acquisition_function, x0.reshape(b, -1), lo, hi, (b, q, d),
-                                             maxiter, options, use_graph)
-        xs = np.stack([r.x for r in results]).reshape(b, q, d)
+        rc = _lbfgsb_rc()
+        if rc is not None:
+            results, calls = _per_restart_rc(acquisition_function, x0.reshape(b, -1), lo, hi, (b, q, d),
+                                             maxiter, options, use_graph, rc)
+        else:
+            results, calls = _per_restart_lbfgsb(acquisition_function, x0.reshape(b, -1), lo, hi,
+                                                 (b, q, d), maxiter, options, use_graph)
+        xs = np.stack([r["x"] for r in results]).reshape(b, q, d)
         X = torch.from_numpy(np.clip(xs, lo, hi)).to(acquisition_function.device)
         v, _ = acquisition_function.value_and_grad_raw(X.contiguous(), False)
-        info = {"mode": "per-restart", "nit": max(int(r.nit) for r in results), "nfev": int(calls),
-                "nit_per_restart": [int(r.nit) for r in results],
-                "message": str(results[0].message), "f0": f0, "f": -float(v.sum())}
+        info = {"mode": "per-restart", "driver": "reverse communication" if rc is not None else "threads",
+                "nit": max(int(r["nit"]) for r in results), "nfev": int(calls),
+                "nit_per_restart": [int(r["nit"]) for r in results],
+                "message": str(results[0]["message"]), "f0": f0, "f": -float(v.sum())}
         gen_candidates_scipy.last_info = info
         return X, v.clone()
     bounds = list(zip(np.tile(lo, b * q), np.tile(hi, b * q)))

@@ -99,3 +99,35 @@ def test_per_restart_mode_raises_without_hanging():
     X0 = torch.rand(5, 2, 2, dtype=torch.float64)
     with pytest.raises(RuntimeError, match="batched acquisition evaluation failed"):
         gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 50}, use_parallel_mode=True)
+
+
+@pytest.mark.timeout(120)
+def test_per_restart_drivers_agree(monkeypatch):
+    """scipy's reverse-communication routine stepped per restart (used where it passes
+    its self-test) and one scipy optimiser per host thread (the fallback) give the
+    same restarts bit for bit."""
+    import numpy as np
+
+    import botorch_gb300.optim as O
+
+    b, q, d = 6, 2, 3
+    X0 = torch.rand(b, q, d, generator=torch.Generator().manual_seed(13), dtype=torch.float64)
+    X_rc, _ = O.gen_candidates_scipy(X0, _FakeAcqf(b, q, d), 0.0, 1.0, {"maxiter": 40}, use_parallel_mode=True)
+    info_rc = O.gen_candidates_scipy.last_info
+    monkeypatch.setattr(O, "_lbfgsb_rc", lambda: None)
+    X_th, _ = O.gen_candidates_scipy(X0, _FakeAcqf(b, q, d), 0.0, 1.0, {"maxiter": 40}, use_parallel_mode=True)
+    info_th = O.gen_candidates_scipy.last_info
+    assert info_th["driver"] == "threads"
+    if info_rc["driver"] == "reverse communication":
+        assert np.array_equal(X_rc.numpy(), X_th.numpy())
+        assert info_rc["nit_per_restart"] == info_th["nit_per_restart"] and info_rc["nfev"] == info_th["nfev"]
+
+
+@pytest.mark.timeout(60)
+def test_per_restart_thread_driver_raises_without_hanging(monkeypatch):
+    import botorch_gb300.optim as O
+
+    monkeypatch.setattr(O, "_lbfgsb_rc", lambda: None)
+    with pytest.raises(RuntimeError, match="batched acquisition evaluation failed"):
+        O.gen_candidates_scipy(torch.rand(5, 2, 2, dtype=torch.float64), _FakeAcqf(5, 2, 2, fail_at=4), 0.0, 1.0,
+                               {"maxiter": 50}, use_parallel_mode=True)
