@@ -552,7 +552,8 @@ def run_optimize(args) -> None:
         "best_value": float(v.max()), "best_value_raw": float(v_raw.max()),
         "final_values_rel_err_vs_fp64": err, "init_s": round(init_s, 2),
         "launches_per_objective_evaluation": acqf.graph_launches(restarts, q),
-        "per_restart_mode": {"lbfgsb_s": round(t5 - t4, 4), "iterations": info_a["nit"],
+        "per_restart_mode": {"driver": info_a.get("driver"), "lbfgsb_s": round(t5 - t4, 4),
+                             "iterations": info_a["nit"],
                              "rounds": info_a["nfev"],
                              "ms_per_round": round(1e3 * (t5 - t4) / max(info_a["nfev"], 1), 3),
                              "restart_sum_final": float(va.sum()), "best_value": float(va.max())},
