@@ -3,6 +3,7 @@
 reference checkout is present), against the reference's unfused Python path,
 and the host-side argument checks of botorch_gb300.logei_fused (no GPU)."""
 
+import math
 from pathlib import Path
 
 import numpy as np
@@ -108,3 +109,22 @@ def test_host_argument_checks_without_gpu():
         lf.forward(obj, cells, cells, 1e-6, 1e-2)
     with pytest.raises(RuntimeError, match="CUDA tensors"):
         lf.backward(torch.zeros(2, 4, 3, dtype=torch.float64), obj, cells, cells, 1e-6, 1e-2)
+
+
+def test_log_areas_workload_is_well_formed():
+    """The benchmark workload: q-subsets of each size are the combinations of the q
+    objective samples, cells are non-empty boxes above the front, the outer ones
+    unbounded above."""
+    import itertools
+
+    from botorch_gb300.testing import log_areas_workload
+
+    w = log_areas_workload(mc=2, restarts=3)
+    assert w.B == 6 and w.nc == 64 and len(w.obj_subsets) == w.q == 4
+    assert w.areas_per_step() == 6 * 64 * sum(math.comb(4, i) for i in range(1, 5))
+    for i, o in enumerate(w.obj_subsets, start=1):
+        combos = list(itertools.combinations(range(4), i))
+        assert o.shape == (6, len(combos), i, 2)
+        assert torch.equal(o[:, 0, 0], w.obj_subsets[0][:, combos[0][0], 0])  # first element of the first subset
+    assert bool((w.cell_upper > w.cell_lower).all())
+    assert bool(torch.isinf(w.cell_upper[:, 1]).all()) and bool(torch.isinf(w.cell_upper[-1, 0]))
