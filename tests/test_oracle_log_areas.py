@@ -128,3 +128,31 @@ def test_log_areas_workload_is_well_formed():
         assert torch.equal(o[:, 0, 0], w.obj_subsets[0][:, combos[0][0], 0])  # first element of the first subset
     assert bool((w.cell_upper > w.cell_lower).all())
     assert bool(torch.isinf(w.cell_upper[:, 1]).all()) and bool(torch.isinf(w.cell_upper[-1, 0]))
+
+
+def test_fused_log_areas_host_reshaping(monkeypatch):
+    """FusedLogAreas's batch flattening, batched-cell reshape and gradient routing,
+    with the C oracle standing in for the kernels (recompute route), against
+    autograd through the reference's unfused steps."""
+    from botorch_gb300 import logei_fused as lf
+
+    monkeypatch.setattr(lf, "JACOBIAN_BUDGET_BYTES", 0)
+    monkeypatch.setattr(lf, "forward", lambda o, cl, cu, tr, tm: ola.forward(o, cl, cu, tr, tm))
+    monkeypatch.setattr(lf, "backward", lambda go, o, cl, cu, tr, tm: ola.backward(go, o, cl, cu, tr, tm))
+    g = torch.Generator().manual_seed(8)
+    obj = torch.randn(4, 3, 6, 2, 2, generator=g, dtype=torch.float64)   # (mc, batch, n_sub, i, m)
+    lo = torch.randn(4, 3, 7, 2, generator=g, dtype=torch.float64) - 0.5  # batched cells
+    up = lo + 1.0
+    w = torch.randn(4, 3, 7, 6, generator=g, dtype=torch.float64)
+    for cells in ((lo, up), (lo[0, 0], up[0, 0])):                       # batched and shared cells
+        x = obj.clone().requires_grad_(True)
+        out = lf.FusedLogAreas.apply(x, cells[0], cells[1], 1e-6, 1e-2)
+        assert out.shape == (4, 3, 7, 6)
+        (out * w).sum().backward()
+        xr = obj.clone().requires_grad_(True)
+        cl = cells[0].reshape(-1, 7, 2) if cells[0].dim() > 2 else cells[0]
+        cu = cells[1].reshape(-1, 7, 2) if cells[1].dim() > 2 else cells[1]
+        ref = ola.python_path_log_areas(xr.reshape(12, 6, 2, 2), cl, cu, 1e-6, 1e-2).reshape(4, 3, 7, 6)
+        (ref * w).sum().backward()
+        torch.testing.assert_close(out.detach(), ref.detach(), atol=1e-6, rtol=1e-6)
+        torch.testing.assert_close(x.grad, xr.grad, atol=1e-6, rtol=1e-6)
