@@ -354,18 +354,16 @@ def run_ours(args) -> None:
         torch.distributed.destroy_process_group()
         return
 
-    # plain float64 GPU path (the denominator of the headline target), smaller b
+    # plain float64 GPU path (the denominator of the headline target): the same
+    # b t-batches per call, replayed from a CUDA graph like the mixed path
     acq64 = make_acqf(model, w, "fp64")
     acq64.check_status = False
-    b64 = 256
-    X64 = Xd[:b64].contiguous()
-    o64 = (torch.empty(b64, dtype=torch.float64, device=device),
-           torch.empty(b64, Q, DIM, dtype=torch.float64, device=device),
-           torch.empty(b64, dtype=torch.int32, device=device))
-    step64 = lambda: acq64.value_and_grad_raw(X64, True, check=False, out=o64)  # noqa: E731
-    step64()
-    ms64 = statistics.median(time_steps(step64, 3, device, flush))
-    fp64_evals = b64 / (ms64 / 1e3)
+    step64 = lambda: acq64.graphed_value_and_grad(Xd, True, check=False)  # noqa: E731
+    step64()  # capture
+    ms64 = statistics.median(time_steps(step64, 2, device, flush))
+    fp64_evals = b / (ms64 / 1e3)
+    o64 = step64()
+    torch.cuda.synchronize(device)
 
     # accuracy of the mixed path against the float64 oracle (and of the fp64 path)
     cpu = None
@@ -400,6 +398,7 @@ def run_ours(args) -> None:
         "clocks": {**clk.summary(), "window": "0.6 s load, timed steps, 0.3 s load; 100 ms sampling"},
         "stage_ms": {k: round(v, 4) for k, v in zip(names, st)},
         "fp64_gpu_evals_per_s": round(fp64_evals, 1),
+        "fp64_gpu_mode": f"CUDA graph replay, {b} t-batches per call (as the mixed path)",
         "speedup_vs_fp64_gpu": round(value / world / fp64_evals, 2),
         "status_ok": status_ok, "wall_s_timed": round(t_wall, 3), **err,
     }
@@ -583,22 +582,35 @@ def _la_step_fns(w, go):
     return step_jac, step_recompute
 
 
-def la_cpu_baseline(w, threads: int, sample_batches: int) -> tuple[float, str]:
-    """The C restatement of the reference kernel (oracle) on `threads` host threads:
-    forward + backward of every subset size over the first `sample_batches` rows."""
+def la_cpu_baseline(w, threads: int, sample_batches: int) -> tuple[float, str, str]:
+    """Forward + backward of every subset size over the first `sample_batches` rows on
+    `threads` host threads: the reference's own kernel (botorch/csrc/logei_fused.cpp)
+    where it was compiled on this host (kind "reference"), else its bit-exact C
+    restatement in the oracle (kind "port")."""
     from oracle import log_areas as ola
+    from oracle.build import build_reference
 
+    ref = build_reference()
     cpu = [o[:sample_batches].cpu() for o in w.obj_subsets]
     cl, cu = w.cell_lower.cpu(), w.cell_upper.cpu()
     gos = [torch.ones(sample_batches, w.nc, o.shape[1], dtype=o.dtype) for o in cpu]
-    ola.forward(cpu[0][:8], cl, cu, w.tau_relu, w.tau_max)  # load / build
+    if ref is not None:
+        torch.set_num_threads(threads)  # the reference kernel threads with at::parallel_for
+        fwd = lambda o: ref.forward(o, cl, cu, w.tau_relu, w.tau_max)  # noqa: E731
+        bwd = lambda g, o: ref.backward(g, o, cl, cu, w.tau_relu, w.tau_max)  # noqa: E731
+        kind = "reference"
+    else:
+        fwd = lambda o: ola.forward(o, cl, cu, w.tau_relu, w.tau_max, threads=threads)  # noqa: E731
+        bwd = lambda g, o: ola.backward(g, o, cl, cu, w.tau_relu, w.tau_max, threads=threads)  # noqa: E731
+        kind = "port"
+    fwd(cpu[0][:8])  # load / build
     t0 = time.perf_counter()
     for o, g in zip(cpu, gos):
-        ola.forward(o, cl, cu, w.tau_relu, w.tau_max, threads=threads)
-        ola.backward(g, o, cl, cu, w.tau_relu, w.tau_max, threads=threads)
+        fwd(o)
+        bwd(g, o)
     dt = time.perf_counter() - t0
     areas = sample_batches * w.nc * sum(int(o.shape[1]) for o in cpu)
-    return areas / dt, f"{sample_batches} of {w.B} sample-batches, all subset sizes, fwd+bwd"
+    return areas / dt, f"{sample_batches} of {w.B} sample-batches, all subset sizes, fwd+bwd", kind
 
 
 def run_log_areas(args) -> None:
@@ -686,10 +698,10 @@ def run_log_areas(args) -> None:
     r = res["f64"]
     achieved_gbs = r["bytes_step"] / (r["ms_per_step"] / 1e3) / 1e9
     threads = os.cpu_count() or 1
-    cpu_value, cpu_sample = (None, None)
+    cpu_value, cpu_sample, cpu_kind = (None, None, None)
     if not args.no_cpu_baseline:
         w64 = log_areas_workload(dtype=torch.float64)
-        cpu_value, cpu_sample = la_cpu_baseline(w64, threads, 2048)
+        cpu_value, cpu_sample, cpu_kind = la_cpu_baseline(w64, threads, 2048)
     line = {
         "metric": LA_METRIC, "value": round(r["areas_per_s"], 1), "unit": "areas/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms_per_step"], 4),
@@ -717,16 +729,18 @@ def run_log_areas(args) -> None:
                                       "forward_jacobian": round(res["f32"]["fwdjac_ms_i2"], 4),
                                       "backward_from_jacobian": round(res["f32"]["bwdjac_ms_i2"], 4)}},
         "cpu_baseline": None if cpu_value is None else {
-            "value": round(cpu_value, 1), "unit": "areas/s", "cores": threads, "kind": "port",
-            "sample": cpu_sample + " (C restatement of the reference kernel, bit-exact to it on x86-64)"},
+            "value": round(cpu_value, 1), "unit": "areas/s", "cores": threads, "kind": cpu_kind,
+            "sample": cpu_sample + (" (the reference's own kernel, compiled on this host)" if cpu_kind == "reference"
+                                    else " (C restatement of the reference kernel, bit-exact to it on x86-64)")},
         "gpu_launches": int(r["launches"]), "clocks": r["clocks"],
     }
     print(json.dumps(line), flush=True)
 
 
 def run_log_areas_reference(args) -> None:
-    """Reference arm of the log-areas benchmark: the reference kernel's C restatement
-    (bit-exact to botorch/csrc/logei_fused.cpp where that compiles) on all host cores."""
+    """Reference arm of the log-areas benchmark on all host cores: the reference's own
+    kernel (botorch/csrc/logei_fused.cpp) where it was compiled on this host, else its
+    C restatement (bit-exact to it on x86-64)."""
     world, rank, _ = dist_info()
     if rank != 0:
         return
@@ -738,14 +752,14 @@ def run_log_areas_reference(args) -> None:
     for _ in range(max(args.warmup, 1)):
         la_cpu_baseline(w, threads, 256)
     vals = [la_cpu_baseline(w, threads, sample) for _ in range(args.steps)]
-    value = statistics.median(v for v, _ in vals)
+    value = statistics.median(v for v, _, _ in vals)
     line = {"metric": LA_METRIC, "value": round(value, 1), "unit": "areas/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded objective samples, 63-point front)",
             "impl": "reference",
             "config": {"workload": "log_areas_m2_q4_nc64_B32768", "B": w.B, "q": 4, "m": 2, "cells": 64},
-            "cpu_baseline": {"value": round(value, 1), "unit": "areas/s", "cores": threads, "kind": "port",
-                             "sample": vals[0][1]},
+            "cpu_baseline": {"value": round(value, 1), "unit": "areas/s", "cores": threads,
+                             "kind": vals[0][2], "sample": vals[0][1]},
             "e2e": {"value": round(value, 1), "unit": "areas/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -779,7 +793,10 @@ def run_reference(args) -> None:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Branin-sum GP workload)", "impl": "reference",
             "config": {"workload": WORKLOAD, "n": N_TRAIN, "d": DIM, "q": Q, "mc_samples": S,
-                       "batch_per_call": args.b, "parallelism": "host CPU, rank 0"},
+                       "batch_per_call": per_step, "workload_batch": args.b,
+                       "parallelism": "host CPU, rank 0"},
+            "rate_basis": "per t-batch value+gradient evaluation; each step is a bounded sample of "
+                          f"{per_step} of the workload's {args.b} t-batches",
             "cpu_baseline": {"value": round(value, 3), "unit": "evals/s", "cores": cores, "kind": "port",
                              "sample": f"{per_step} t-batches per step, value+grad, float64"},
             "e2e": {"value": round(value, 3), "unit": "evals/s", "h2d_bytes_per_step": 0,

@@ -361,15 +361,23 @@ int acq_call(const bgb_acq_t* a, const double* X, int64_t b, double* value, doub
 }
 
 // Device address of g_noalloc_scratch on the current device, looked up once per
-// device (cudaGetSymbolAddress with that device current) and cached.
+// device (cudaGetSymbolAddress with that device current) and cached. `stream`
+// must belong to the current device.
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
-int noalloc_scratch(void** out) {
+int noalloc_scratch(cudaStream_t stream, void** out) {
     int dev = -1;
     BGB_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) return BGB_ERR_UNSUPPORTED;
+    // the array's address is per device: a stream of another device would get
+    // this device's address, so such a call is rejected
+    if (stream != nullptr) {
+        int sdev = -1;
+        BGB_CUDA_TRY(cudaStreamGetDevice(stream, &sdev));
+        if (sdev != dev) return BGB_ERR_ARG;
+    }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (g_noalloc_ptr[dev] == nullptr) {
         void* p = nullptr;
@@ -683,7 +691,7 @@ int bgb_acq_forward_backward_noalloc(const bgb_acq_t* acq, const double* X, int6
         BGB_NOALLOC_SCRATCH_BYTES)
         return BGB_ERR_SCRATCH_LIMIT;
     void* scratch = nullptr;
-    int rc = noalloc_scratch(&scratch);
+    int rc = noalloc_scratch(as_stream(stream), &scratch);
     if (rc) return rc;
     // acq_call clears the device error word on `stream` before its first launch
     return acq_call(acq, X, b, value, grad, status, scratch, BGB_NOALLOC_SCRATCH_BYTES,

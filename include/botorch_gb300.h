@@ -313,6 +313,8 @@ int bgb_acq_forward_backward_timed(const bgb_acq_t* acq, const double* X, int64_
  *   - The first call on each device looks up the array's address on that device
  *     (with that device current), which may load the library's device code
  *     there. Make that first call before any stream capture on the device.
+ *   - `stream` must belong to the current device (the array's address is per
+ *     device); a stream of another device returns BGB_ERR_ARG.
  *   - All calls on a device share the one array. Calls that overlap on the GPU
  *     (two streams, or two host threads with their own streams) race and
  *     corrupt each other's results: issue them on one stream, or serialise them.

@@ -27,12 +27,13 @@ computes.
 from __future__ import annotations
 
 import math
+import warnings
 
 import torch
 from torch import Tensor
 
 from oracle import safe_math
-from oracle.gp import ExactGP, NanError, psd_safe_cholesky
+from oracle.gp import ExactGP, NanError, NotPSDError, psd_safe_cholesky
 from oracle.sampling import draw_sobol_normal_samples, qlognei_base_samples
 
 TAU_RELU = 1e-6
@@ -155,9 +156,30 @@ class QLogNoisyExpectedImprovement:
         X_full = torch.cat([Xb, X], dim=-2)
         mean, cov = self.model.posterior(X_full)
         if not self.cache_root:
-            Lf = psd_safe_cholesky(cov)
-            Yf = mean.unsqueeze(0) + torch.einsum("bij,sj->sbi", Lf, Z)
-            return Yf[..., r:], Yf[..., :r].amax(dim=-1)
+            # the incumbent from the joint draw's own baseline samples, without gradient
+            # (acquisition/utils.py:137-141)
+            Yf = self._joint_samples(mean, cov, Z)
+            return Yf[..., r:], Yf[..., :r].amax(dim=-1).detach()
+        try:
+            Y = self._cached_root_samples(mean, cov, Z, q)
+        except (NanError, NotPSDError):
+            # cached_cholesky.py:143-158: warn, then sample the joint posterior; the
+            # incumbent stays the cached one (logei.py:501-512)
+            warnings.warn("Low-rank cholesky updates failed due NaNs or due to an ill-conditioned "
+                          "covariance matrix. Falling back to standard sampling.", RuntimeWarning)
+            Y = self._joint_samples(mean, cov, Z)[..., r:]
+        return Y, self.best_f.unsqueeze(-1).expand(Y.shape[:-1])
+
+    @staticmethod
+    def _joint_samples(mean: Tensor, cov: Tensor, Z: Tensor) -> Tensor:
+        """S x b x (r+q) samples mean + chol(cov) z from the joint posterior
+        (MultivariateNormal.rsample through psd_safe_cholesky of the whole covariance)."""
+        Lf = psd_safe_cholesky(cov)
+        return mean.unsqueeze(0) + torch.einsum("bij,sj->sbi", Lf, Z)
+
+    def _cached_root_samples(self, mean: Tensor, cov: Tensor, Z: Tensor, q: int) -> Tensor:
+        """S x b x q samples from the low-rank update of the cached root (low_rank.py:84-172)."""
+        r = self.r
         bottom = cov[..., -q:, :]
         bl, br = bottom[..., :r], bottom[..., r:]
         if r > 0:
@@ -170,7 +192,7 @@ class QLogNoisyExpectedImprovement:
         Y = mean[..., -q:].unsqueeze(0) + torch.einsum("bij,sj->sbi", new_Lq, Z)
         if not torch.isfinite(Y).all():
             raise NanError("Samples contain nans or infs.")
-        return Y, self.best_f.unsqueeze(-1).expand(Y.shape[:-1])
+        return Y
 
     def forward(self, X: Tensor) -> Tensor:
         Y, best_f = self.samples(X)

@@ -50,11 +50,16 @@ def default_jitter(dtype: torch.dtype) -> float:
     return 1e-8 if dtype == torch.float64 else 1e-6
 
 
-def psd_safe_cholesky(A: Tensor, max_tries: int = 6, jitter: float | None = None) -> Tensor:
-    """Batched Cholesky with per-member jitter retries (linear_operator's published algorithm)."""
+def psd_safe_cholesky(A: Tensor, max_tries: int = 6, jitter: float | None = None,
+                      return_jitter: bool = False):
+    """Batched Cholesky with per-member jitter retries (linear_operator's published algorithm).
+
+    With ``return_jitter`` the total jitter added to the last failing member's
+    diagonal (0.0 when the plain factorisation succeeds) is returned beside L.
+    """
     L, info = torch.linalg.cholesky_ex(A)
     if not torch.any(info):
-        return L
+        return (L, 0.0) if return_jitter else L
     if torch.isnan(A).any():
         raise NanError("cholesky_cpu: input matrix contains NaNs")
     if jitter is None:
@@ -68,7 +73,7 @@ def psd_safe_cholesky(A: Tensor, max_tries: int = 6, jitter: float | None = None
         jitter_prev = jitter_new
         L, info = torch.linalg.cholesky_ex(Aprime)
         if not torch.any(info):
-            return L
+            return (L, jitter_new) if return_jitter else L
     raise NotPSDError(f"Matrix not positive definite after repeatedly adding jitter up to {jitter_new:.1e}.")
 
 
@@ -151,7 +156,10 @@ class ExactGP:
         y = self.tf.transform(Y).squeeze(-1)
         K = self.k(self.X, self.X)
         K.diagonal().add_(self.noise)
-        self.L = psd_safe_cholesky(K)
+        self.L, self.jitter = psd_safe_cholesky(K, return_jitter=True)
+        # a perturbation (standardised units) added to the posterior mean of the last
+        # mean_shift.numel() points of every posterior call; None in normal use
+        self.mean_shift: Tensor | None = None
         self.alpha = torch.cholesky_solve((y - self.mean_constant).unsqueeze(-1), self.L).squeeze(-1)
 
     def k(self, X1: Tensor, X2: Tensor) -> Tensor:
@@ -161,8 +169,15 @@ class ExactGP:
         """Mean and covariance in the standardised space for ``batch x m x d`` inputs."""
         Ks = self.k(X, self.X)                        # batch x m x n
         mean = self.mean_constant + Ks @ self.alpha
-        V = torch.linalg.solve_triangular(self.L, Ks.transpose(-1, -2), upper=False)  # batch x n x m
-        cov = self.k(X, X) - V.transpose(-1, -2) @ V
+        if self.mean_shift is not None:  # sensitivity studies: shift the last points' means
+            k = self.mean_shift.shape[-1]
+            mean = torch.cat([mean[..., :-k], mean[..., -k:] + self.mean_shift], dim=-1)
+        # one triangular solve with all batch x m right-hand sides (a batched solve
+        # would broadcast the n x n factor over the batch)
+        m, n = Ks.shape[-2], Ks.shape[-1]
+        V = torch.linalg.solve_triangular(self.L, Ks.reshape(-1, n).transpose(0, 1), upper=False)
+        V = V.transpose(0, 1).reshape(*Ks.shape[:-2], m, n)  # batch x m x n: rows L^-1 k(x_i, Xt)
+        cov = self.k(X, X) - V @ V.transpose(-1, -2)
         return mean, cov
 
     def posterior(self, X: Tensor) -> tuple[Tensor, Tensor]:

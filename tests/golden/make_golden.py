@@ -1,7 +1,7 @@
 """Generate tests/golden/reference_golden.npz from the reference's own modules.
 
-Run in a container that has the BoTorch sources (argument 1, default the
-read-only mount used when the fixtures were made). gpytorch and
+Run in a container that has the BoTorch sources; argument 1 is the root of
+that checkout (required). gpytorch and
 linear_operator are not importable there, so ``botorch/__init__.py`` cannot
 run; the modules below only need torch, numpy and scipy, and are loaded by
 registering bare package stubs whose ``__path__`` points at the reference
@@ -88,4 +88,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_golden.py <root of the reference checkout>")
+    main(sys.argv[1])

@@ -60,8 +60,8 @@ def cases(dtype: torch.dtype):
         yield name, obj, lo, up
 
 
-def main() -> None:
-    ref = build_reference()
+def main(root: str) -> None:
+    ref = build_reference(root)
     if ref is None:
         raise SystemExit("the reference checkout is not present: cannot generate the fixtures")
     out = {}
@@ -82,4 +82,6 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_log_areas_golden.py <root of the reference checkout>")
+    main(sys.argv[1])

@@ -13,7 +13,10 @@ not depend on the CPU arithmetic of the machine that hosts the GPU. Cases:
                   value + gradient of every 64th of the 4096 t-batches.
 
 A checksum of each candidate tensor is stored so that a test can verify that
-the seeded generator reproduced the same inputs on the GPU host.
+the seeded generator reproduced the same inputs on the GPU host. For the qLogNEI
+cases, ``*_sens_v`` / ``*_sens_g`` hold each t-batch's sensitivity to a 1e-6
+shift of the standardised posterior mean (oracle/sensitivity.py), which bounds
+the mixed path's error where float32 rounding of the mean is amplified.
 """
 
 from __future__ import annotations
@@ -31,6 +34,7 @@ from botorch_gb300 import testing as T  # noqa: E402
 from oracle.acquisition import (QExpectedImprovement, QLogNoisyExpectedImprovement,  # noqa: E402
                                 qei_value_and_grad)
 from oracle.gp import ExactGP  # noqa: E402
+from oracle.sensitivity import mean_sensitivity  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "parity_fixtures.npz"
 
@@ -55,18 +59,22 @@ def main() -> None:
     a = QLogNoisyExpectedImprovement(model(w), w.train_X, w.n_samples, w.seed)
     idx = torch.arange(0, 256)
     v, g = a.value_and_grad(w.X[idx])
+    sv, sg = mean_sensitivity(a, w.X[idx], v, g)
     out.update({"qlognei_diff_idx": idx.numpy(), "qlognei_diff_value": v.numpy(),
                 "qlognei_diff_grad": g.numpy(), "qlognei_diff_Xb": a.X_baseline.numpy(),
-                "qlognei_diff_Xsum": checksum(w.X)})
+                "qlognei_diff_Xsum": checksum(w.X), "qlognei_diff_sens_v": sv.numpy(),
+                "qlognei_diff_sens_g": sg.numpy()})
 
     w = T.qlognei_branin(n=4096, b=4096, q=8, d=20)
     torch.manual_seed(0)
     a = QLogNoisyExpectedImprovement(model(w), w.train_X, w.n_samples, w.seed)
     idx = torch.arange(0, 4096, 64)
     v, g = a.value_and_grad(w.X[idx])
+    sv, sg = mean_sensitivity(a, w.X[idx], v, g)
     out.update({"qlognei_branin_idx": idx.numpy(), "qlognei_branin_value": v.numpy(),
                 "qlognei_branin_grad": g.numpy(), "qlognei_branin_Xb": a.X_baseline.numpy(),
-                "qlognei_branin_Xsum": checksum(w.X)})
+                "qlognei_branin_Xsum": checksum(w.X), "qlognei_branin_sens_v": sv.numpy(),
+                "qlognei_branin_sens_g": sg.numpy()})
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

@@ -11,7 +11,7 @@ import pytest
 import torch
 
 from oracle import log_areas as ola
-from oracle.build import REFERENCE_SRC
+from oracle.build import build_reference
 
 GOLDEN = Path(__file__).parent / "golden" / "log_areas_golden.npz"
 
@@ -71,11 +71,10 @@ def test_oracle_matches_unfused_python_path():
         torch.testing.assert_close(g, x.grad, atol=1e-6, rtol=1e-6, msg=key)
 
 
-@pytest.mark.skipif(not REFERENCE_SRC.exists(), reason="reference checkout not present")
 def test_oracle_matches_live_reference_kernel():
-    from oracle.build import build_reference
-
     ref = build_reference()
+    if ref is None:
+        pytest.skip("the reference kernel was not built here (no reference checkout)")
     g = torch.Generator().manual_seed(3)
     for dtype in (torch.float64, torch.float32):
         for B, n_sub, isz, m, nc, batched in [(4, 6, 2, 2, 5, False), (3, 4, 7, 3, 6, True), (2, 1, 32, 8, 2, False)]:
