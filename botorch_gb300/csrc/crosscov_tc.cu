@@ -12,10 +12,17 @@
 //   forward  V = Kc L^-T   (B operand stored as L^-1, K-major; k < n0 + BN)
 //   adjoint  D = H  L^-1   (B operand stored as L^-T, K-major; k >= n0)
 //
-// One CTA computes a 128 x 256 tile of C. Warp roles: warp 0 issues the TMA
-// loads (one elected lane), warp 1 owns the TMEM allocation and issues the
-// MMAs (one elected lane), warps 2-9 drain the accumulators. Two shared-memory
-// stages of {A_hi, A_lo, B_hi, B_lo} (96 KB each, 64 K-elements deep).
+// Two forms share one kernel body. PAIR = 2 (the default): a cluster of two CTAs
+// on two SMs computes a 256 x 256 tile of C with tcgen05.mma.cta_group::2
+// (M = 256), each CTA staging its own 128 rows of A and 128 of the 256 rows of B,
+// so each SM's shared memory feeds half of B per MMA; three stages of 64 KB.
+// PAIR = 1: one CTA per 128 x 256 tile, two stages of 96 KB. Warp roles: warp 0
+// issues the TMA loads (one elected lane; in the pair, each CTA its own rows,
+// completing on the leader CTA's barrier), warp 1 owns the TMEM allocation and
+// (leader CTA only) issues the MMAs, warps 2-9 drain the accumulators and store
+// C through shared memory with TMA. The kernel is persistent: one CTA (cluster)
+// per SM (pair) walks a static, work-balanced schedule of tiles, keeping TMEM
+// and the pipeline across tiles.
 //
 // Accumulation: the K range is cut into chunks of TC_FLUSH k-blocks; each chunk
 // is accumulated in one of two TMEM accumulators (ping-pong, 2 x 256 columns)
@@ -28,6 +35,7 @@
 // its TMEM and returns.
 #include <cuda.h>
 #include <cuda_fp16.h>
+#include <stdlib.h>
 
 #include "bgb_common.cuh"
 #include "bgb_kernels.cuh"
@@ -37,20 +45,33 @@ namespace bgb {
 namespace {
 
 constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64;  // BK: float16 elements (128 bytes)
-constexpr int TC_STAGES = 2;
 constexpr int TC_UMMA_K = 16;                         // float16 K per tcgen05.mma
 constexpr uint32_t A_TILE = TC_BM * TC_BK * 2;        // 16 KB
-constexpr uint32_t B_TILE = TC_BN * TC_BK * 2;        // 32 KB
-constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr int TC_THREADS = 320;                       // 10 warps
 constexpr int TC_FLUSH = 1;                           // k-blocks per TMEM accumulation chunk
 constexpr uint32_t TMEM_COLS = 512;                   // two 128 x 256 float32 accumulators
-constexpr size_t TC_SMEM = TC_STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
-// instruction descriptor (kind::f16): D f32, A/B f16, both K-major, N = 256, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
-                            ((uint32_t)(TC_BM >> 4) << 24);
+// Tile geometry of the two forms. PAIR = 1: one CTA computes a 128 x 256 tile
+// (B tile 256 rows), two stages of 96 KB. PAIR = 2 (cta_group::2): a cluster
+// of two CTAs on two SMs computes a 256 x 256 tile with one M = 256 MMA; each
+// CTA stages its own 128 rows of A and 128 of the 256 B rows, so the shared
+// memory each SM reads per MMA halves; three stages of 64 KB. Both keep one
+// 32 x 32 float32 staging tile per epilogue warp for the TMA stores of C.
+template <int PAIR>
+struct TcCfg {
+    static constexpr int STAGES = PAIR == 2 ? 3 : 2;
+    static constexpr int B_ROWS = TC_BN / PAIR;
+    static constexpr uint32_t B_TILE = (uint32_t)B_ROWS * TC_BK * 2;
+    static constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
+    static constexpr uint32_t TX_BYTES = STAGE_BYTES * PAIR;  // bytes that complete one stage
+    static constexpr uint32_t STAGING = 8 * 32 * 32 * 4;      // 8 epilogue warps x 4 KB
+    static constexpr size_t SMEM = STAGES * STAGE_BYTES + STAGING + 1024 /*align*/ + 256 /*barriers*/;
+    // instruction descriptor (kind::f16): D f32, A/B f16, both K-major, N = 256, M = 128 PAIR
+    static constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) |
+                                      ((uint32_t)(TC_BN >> 3) << 17) |
+                                      ((uint32_t)((TC_BM * PAIR) >> 4) << 24);
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -60,6 +81,24 @@ __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Address of the same shared-memory location in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t peer_addr(uint32_t saddr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -72,8 +111,20 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                  : "memory");
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+// Arrive on barrier `bar` of CTA `rank` of the cluster (PAIR = 2) or of this CTA.
+// The arrival orders this thread's completed tcgen05.ld (after wait::ld and a
+// tcgen05 fence) before the MMAs the waiting thread issues next; no
+// cluster-scope memory fence is needed for that (one per arrival stalled the
+// epilogue warps measurably).
+template <int PAIR>
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar, uint32_t rank) {
+    if constexpr (PAIR == 2) {
+        asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(
+                         peer_addr(smem_u32(bar), rank))
+                     : "memory");
+    } else {
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+    }
 }
 
 // Wait for the phase with parity `phase` to complete; false after kWaitNs or
@@ -97,13 +148,24 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase,
     }
 }
 
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
-        : "memory");
+// 2-D tile load into this CTA's shared memory; completion is counted on the
+// mbarrier at shared::cluster address `bar` (PAIR = 2: the leader CTA's).
+template <int PAIR>
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint32_t bar, int x,
+                                            int y) {
+    if constexpr (PAIR == 2) {
+        asm volatile(
+            "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes "
+            "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+            "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+            : "memory");
+    } else {
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+            "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+            "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+            : "memory");
+    }
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of 1024 bytes.
@@ -117,20 +179,68 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
     return d;
 }
 
+template <int PAIR>
 __device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                          uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+    if constexpr (PAIR == 2) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(TcCfg<2>::IDESC), "r"(accumulate));
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(TcCfg<1>::IDESC), "r"(accumulate));
+    }
 }
 
+// Arrive on `bar` once the MMAs issued so far have completed; PAIR = 2: on the
+// barrier at the same offset in both CTAs of the pair.
+template <int PAIR>
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(bar))
-        : "memory");
+    if constexpr (PAIR == 2) {
+        asm volatile(
+            "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+            "[%0], %1;" ::"r"(smem_u32(bar)),
+            "h"((uint16_t)3)
+            : "memory");
+    } else {
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(bar))
+            : "memory");
+    }
+}
+
+// TMEM allocation: with cta_group::2, one warp of each CTA of the pair takes
+// part in the allocation and in the release.
+template <int PAIR>
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot) {
+    if constexpr (PAIR == 2) {
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    } else {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+}
+
+template <int PAIR>
+__device__ __forceinline__ void tmem_dealloc(uint32_t tmem) {
+    if constexpr (PAIR == 2) {
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(TMEM_COLS));
+    } else {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(TMEM_COLS));
+    }
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -149,183 +259,284 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 struct TcMaps {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
+    CUtensorMap c;  // float32 output, 32 x 32 boxes, 128-byte swizzle
 };
 
-// kmode: KB_UPPER (forward, k < n0 + BN) or KB_LOWER (adjoint, k >= n0).
+// 2-D tile store from this CTA's shared memory (bulk async group).
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void* src, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+            reinterpret_cast<uint64_t>(map)),
+        "r"(smem_u32(src)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Static schedule shared by every role of a CTA (no broadcast needed): super-tile
+// s = (row block, p) holds the output column blocks p and n_tiles - 1 - p of one
+// row block. Their triangular k ranges add up to the same length for every p, so
+// a round-robin of super-tiles over the clusters balances the work; consecutive
+// super-tiles share the row block, so the A rows in flight stay in L2. The longer
+// k range of the two runs first.
+struct TileSched {
+    int n_tiles, P, total, kmode;
+    __device__ TileSched(int m_tiles, int n_tiles_, int kmode_)
+        : n_tiles(n_tiles_), P((n_tiles_ + 1) / 2), total(m_tiles * ((n_tiles_ + 1) / 2)),
+          kmode(kmode_) {}
+    // tile h (0, 1) of super-tile s; false when s holds a single (middle) column block
+    __device__ bool tile(int s, int h, int& m_tile, int& n_tile) const {
+        const int p = s % P;
+        m_tile = s / P;
+        const int lo = p, hi = n_tiles - 1 - p;
+        if (h == 1 && hi == lo) return false;
+        const bool hi_first = (kmode != KB_LOWER);  // KB_UPPER: k range grows with the block
+        n_tile = ((h == 0) == hi_first) ? hi : lo;
+        return true;
+    }
+    __device__ void k_range(int n_tile, int K, int& kbeg, int& nkb) const {
+        const int n0 = n_tile * TC_BN;
+        int kend = K;
+        kbeg = 0;
+        if (kmode == KB_UPPER) kend = min(K, n0 + TC_BN);
+        else if (kmode == KB_LOWER) kbeg = (n0 / TC_BK) * TC_BK;
+        nkb = kend > kbeg ? (kend - kbeg + TC_BK - 1) / TC_BK : 0;
+    }
+};
+
+// kmode: KB_UPPER (forward, k < n0 + BN), KB_LOWER (adjoint, k >= n0) or KFULL.
+// Persistent: each CTA (PAIR = 2: each cluster of two CTAs, rank 0 issuing the
+// MMAs) walks the tiles of the static schedule above. TMEM is allocated once;
+// the stage and accumulator counters run on across tiles, so the next tile's
+// loads and MMAs proceed while the epilogue warps store the previous tile.
+template <int PAIR>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_gemm_kernel(const __grid_constant__ TcMaps maps, float* __restrict__ C, int64_t ldc,
-                   int M, int N, int K, int kmode, int n_tiles, const float* __restrict__ row_mul,
+    tc_gemm_kernel(const __grid_constant__ TcMaps maps, int M, int N, int K, int kmode,
+                   int m_tiles, int n_tiles, const float* __restrict__ row_mul,
                    float row_mul_const, const float* __restrict__ col_mul, int* __restrict__ err) {
+    using Cfg = TcCfg<PAIR>;
+    constexpr int STAGES = Cfg::STAGES;
     extern __shared__ __align__(1024) uint8_t smraw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) &
                                                ~(uintptr_t)1023);
-    uint64_t* full = reinterpret_cast<uint64_t*>(base + TC_STAGES * STAGE_BYTES);
-    uint64_t* empty = full + TC_STAGES;
-    uint64_t* accf = empty + TC_STAGES;  // accumulator a holds a finished chunk
-    uint64_t* acce = accf + 2;           // accumulator a has been drained
+    float* staging = reinterpret_cast<float*>(base + STAGES * Cfg::STAGE_BYTES);  // 1024-aligned
+    uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * Cfg::STAGE_BYTES + Cfg::STAGING);
+    uint64_t* empty = full + STAGES;
+    uint64_t* accf = empty + STAGES;  // accumulator a holds a finished chunk
+    uint64_t* acce = accf + 2;        // accumulator a has been drained
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
     int* fail = reinterpret_cast<int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    // tile order: consecutive CTAs share the A row-block (all n-tiles of one m-tile),
-    // and within it the longest k range comes first (KB_UPPER: the last column
-    // blocks, KB_LOWER: the first), so the final wave holds the short tiles
-    const int m_tile = blockIdx.x / n_tiles;
-    const int n_idx = blockIdx.x % n_tiles;
-    const int n_tile = (kmode == KB_UPPER) ? n_tiles - 1 - n_idx : n_idx;
-    const int m0 = m_tile * TC_BM, n0 = n_tile * TC_BN;
-    int kbeg = 0, kend = K;
-    if (kmode == KB_UPPER) kend = min(K, n0 + TC_BN);
-    else if (kmode == KB_LOWER) kbeg = (n0 / TC_BK) * TC_BK;
-    const int nkb = (kend - kbeg + TC_BK - 1) / TC_BK;
+    const uint32_t rank = (PAIR == 2) ? cluster_rank() : 0u;
+    const bool leader = (rank == 0);
+    const int cluster = blockIdx.x / PAIR, nclusters = gridDim.x / PAIR;
+    const TileSched sched(m_tiles, n_tiles, kmode);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < TC_STAGES; ++s) {
+        for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(&accf[a], 1);
-            mbar_init(&acce[a], 8);  // one arrival per epilogue warp
+            mbar_init(&acce[a], 8 * PAIR);  // one arrival per epilogue warp of the pair
         }
         *fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                         smem_u32(tmem_slot)),
-                     "r"(TMEM_COLS));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
+    if (warp == 1) tmem_alloc<PAIR>(tmem_slot);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
+    if constexpr (PAIR == 2) cluster_sync();  // the peer's barriers exist before any remote use
+    else __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0 && lane == 0) {
-        // ---------------- TMA producer
-        int issued = 0;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % TC_STAGES;
-            if (kb >= TC_STAGES && !mbar_wait(&empty[s], ((kb / TC_STAGES) - 1) & 1, fail)) {
-                atomicExch(fail, 1);
-                break;
-            }
-            if (*(volatile int*)fail) break;
-            uint8_t* st = base + s * STAGE_BYTES;
-            const int k = kbeg + kb * TC_BK;
-            mbar_expect_tx(&full[s], STAGE_BYTES);
-            tma_load_2d(st, &maps.a_hi, &full[s], k, m0);
-            tma_load_2d(st + A_TILE, &maps.a_lo, &full[s], k, m0);
-            tma_load_2d(st + 2 * A_TILE, &maps.b_hi, &full[s], k, n0);
-            tma_load_2d(st + 2 * A_TILE + B_TILE, &maps.b_lo, &full[s], k, n0);
-            issued = kb + 1;
-        }
-        // copies in flight must land before the CTA may exit: wait for the last
-        // phase armed on each stage (bounded)
-        if (*(volatile int*)fail) {
-            for (int kb = issued - TC_STAGES < 0 ? 0 : issued - TC_STAGES; kb < issued; ++kb)
-                mbar_wait(&full[kb % TC_STAGES], (kb / TC_STAGES) & 1);
-        }
-    } else if (warp == 1 && lane == 0) {
-        // ---------------- MMA issuer
-        const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
-        for (int c = 0; c < nch; ++c) {
-            const int a = c & 1;
-            if (c >= 2 && !mbar_wait(&acce[a], ((c >> 1) - 1) & 1, fail)) {
-                atomicCAS(fail, 0, 4);
-                break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t tacc = tmem + (uint32_t)(a * TC_BN);
-            const int kb_end = min(nkb, (c + 1) * TC_FLUSH);
-            bool ok = true;
-            for (int kb = c * TC_FLUSH; kb < kb_end; ++kb) {
-                const int s = kb % TC_STAGES;
-                if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, fail)) {
-                    atomicCAS(fail, 0, 2);
-                    ok = false;
-                    break;
+        // ---------------- TMA producer (each CTA loads its own rows of A and of B)
+        int g = 0;  // k-blocks issued by this CTA
+        bool stop = false;
+        for (int s = cluster; s < sched.total && !stop; s += nclusters) {
+            for (int h = 0; h < 2 && !stop; ++h) {
+                int m_tile, n_tile, kbeg, nkb;
+                if (!sched.tile(s, h, m_tile, n_tile)) continue;
+                sched.k_range(n_tile, K, kbeg, nkb);
+                const int arow = m_tile * TC_BM * PAIR + (int)rank * TC_BM;
+                const int brow = n_tile * TC_BN + (int)rank * Cfg::B_ROWS;
+                for (int kb = 0; kb < nkb; ++kb, ++g) {
+                    const int st = g % STAGES;
+                    if (g >= STAGES && !mbar_wait(&empty[st], ((g / STAGES) - 1) & 1, fail)) {
+                        atomicExch(fail, 1);
+                        stop = true;
+                        break;
+                    }
+                    if (*(volatile int*)fail) {
+                        stop = true;
+                        break;
+                    }
+                    uint8_t* sp = base + st * Cfg::STAGE_BYTES;
+                    const int k = kbeg + kb * TC_BK;
+                    // the stage completes on the leader's barrier once both CTAs' bytes landed
+                    if (leader) mbar_expect_tx(&full[st], Cfg::TX_BYTES);
+                    const uint32_t bar =
+                        (PAIR == 2) ? peer_addr(smem_u32(&full[st]), 0) : smem_u32(&full[st]);
+                    tma_load_2d<PAIR>(sp, &maps.a_hi, bar, k, arow);
+                    tma_load_2d<PAIR>(sp + A_TILE, &maps.a_lo, bar, k, arow);
+                    tma_load_2d<PAIR>(sp + 2 * A_TILE, &maps.b_hi, bar, k, brow);
+                    tma_load_2d<PAIR>(sp + 2 * A_TILE + Cfg::B_TILE, &maps.b_lo, bar, k, brow);
                 }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
-                const uint32_t a_hi = sa, a_lo = sa + A_TILE, b_hi = sa + 2 * A_TILE,
-                               b_lo = sa + 2 * A_TILE + B_TILE;
+            }
+        }
+        // copies in flight must land before the CTA may exit: the leader waits for
+        // the last phase armed on each stage (bounded); the peer cannot wait on the
+        // leader's barrier and relies on the delay before the final cluster barrier
+        if (*(volatile int*)fail && leader) {
+            for (int gg = g - STAGES < 0 ? 0 : g - STAGES; gg < g; ++gg)
+                mbar_wait(&full[gg % STAGES], (gg / STAGES) & 1);
+        }
+    } else if (warp == 1 && lane == 0 && leader) {
+        // ---------------- MMA issuer (the leader CTA of the pair)
+        int g = 0, cg = 0;  // k-blocks consumed, accumulator chunks started
+        bool stop = false;
+        for (int s = cluster; s < sched.total && !stop; s += nclusters) {
+            for (int h = 0; h < 2 && !stop; ++h) {
+                int m_tile, n_tile, kbeg, nkb;
+                if (!sched.tile(s, h, m_tile, n_tile)) continue;
+                sched.k_range(n_tile, K, kbeg, nkb);
+                const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
+                for (int c = 0; c < nch && !stop; ++c, ++cg) {
+                    const int a = cg & 1;
+                    if (cg >= 2 && !mbar_wait(&acce[a], ((cg >> 1) - 1) & 1, fail)) {
+                        atomicCAS(fail, 0, 4);
+                        stop = true;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t tacc = tmem + (uint32_t)(a * TC_BN);
+                    const int kb_end = min(nkb, (c + 1) * TC_FLUSH);
+                    for (int kb = c * TC_FLUSH; kb < kb_end; ++kb, ++g) {
+                        const int st = g % STAGES;
+                        if (!mbar_wait(&full[st], (g / STAGES) & 1, fail)) {
+                            atomicCAS(fail, 0, 2);
+                            stop = true;
+                            break;
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t sa = smem_u32(base + st * Cfg::STAGE_BYTES);
+                        const uint32_t a_hi = sa, a_lo = sa + A_TILE, b_hi = sa + 2 * A_TILE,
+                                       b_lo = sa + 2 * A_TILE + Cfg::B_TILE;
 #pragma unroll
-                for (int kk = 0; kk < TC_BK / TC_UMMA_K; ++kk) {
-                    const uint32_t off = kk * TC_UMMA_K * 2;  // bytes along K in the 128-B row
-                    const uint32_t acc = (kb > c * TC_FLUSH || kk > 0) ? 1u : 0u;
-                    umma_f16(tacc, sdesc(a_lo + off), sdesc(b_hi + off), acc);
-                    umma_f16(tacc, sdesc(a_hi + off), sdesc(b_lo + off), 1u);
-                    umma_f16(tacc, sdesc(a_hi + off), sdesc(b_hi + off), 1u);
+                        for (int kk = 0; kk < TC_BK / TC_UMMA_K; ++kk) {
+                            const uint32_t off = kk * TC_UMMA_K * 2;  // bytes along K in the 128-B row
+                            const uint32_t acc = (kb > c * TC_FLUSH || kk > 0) ? 1u : 0u;
+                            umma_f16<PAIR>(tacc, sdesc(a_lo + off), sdesc(b_hi + off), acc);
+                            umma_f16<PAIR>(tacc, sdesc(a_hi + off), sdesc(b_lo + off), 1u);
+                            umma_f16<PAIR>(tacc, sdesc(a_hi + off), sdesc(b_hi + off), 1u);
+                        }
+                        umma_commit<PAIR>(&empty[st]);
+                    }
+                    umma_commit<PAIR>(&accf[a]);
                 }
-                umma_commit(&empty[s]);
             }
-            umma_commit(&accf[a]);
-            if (!ok) break;
         }
     } else if (warp >= 2) {
         // ---------------- epilogue: drain chunks into float32 registers, then store C
         const int quarter = warp % 4;          // TMEM lanes 32*quarter .. +31
         const int half = (warp - 2) / 4;       // columns 128*half .. +127
-        const int row = m0 + quarter * 32 + lane;
-        const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
-        float tot[TC_BN / 2];
-#pragma unroll
-        for (int j = 0; j < TC_BN / 2; ++j) tot[j] = 0.f;
+        float* stg = staging + (warp - 2) * 32 * 32;
+        int cg = 0;
         bool good = true;
-        for (int c = 0; c < nch; ++c) {
-            const int a = c & 1;
-            const bool ok = mbar_wait(&accf[a], (c >> 1) & 1, fail);
-            // warp-uniform decision: tcgen05.ld is a .sync.aligned warp instruction
-            const int drain = __shfl_sync(0xffffffffu, (ok && *(volatile int*)fail == 0) ? 1 : 0, 0);
-            if (!drain) {
-                if (lane == 0) atomicCAS(fail, 0, 3);
-                good = false;
-                break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) +
-                                   (uint32_t)(a * TC_BN + half * (TC_BN / 2));
+        for (int s = cluster; s < sched.total && good; s += nclusters) {
+            for (int h = 0; h < 2 && good; ++h) {
+                int m_tile, n_tile, kbeg, nkb;
+                if (!sched.tile(s, h, m_tile, n_tile)) continue;
+                sched.k_range(n_tile, K, kbeg, nkb);
+                const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
+                const int row0 = m_tile * TC_BM * PAIR + (int)rank * TC_BM + quarter * 32;
+                const int row = row0 + lane;
+                float tot[TC_BN / 2];
 #pragma unroll
-            for (int j = 0; j < TC_BN / 2 / 32; ++j) {
-                uint32_t r[32];
-                tmem_ld32(tbase + (uint32_t)(j * 32), r);
+                for (int j = 0; j < TC_BN / 2; ++j) tot[j] = 0.f;
+                for (int c = 0; c < nch; ++c, ++cg) {
+                    const int a = cg & 1;
+                    const bool ok = mbar_wait(&accf[a], (cg >> 1) & 1, fail);
+                    // warp-uniform decision: tcgen05.ld is a .sync.aligned warp instruction
+                    const int drain =
+                        __shfl_sync(0xffffffffu, (ok && *(volatile int*)fail == 0) ? 1 : 0, 0);
+                    if (!drain) {
+                        if (lane == 0) atomicCAS(fail, 0, 3);
+                        good = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) +
+                                           (uint32_t)(a * TC_BN + half * (TC_BN / 2));
 #pragma unroll
-                for (int v = 0; v < 32; ++v) tot[j * 32 + v] += __uint_as_float(r[v]);
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&acce[a]);
-        }
-        if (good && row < M) {
-            // undo the operand scales: row multiplier times column multiplier
-            const int c0 = n0 + half * (TC_BN / 2);
-            const float rm = row_mul != nullptr ? row_mul[row] : row_mul_const;
-            float* dst = C + (int64_t)row * ldc + c0;
-            if (c0 + TC_BN / 2 <= N && (ldc % 4) == 0 &&
-                (reinterpret_cast<uintptr_t>(col_mul + c0) % 16) == 0) {
-                const float4* cm4 = reinterpret_cast<const float4*>(col_mul + c0);
+                    for (int j = 0; j < TC_BN / 2 / 32; ++j) {
+                        uint32_t r[32];
+                        tmem_ld32(tbase + (uint32_t)(j * 32), r);
 #pragma unroll
-                for (int v = 0; v < TC_BN / 2 / 4; ++v) {
-                    const float4 cm = cm4[v];
-                    reinterpret_cast<float4*>(dst)[v] =
-                        make_float4(tot[4 * v] * rm * cm.x, tot[4 * v + 1] * rm * cm.y,
-                                    tot[4 * v + 2] * rm * cm.z, tot[4 * v + 3] * rm * cm.w);
+                        for (int v = 0; v < 32; ++v) tot[j * 32 + v] += __uint_as_float(r[v]);
+                    }
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive<PAIR>(&acce[a], 0);
                 }
-            } else {
+                if (!good) break;
+                // undo the operand scales (row multiplier times column multiplier) and
+                // store through shared memory: per 32-column group the warp writes its
+                // 32 x 32 tile (row = lane, 128-byte swizzle: 16-byte chunk v of row i at
+                // v ^ (i % 8)) and one lane issues a TMA store of it, so global writes are
+                // whole 128-byte row segments; the TMA clips rows >= M and columns >= N
+                const int c0 = n_tile * TC_BN + half * (TC_BN / 2);
+                const float rm = row < M ? (row_mul != nullptr ? row_mul[row] : row_mul_const) : 0.f;
 #pragma unroll
-                for (int v = 0; v < TC_BN / 2; ++v)
-                    if (c0 + v < N) dst[v] = tot[v] * rm * col_mul[c0 + v];
+                for (int j = 0; j < TC_BN / 2 / 32; ++j) {
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    __syncwarp();
+#pragma unroll
+                    for (int v = 0; v < 8; ++v) {
+                        const int col = c0 + j * 32 + 4 * v;
+                        float4 cm;
+                        if (col + 3 < N) {
+                            cm = *reinterpret_cast<const float4*>(col_mul + col);
+                        } else {
+                            cm.x = col < N ? col_mul[col] : 0.f;
+                            cm.y = col + 1 < N ? col_mul[col + 1] : 0.f;
+                            cm.z = col + 2 < N ? col_mul[col + 2] : 0.f;
+                            cm.w = 0.f;
+                        }
+                        const float* t = tot + j * 32 + 4 * v;
+                        *reinterpret_cast<float4*>(stg + lane * 32 + ((v ^ (lane & 7)) * 4)) =
+                            make_float4(t[0] * rm * cm.x, t[1] * rm * cm.y, t[2] * rm * cm.z,
+                                        t[3] * rm * cm.w);
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) {
+                        tma_store_2d(&maps.c, stg, c0 + j * 32, row0);
+                        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                    }
+                }
             }
         }
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        __syncwarp();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
+    if constexpr (PAIR == 2) {
+        // after a failure, give bulk copies still in flight (which count on the
+        // leader's barriers) time to land before either CTA of the pair exits
+        if (*(volatile int*)fail) {
+            const unsigned long long t0 = global_ns();
+            while (global_ns() - t0 < 50000ull) {
+            }
+        }
+        cluster_sync();
+    } else {
+        __syncthreads();
+    }
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"(TMEM_COLS));
+        tmem_dealloc<PAIR>(tmem);
     }
     if (threadIdx.x == 0 && *fail) atomicExch(err, *fail);
 }
@@ -398,6 +609,88 @@ bool make_map(CUtensorMap* map, const __half* ptr, int64_t rows, int64_t cols, i
     return r == CUDA_SUCCESS;
 }
 
+// 2-D row-major float32 matrix (rows x cols, leading dimension ld) as a TMA map
+// with 32 x 32 boxes and 128-byte swizzle: the epilogue's stores of C.
+bool make_map_f32(CUtensorMap* map, const float* ptr, int64_t rows, int64_t cols, int64_t ld) {
+    EncodeTiledFn fn = encode_fn();
+    if (fn == nullptr) return false;
+    if ((reinterpret_cast<uintptr_t>(ptr) & 15) != 0 || (ld * 4) % 16 != 0) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides,
+                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+// Clusters of form PAIR that can be resident at once (one CTA per SM), per device.
+template <int PAIR>
+int resident_clusters() {
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kNumSMs / PAIR;
+    if (cached[dev] == 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(PAIR * 64);
+        cfg.blockDim = dim3(TC_THREADS);
+        cfg.dynamicSmemBytes = TcCfg<PAIR>::SMEM;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = PAIR;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, tc_gemm_kernel<PAIR>, &cfg) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = kNumSMs / PAIR;
+        }
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
+// One persistent launch of the GEMM in form PAIR over m_tiles x n_tiles tiles:
+// as many clusters of PAIR CTAs as are resident at once, or fewer when there are
+// fewer super-tiles (pairs of column blocks of one row block).
+template <int PAIR>
+int launch_tc(const TcMaps& maps, int64_t M, int64_t N, int64_t K, int kmode, int m_tiles,
+              int n_tiles, const float* row_mul, float row_mul_const, const float* col_mul,
+              int* err, cudaStream_t stream) {
+    // the shared-memory opt-in is a per-device function attribute
+    static bool attr_set[64] = {};
+    int dev = 0;
+    BGB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+        BGB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel<PAIR>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)TcCfg<PAIR>::SMEM));
+        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    }
+    const int64_t super_tiles = (int64_t)m_tiles * ((n_tiles + 1) / 2);
+    const int64_t resident = resident_clusters<PAIR>();
+    const int64_t clusters = super_tiles < resident ? super_tiles : resident;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(clusters * PAIR));
+    cfg.blockDim = dim3(TC_THREADS);
+    cfg.dynamicSmemBytes = TcCfg<PAIR>::SMEM;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = PAIR;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    BGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, tc_gemm_kernel<PAIR>, maps, (int)M, (int)N, (int)K, kmode,
+                                    m_tiles, n_tiles, row_mul, row_mul_const, col_mul, err));
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
 }  // namespace
 
 bool tc_gemm_available() { return encode_fn() != nullptr; }
@@ -421,25 +714,24 @@ int tc_gemm_f16x3(int64_t M, int64_t N, int64_t K, const __half* A_hi, const __h
                   int64_t ldc, int kmode, const float* row_mul, float row_mul_const,
                   const float* col_mul, int* err, cudaStream_t stream) {
     if (M <= 0 || N <= 0) return BGB_OK;
-    if (col_mul == nullptr) return BGB_ERR_ARG;
+    if (col_mul == nullptr || (reinterpret_cast<uintptr_t>(col_mul) & 15) != 0) return BGB_ERR_ARG;
+    // form: the two-SM pair (default) or, with BGB_TC_PAIR=1 in the environment, the
+    // single-SM form (a comparison aid)
+    static const int pair = [] {
+        const char* e = getenv("BGB_TC_PAIR");
+        return (e != nullptr && e[0] == '1') ? 1 : 2;
+    }();
     TcMaps maps;
+    const int b_rows = TC_BN / pair;
     if (!make_map(&maps.a_hi, A_hi, M, K, lda, TC_BM) || !make_map(&maps.a_lo, A_lo, M, K, lda, TC_BM) ||
-        !make_map(&maps.b_hi, B_hi, N, K, ldbs, TC_BN) || !make_map(&maps.b_lo, B_lo, N, K, ldbs, TC_BN))
+        !make_map(&maps.b_hi, B_hi, N, K, ldbs, b_rows) || !make_map(&maps.b_lo, B_lo, N, K, ldbs, b_rows) ||
+        !make_map_f32(&maps.c, C, M, N, ldc))
         return BGB_ERR_UNSUPPORTED;
-    // the shared-memory opt-in is a per-device function attribute
-    static bool attr_set[64] = {};
-    int dev = 0;
-    BGB_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        BGB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)TC_SMEM));
-        if (dev >= 0 && dev < 64) attr_set[dev] = true;
-    }
-    const int m_tiles = (int)ceil_div(M, TC_BM), n_tiles = (int)ceil_div(N, TC_BN);
-    tc_gemm_kernel<<<(unsigned)(m_tiles * n_tiles), TC_THREADS, TC_SMEM, stream>>>(
-        maps, C, ldc, (int)M, (int)N, (int)K, kmode, n_tiles, row_mul, row_mul_const, col_mul, err);
-    BGB_CHECK_LAUNCH();
-    return BGB_OK;
+    const int m_tiles = (int)ceil_div(M, (int64_t)TC_BM * pair), n_tiles = (int)ceil_div(N, TC_BN);
+    return pair == 2 ? launch_tc<2>(maps, M, N, K, kmode, m_tiles, n_tiles, row_mul, row_mul_const,
+                                    col_mul, err, stream)
+                     : launch_tc<1>(maps, M, N, K, kmode, m_tiles, n_tiles, row_mul, row_mul_const,
+                                    col_mul, err, stream);
 }
 
 }  // namespace bgb
