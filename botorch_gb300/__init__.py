@@ -8,7 +8,7 @@ gradient), computed by hand-written sm_103a CUDA kernels behind the C ABI in
 
 from botorch_gb300.acquisition import (qExpectedImprovement, qLogNoisyExpectedImprovement,
                                        prune_inferior_points)
-from botorch_gb300.exceptions import NanError, NotPSDError, UnsupportedError
+from botorch_gb300.exceptions import BotorchWarning, NanError, NotPSDError, UnsupportedError
 from botorch_gb300.gp_regression import GPyTorchPosterior, SingleTaskGP, Standardize
 from botorch_gb300.kernels import (ConstantMean, GaussianLikelihood, MaternKernel, RBFKernel,
                                    ScaleKernel)
@@ -18,5 +18,5 @@ __all__ = [
     "SingleTaskGP", "GPyTorchPosterior", "Standardize", "qExpectedImprovement",
     "qLogNoisyExpectedImprovement", "prune_inferior_points", "SobolQMCNormalSampler",
     "draw_sobol_normal_samples", "MaternKernel", "RBFKernel", "ScaleKernel", "GaussianLikelihood",
-    "ConstantMean", "NotPSDError", "NanError", "UnsupportedError",
+    "ConstantMean", "NotPSDError", "NanError", "UnsupportedError", "BotorchWarning",
 ]

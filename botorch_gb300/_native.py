@@ -21,6 +21,9 @@ BGB_DEVICE_TIMEOUT = 3
 BGB_FLAG_SIMT = 1
 BGB_FLAG_ADJ_CTAS_SHIFT = 8
 BGB_FLAG_ADJ_CTAS_MASK = 0xFF00
+BGB_FLAG_JOINT_SAMPLING = 2     # joint (r+q) sampling, cached incumbent: the fallback path
+BGB_FLAG_UNCACHED_ROOT = 4      # with JOINT_SAMPLING: cache_root=False
+JOINT_LEVELS = 7                # psd_safe_cholesky: plain + 6 jitter levels
 BGB_ERR_ARG = -1
 BGB_ERR_WORKSPACE = -2
 BGB_ERR_CUDA = -3
@@ -62,7 +65,8 @@ class BgbAcq(ctypes.Structure):
                 ("Lhi", c_vp), ("Llo", c_vp), ("LThi", c_vp), ("LTlo", c_vp), ("Lmul", c_vp),
                 ("LTmul", c_vp), ("ldl", c_i64), ("beta_absmax", c_f64),
                 ("X_baseline", c_vp), ("Lb_inv", c_vp),
-                ("Z", c_vp), ("best_f", c_vp), ("tau_relu", c_f64), ("tau_max", c_f64)]
+                ("Z", c_vp), ("best_f", c_vp), ("tau_relu", c_f64), ("tau_max", c_f64),
+                ("Lb_inv_lv", c_vp), ("best_f_lv", c_vp)]
 
 
 _SIGNATURES = {
@@ -101,6 +105,9 @@ _SIGNATURES = {
                                      c_i32, c_vp, c_vp, c_vp, ctypes.POINTER(c_f64), c_vp, c_size,
                                      c_vp]),
     "bgb_qlognei_baseline_workspace_bytes": (c_size, [c_i64, c_i32, c_i32]),
+    "bgb_qlognei_joint_levels": (c_i32, [ctypes.POINTER(BgbGP), c_vp, c_vp, c_vp, c_i32, c_vp,
+                                         c_i32, c_vp, c_vp, c_vp, c_size, c_vp]),
+    "bgb_qlognei_joint_levels_workspace_bytes": (c_size, [c_i64, c_i32, c_i32]),
     "bgb_posterior": (c_i32, [ctypes.POINTER(BgbAcq), c_vp, c_i64, c_vp, c_vp, c_vp, c_size,
                               c_vp]),
     "bgb_acq_workspace_bytes": (c_size, [ctypes.POINTER(BgbAcq), c_i64]),

@@ -17,12 +17,13 @@ from __future__ import annotations
 
 import ctypes
 import math
+import warnings
 
 import torch
 from torch import Tensor
 
 from botorch_gb300 import _native as nat
-from botorch_gb300.exceptions import NanError, NotPSDError, UnsupportedError
+from botorch_gb300.exceptions import BotorchWarning, NanError, NotPSDError, UnsupportedError
 from botorch_gb300.gp_regression import SingleTaskGP
 from botorch_gb300.sampling import SobolQMCNormalSampler, draw_sobol_normal_samples
 
@@ -121,13 +122,39 @@ class _MCAcquisition:
 
     def value_and_grad_raw(self, Xd: Tensor, need_grad: bool, check: bool | None = None,
                            out: tuple | None = None, ws: "nat.Workspace | None" = None):
-        """Native call on a contiguous float64 ``b x q x d`` device tensor."""
-        lib = nat.lib()
+        """Native call on a contiguous float64 ``b x q x d`` device tensor.
+
+        With the status check on (``check``, default ``self.check_status``), a
+        t-batch whose sampling failed raises NotPSDError / NanError, after the
+        fallback of ``_fall_back`` where the acquisition function has one.
+        """
         b, q, d = Xd.shape
         if b == 0:
             empty = torch.empty(0, dtype=torch.float64, device=self.device)
             return empty, (torch.empty(0, q, d, dtype=torch.float64, device=self.device) if need_grad else None)
         acq, ws_bytes = self._call_struct(q)
+        value, grad, status = self._native_call(Xd, need_grad, acq, ws_bytes, out, ws)
+        if (self.check_status if check is None else check):
+            value, grad = self._checked(Xd, need_grad, value, grad, status)
+        return value, grad
+
+    def _checked(self, Xd: Tensor, need_grad: bool, value: Tensor, grad, status: Tensor):
+        """Raise for failed t-batches, or return the fallback's results."""
+        worst = int(status.max().item()) if status.numel() > 0 else 0
+        if worst in (nat.BGB_NOT_PSD, nat.BGB_NAN):
+            fb = self._fall_back(Xd, need_grad)
+            if fb is not None:
+                value, grad, status = fb
+        self._raise_for_status(status)
+        return value, grad
+
+    def _fall_back(self, Xd: Tensor, need_grad: bool):
+        """(value, grad, status) of another sampling route after a failed call, or None."""
+        return None
+
+    def _native_call(self, Xd: Tensor, need_grad: bool, acq, ws_bytes: dict, out=None, ws=None):
+        lib = nat.lib()
+        b, q, d = Xd.shape
         if out is None:
             value = torch.empty(b, dtype=torch.float64, device=self.device)
             grad = torch.empty(b, q, d, dtype=torch.float64, device=self.device) if need_grad else None
@@ -145,9 +172,7 @@ class _MCAcquisition:
             rc = lib.bgb_acq_forward(ctypes.byref(acq), nat.ptr(Xd), b, nat.ptr(value),
                                      nat.ptr(status), wp, wb, stream)
         nat.check(rc, type(self).__name__)
-        if (self.check_status if check is None else check):
-            self._raise_for_status(status)
-        return value, grad
+        return value, grad, status
 
     @staticmethod
     def _raise_for_status(status: Tensor) -> None:
@@ -203,7 +228,7 @@ class _MCAcquisition:
         entry["graph"].replay()
         value, grad, status = entry["out"]
         if (self.check_status if check is None else check):
-            self._raise_for_status(status)
+            value, grad = self._checked(Xd, need_grad, value, grad, status)
         return value, grad
 
     def graph_launches(self, b: int, q: int, need_grad: bool = True) -> int:
@@ -212,17 +237,24 @@ class _MCAcquisition:
                                   int(self.adjoint_ctas_per_sm)))
         return 0 if entry is None else int(entry["launches"])
 
-    def _call_struct(self, q: int):
+    def _call_struct(self, q: int, flags: int = 0):
         """The call struct for q points, rebuilt only when its base samples change
-        (a new baseline or pending points) or the GEMM form is switched."""
-        key = (q, bool(self.use_tensor_cores), int(self.adjoint_ctas_per_sm))
+        (a new baseline or pending points) or the GEMM form is switched. ``flags``:
+        extra BGB_FLAG_* bits (the sampling route)."""
+        key = (q, bool(self.use_tensor_cores), int(self.adjoint_ctas_per_sm), flags)
         hit = self._structs.get(key)
         if hit is None or hit[1] is not self._Z.get(q):
             acq = self._acq_struct(q)
             acq.flags |= (int(self.adjoint_ctas_per_sm) << nat.BGB_FLAG_ADJ_CTAS_SHIFT) & nat.BGB_FLAG_ADJ_CTAS_MASK
+            acq.flags |= flags
+            if flags & nat.BGB_FLAG_JOINT_SAMPLING:
+                self._set_joint_operands(acq)
             hit = (acq, self._Z.get(q), {})
             self._structs[key] = hit
         return hit[0], hit[2]
+
+    def _set_joint_operands(self, acq: nat.BgbAcq) -> None:
+        raise UnsupportedError("joint sampling needs a baseline")
 
     def _device_Z(self, q: int) -> Tensor:
         if q not in self._Z:
@@ -329,8 +361,9 @@ class qLogNoisyExpectedImprovement(_MCAcquisition):
         super().__init__(model, sampler, objective, posterior_transform, constraints, precision)
         if not fat:
             raise UnsupportedError("fat=False (logsumexp q-reduction) is not supported on this path")
-        if cache_root is False:
-            raise UnsupportedError("only the cached-root form is implemented on this path")
+        # cache_root=False: every call samples the joint (r+q)-dim posterior and takes
+        # the incumbent from its own baseline samples (logei.py:543-553)
+        self.cache_root = cache_root is not False
         if not incremental:
             raise UnsupportedError("incremental=False is not supported on this path")
         if not (tau_max > 0 and tau_relu > 0):
@@ -375,6 +408,7 @@ class qLogNoisyExpectedImprovement(_MCAcquisition):
         nat.check(rc, "qLogNEI baseline")
         self.baseline_jitter = jit.value
         self._Vb64, self._Vb32, self._VbT64, self._VbT32 = m.baseline_operands(self._Xb, self.precision)
+        self._joint = None  # per-level operands of joint sampling, built on first use
         self._Z = {}
 
     @property
@@ -396,6 +430,49 @@ class qLogNoisyExpectedImprovement(_MCAcquisition):
             self._init_baseline(self._X_baseline, X_pending)
         finally:
             self.prune_baseline = saved
+
+    def _sampling_flags(self) -> int:
+        if self.cache_root:
+            return 0
+        return nat.BGB_FLAG_JOINT_SAMPLING | nat.BGB_FLAG_UNCACHED_ROOT
+
+    def _call_struct(self, q: int, flags: int | None = None):
+        return super()._call_struct(q, self._sampling_flags() if flags is None else flags)
+
+    def _set_joint_operands(self, acq: nat.BgbAcq) -> None:
+        """Per-jitter-level inverse roots of the baseline covariance and incumbents
+        (bgb_qlognei_joint_levels), computed once per baseline."""
+        if self._joint is None:
+            m, r, S, dev = self.model, self.r, self.sampler.num_samples, self.device
+            Lb_inv_lv = torch.empty(nat.JOINT_LEVELS, r, r, dtype=torch.float64, device=dev)
+            best_f_lv = torch.empty(nat.JOINT_LEVELS, S, dtype=torch.float64, device=dev)
+            Zb_dev = self._Zb.to(dev, torch.float64).contiguous()
+            lib = nat.lib()
+            ws = nat.Workspace(dev)
+            wp, wb = ws.get(lib.bgb_qlognei_joint_levels_workspace_bytes(m.n, r, S))
+            gp = m.gp_struct()
+            with torch.cuda.device(dev):
+                rc = lib.bgb_qlognei_joint_levels(ctypes.byref(gp), nat.ptr(m.Linv), nat.ptr(m.alpha),
+                                                  nat.ptr(self._Xb), r, nat.ptr(Zb_dev), S,
+                                                  nat.ptr(Lb_inv_lv), nat.ptr(best_f_lv), wp, wb,
+                                                  nat.stream_handle(dev))
+            nat.check(rc, "qLogNEI joint sampling operands")
+            self._joint = (Lb_inv_lv, best_f_lv)
+        acq.Lb_inv_lv = nat.ptr(self._joint[0])
+        acq.best_f_lv = nat.ptr(self._joint[1])
+
+    def _fall_back(self, Xd: Tensor, need_grad: bool):
+        """The reference's fallback (botorch/acquisition/cached_cholesky.py:143-158): when
+        the low-rank update of the cached root fails for a t-batch of the call (NaN
+        samples or a non-PSD Schur complement), the whole call is sampled again from
+        the joint (r+q)-dim posterior with the cached incumbent, with a warning."""
+        if not self.cache_root:
+            return None
+        warnings.warn("Low-rank cholesky updates failed due NaNs or due to an ill-conditioned "
+                      "covariance matrix. Falling back to standard sampling.", BotorchWarning,
+                      stacklevel=4)
+        acq, ws_bytes = self._call_struct(Xd.shape[1], nat.BGB_FLAG_JOINT_SAMPLING)
+        return self._native_call(Xd, need_grad, acq, ws_bytes)
 
     def _base_samples(self, q: int) -> Tensor:
         """S x (r+q): the (r+q)-dim draw with its first r columns replaced by the baseline draw."""

@@ -44,6 +44,12 @@ struct QBatchArgs {
     double beta_absmax;     // max |beta| (row-scale bound of the float16 adjoint operand)
     int adj_ctas_per_sm;    // adjoint slab split target (0: default)
     float* hmul;            // tensor cores: b*q inverse row scales of the float16 H
+    // joint sampling (the reference's fallback to full joint sampling, and
+    // cache_root=False): psd_safe_cholesky of the whole (r+q) x (r+q) covariance
+    // per t-batch, level t adding j_t (0, then jitter 10^(t-1)) to its diagonal
+    int joint;              // 0: cached root; 1: joint, cached best_f; 2: joint, best_f per level
+    const double* Lb_inv_lv;  // (max_tries+1) x r x r: chol(Sigma_bb + j_t I)^-1, NaN at [0] if it failed
+    const double* best_f_lv;  // (max_tries+1) x S: max over the baseline of the level's samples
 };
 
 // mu, Sigma_qq and Sigma_qb in one pass over V (q <= 8, r <= 4); returns

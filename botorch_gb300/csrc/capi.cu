@@ -84,6 +84,10 @@ int64_t kc_region_elems(const bgb_acq_t* a, int64_t rows) {
     return use_tc(a) ? rows * a->ldl : rows * a->gp.n;
 }
 
+int joint_mode(const bgb_acq_t* a);
+// best_f sets the mixed path converts to float pairs: one, or one per jitter level
+int64_t bf_levels(const bgb_acq_t* a) { return joint_mode(a) == 2 ? 7 : 1; }
+
 // Workspace of one call: the Kc (later H, later the adjoint's slab partials)
 // region, C = V (later D) rows x ldb, P rows x r, the float64 per-batch blocks,
 // the device error word, and for the mixed path the scaled candidates, the
@@ -107,7 +111,7 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
     if (es == sizeof(float)) {
         total += align_up(sizeof(float) * rows * a->gp.d);
         total += align_up(sizeof(float) * (size_t)a->n_samples * (a->r + a->q));
-        total += align_up(sizeof(float) * 2 * (size_t)a->n_samples);
+        total += align_up(sizeof(float) * 2 * (size_t)a->n_samples * bf_levels(a));
         if (tc) total += align_up(sizeof(float) * rows);
     }
     if (ar == nullptr) return total;
@@ -132,10 +136,17 @@ size_t acq_ws_layout(const bgb_acq_t* a, int64_t b, Arena* ar, QBatchArgs* qa, v
     if (es == sizeof(float)) {
         qa->zt = ar->take<float>(rows * a->gp.d);
         qa->z32 = ar->take<float>((int64_t)a->n_samples * (a->r + a->q));
-        qa->bf32 = ar->take<float>(2 * (int64_t)a->n_samples);
+        qa->bf32 = ar->take<float>(2 * (int64_t)a->n_samples * bf_levels(a));
         if (tc) qa->hmul = ar->take<float>(rows);
     }
     return total;
+}
+
+// Sampling of the q new points: 0 cached root, 1 joint sampling with the cached
+// incumbent (the reference's fallback), 2 joint sampling without the cached root.
+int joint_mode(const bgb_acq_t* a) {
+    if (a->r <= 0 || !(a->flags & BGB_FLAG_JOINT_SAMPLING)) return 0;
+    return (a->flags & BGB_FLAG_UNCACHED_ROOT) ? 2 : 1;
 }
 
 void fill_qargs(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa) {
@@ -164,6 +175,9 @@ void fill_qargs(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa) 
     qa->best_f = a->best_f;
     qa->beta_absmax = a->beta_absmax;
     qa->adj_ctas_per_sm = (a->flags & BGB_FLAG_ADJ_CTAS_MASK) >> BGB_FLAG_ADJ_CTAS_SHIFT;
+    qa->joint = joint_mode(a);
+    qa->Lb_inv_lv = a->Lb_inv_lv;
+    qa->best_f_lv = a->best_f_lv;
 }
 
 int valid_acq(const bgb_acq_t* a) {
@@ -183,6 +197,8 @@ int valid_acq(const bgb_acq_t* a) {
         return 0;
     }
     if (a->r > 0 && (a->X_baseline == nullptr || a->Lb_inv == nullptr)) return 0;
+    if (joint_mode(a) >= 1 && a->Lb_inv_lv == nullptr) return 0;
+    if (joint_mode(a) == 2 && a->best_f_lv == nullptr) return 0;
     return 1;
 }
 

@@ -196,4 +196,59 @@ int bgb_qlognei_baseline(const bgb_gp_t* gp, const double* Linv, const double* a
     return BGB_OK;
 }
 
+size_t bgb_qlognei_joint_levels_workspace_bytes(int64_t n, int32_t r, int32_t S) {
+    return joint_ws(n, r) + align_up(sizeof(double) * r) + 2 * align_up(sizeof(double) * r * r) +
+           bgb_cholesky_workspace_bytes(r) + bgb_tri_inverse_workspace_bytes(r) +
+           align_up(sizeof(double) * (int64_t)S * r);
+}
+
+int bgb_qlognei_joint_levels(const bgb_gp_t* gp, const double* Linv, const double* alpha,
+                             const double* X_baseline, int32_t r, const double* Zb, int32_t S,
+                             double* Lb_inv_lv, double* best_f_lv, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+    if (!valid_gp(gp) || Linv == nullptr || alpha == nullptr || X_baseline == nullptr ||
+        Zb == nullptr || Lb_inv_lv == nullptr || best_f_lv == nullptr || r <= 0 || S <= 0)
+        return BGB_ERR_ARG;
+    if (workspace == nullptr ||
+        workspace_bytes < bgb_qlognei_joint_levels_workspace_bytes(gp->n, r, S))
+        return BGB_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    Arena ar{static_cast<char*>(workspace), workspace_bytes, 0};
+    double* mean = ar.take<double>(r);
+    double* covar = ar.take<double>((int64_t)r * r);
+    double* L = ar.take<double>((int64_t)r * r);
+    void* cws = ar.take<char>(bgb_cholesky_workspace_bytes(r));
+    double* tws = ar.take<double>(bgb_tri_inverse_workspace_bytes(r) / sizeof(double));
+    double* samples = ar.take<double>((int64_t)S * r);
+    int rc = posterior_joint(gp, Linv, alpha, X_baseline, r, mean, covar, &ar, st);
+    if (rc) return rc;
+    constexpr int kLevels = 7;  // plain, then jitter 1e-8 x 10^t for t < 6 (botorch/__init__.py:54)
+    for (int t = 0; t < kLevels; ++t) {
+        const double jit = t == 0 ? 0.0 : 1e-8 * pow(10.0, (double)(t - 1));
+        double* Li = Lb_inv_lv + (int64_t)t * r * r;
+        double* bf = best_f_lv + (int64_t)t * S;
+        rc = copy_matrix_f64(covar, r, L, r, r, r, jit, st);
+        if (rc) return rc;
+        int32_t info = 0;
+        rc = bgb_cholesky(L, r, r, &info, cws, bgb_cholesky_workspace_bytes(r), stream);
+        if (rc == BGB_NOT_PSD) {
+            // all-ones bytes are a NaN pattern: marks the level as failed
+            BGB_CUDA_TRY(cudaMemsetAsync(Li, 0xFF, sizeof(double) * r * r, st));
+            BGB_CUDA_TRY(cudaMemsetAsync(bf, 0xFF, sizeof(double) * S, st));
+            continue;
+        }
+        if (rc) return rc;
+        rc = copy_matrix_f64(L, r, Li, r, r, r, 0.0, st);
+        if (rc) return rc;
+        rc = tri_inverse_f64(Li, r, r, tws, st);
+        if (rc) return rc;
+        rc = gemm_f64(S, r, r, 1.0, Zb, r, 0, L, r, 1, 0.0, samples, r, KFULL, 0, nullptr, st);
+        if (rc) return rc;
+        row_max_kernel<<<(unsigned)ceil_div(S, 128), 128, 0, st>>>(samples, mean, S, r, bf);
+        BGB_CHECK_LAUNCH();
+    }
+    BGB_CUDA_TRY(cudaStreamSynchronize(st));
+    return BGB_OK;
+}
+
 }  // extern "C"

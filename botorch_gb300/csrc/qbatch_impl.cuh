@@ -517,49 +517,80 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     for (int i = tid; i < q; i += blockDim.x) mu[i] = a.y_mean + sy * a.mu[bidx * q + i];
     for (int p = tid; p < q * q; p += blockDim.x) M[p] = sy2 * a.sig[bidx * q * q + p];
     __syncthreads();
-    // (2) bl = Sigma_qb Lb^-T  (Lq[:, :r]);  Lb_inv lower triangular
-    for (int p = tid; p < q * r; p += blockDim.x) {
-        int i = p / r, k = p % r;
-        double s = 0.0;
-        for (int kk = 0; kk <= k; ++kk) s += sy2 * a.sqb[(bidx * q + i) * r + kk] * a.Lb_inv[k * r + kk];
-        Lq[i * D + k] = s;
-    }
+    // (2)-(4) the q new rows [bl, br] of the Cholesky factor of the joint covariance
+    //   cached root (joint == 0): bl = Sigma_qb Lb^-T, br = psd_safe_cholesky(Sigma_qq - bl bl^T)
+    //   joint sampling: psd_safe_cholesky of the whole (r+q) x (r+q) matrix, blockwise:
+    //   at jitter level t, bl = Sigma_qb L_t^-T with L_t = chol(Sigma_bb + j_t I), and
+    //   br = chol(Sigma_qq + j_t I - bl bl^T); the first level where both succeed
+    __shared__ int s_lv;
+    const double* Lbi = a.Lb_inv;
+    const int nlv = a.joint ? a.max_tries + 1 : 1;
+    if (tid == 0) s_lv = -1;
     __syncthreads();
-    // (3) M = Sigma_qq - bl bl^T
-    for (int p = tid; p < q * q; p += blockDim.x) {
-        int i = p / q, j = p % q;
-        double s = 0.0;
-        for (int k = 0; k < r; ++k) s += Lq[i * D + k] * Lq[j * D + k];
-        M[p] -= s;
-    }
-    __syncthreads();
-    // (4) psd_safe_cholesky(M): plain, then jitter j * 10^i (i < max_tries) for this batch only
-    if (tid == 0) {
-        int status = 0;
-        bool has_nan = false;
-        for (int p = 0; p < q * q; ++p) has_nan |= isnan(M[p]);
-        for (int p = 0; p < q * q; ++p) scr[p] = M[p];
-        int info = has_nan ? 1 : chol_small(scr, q);
-        if (info != 0) {
-            if (has_nan) {
-                status = BGB_NAN;
-            } else {
-                double jprev = 0.0;
-                status = BGB_NOT_PSD;
-                for (int t = 0; t < a.max_tries; ++t) {
-                    double jnew = a.jitter * pow(10.0, (double)t);
-                    for (int i = 0; i < q; ++i) M[i * q + i] += jnew - jprev;
-                    jprev = jnew;
-                    for (int p = 0; p < q * q; ++p) scr[p] = M[p];
-                    if (chol_small(scr, q) == 0) { status = 0; break; }
-                }
+    for (int lv = 0; lv < nlv; ++lv) {
+        if (a.joint) {
+            Lbi = a.Lb_inv_lv + (int64_t)lv * r * r;
+            if (r > 0 && isnan(Lbi[0])) continue;  // chol(Sigma_bb + j_t I) failed at this level
+            if (lv > 0) {  // M holds the previous level's attempt
+                for (int p = tid; p < q * q; p += blockDim.x) M[p] = sy2 * a.sig[bidx * q * q + p];
+                __syncthreads();
             }
         }
-        for (int i = 0; i < q; ++i)
-            for (int j = 0; j < q; ++j) Lq[i * D + r + j] = (j <= i) ? scr[i * q + j] : 0.0;
-        s_status = status;
+        const double jit = (a.joint && lv > 0) ? a.jitter * pow(10.0, (double)(lv - 1)) : 0.0;
+        // (2) bl = Sigma_qb Lb^-T  (Lq[:, :r]);  Lb_inv lower triangular
+        for (int p = tid; p < q * r; p += blockDim.x) {
+            int i = p / r, k = p % r;
+            double s = 0.0;
+            for (int kk = 0; kk <= k; ++kk) s += sy2 * a.sqb[(bidx * q + i) * r + kk] * Lbi[k * r + kk];
+            Lq[i * D + k] = s;
+        }
+        __syncthreads();
+        // (3) M = Sigma_qq (+ j_t I) - bl bl^T
+        for (int p = tid; p < q * q; p += blockDim.x) {
+            int i = p / q, j = p % q;
+            double s = 0.0;
+            for (int k = 0; k < r; ++k) s += Lq[i * D + k] * Lq[j * D + k];
+            M[p] += (i == j ? jit : 0.0) - s;
+        }
+        __syncthreads();
+        // (4) cached root: psd_safe_cholesky(M), plain then jitter j * 10^i (i < max_tries)
+        // for this batch only; joint: the plain factorisation at this level
+        if (tid == 0) {
+            int status = 0;
+            bool has_nan = false;
+            for (int p = 0; p < q * q; ++p) has_nan |= isnan(M[p]);
+            for (int p = 0; p < q * q; ++p) scr[p] = M[p];
+            int info = has_nan ? 1 : chol_small(scr, q);
+            if (info != 0) {
+                if (has_nan) {
+                    status = BGB_NAN;
+                } else {
+                    double jprev = 0.0;
+                    status = BGB_NOT_PSD;
+                    for (int t = 0; t < (a.joint ? 0 : a.max_tries); ++t) {
+                        double jnew = a.jitter * pow(10.0, (double)t);
+                        for (int i = 0; i < q; ++i) M[i * q + i] += jnew - jprev;
+                        jprev = jnew;
+                        for (int p = 0; p < q * q; ++p) scr[p] = M[p];
+                        if (chol_small(scr, q) == 0) { status = 0; break; }
+                    }
+                }
+            }
+            for (int i = 0; i < q; ++i)
+                for (int j = 0; j < q; ++j) Lq[i * D + r + j] = (j <= i) ? scr[i * q + j] : 0.0;
+            s_status = status;
+            if (status == 0) s_lv = lv;
+        }
+        __syncthreads();
+        if (s_status != BGB_NOT_PSD) break;  // factorised, or NaN (no jitter helps)
     }
-    __syncthreads();
+    if (a.joint && s_lv < 0 && s_status == 0) {  // every level's chol(Sigma_bb + j_t I) failed
+        __syncthreads();
+        if (tid == 0) s_status = BGB_NOT_PSD;
+        __syncthreads();
+    }
+    if (a.joint && s_lv >= 0) Lbi = a.Lb_inv_lv + (int64_t)s_lv * r * r;
+    const double* best_f = (a.joint == 2 && s_lv >= 0) ? a.best_f_lv + (int64_t)s_lv * S : a.best_f;
     if (s_status != 0) {
         if (tid == 0) {
             a.status[bidx] = s_status;
@@ -578,7 +609,7 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     int local_bad = 0;
     for (int s = tid; s < S; s += blockDim.x) {
         const double* z = a.Z + (int64_t)s * D;
-        const double bf = qei ? a.best_f[0] : a.best_f[s];
+        const double bf = qei ? a.best_f[0] : best_f[s];
         double li[kMaxQ];
         double Mx = -INFINITY;
         for (int i = 0; i < q; ++i) {
@@ -663,7 +694,7 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
         for (int ls = tid; ls < sc; ls += blockDim.x) {
             const int s = s0 + ls;
             const double* z = a.Z + (int64_t)s * D;
-            const double bf = qei ? a.best_f[0] : a.best_f[s];
+            const double bf = qei ? a.best_f[0] : best_f[s];
             double u[kMaxQ], li[kMaxQ], g[kMaxQ];
             double Mx = -INFINITY;
             for (int i = 0; i < q; ++i) {
@@ -762,7 +793,7 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
     for (int p = tid; p < q * r; p += blockDim.x) {
         const int i = p / r, kp = p % r;
         double s = 0.0;
-        for (int k = kp; k < r; ++k) s += dLq[i * D + k] * a.Lb_inv[k * r + kp];
+        for (int k = kp; k < r; ++k) s += dLq[i * D + k] * Lbi[k * r + kp];
         a.gqb[(bidx * q + i) * r + kp] = sy2 * s;
     }
     for (int p = tid; p < q * q; p += blockDim.x) a.gqq[bidx * q * q + p] = sy2 * gA[p];
@@ -907,36 +938,64 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     }
     for (int p = tid; p < q * q; p += kBsThreads) M[p] = sy2 * a.sig[bidx * q * q + p];
     __syncthreads();
-    // (2) bl = Sigma_qb Lb^-T (Lb^-1 lower triangular)
-    for (int p = tid; p < q * r; p += kBsThreads) {
-        const int i = p / r, k = p % r;
-        double acc = 0.0;
-        for (int kk = 0; kk <= k; ++kk) acc += sy2 * a.sqb[(bidx * q + i) * r + kk] * a.Lb_inv[k * r + kk];
-        Lq[i * D + k] = acc;
-    }
+    // (2)-(4) the q new rows [bl, br] of the Cholesky factor of the joint covariance:
+    // cached root (joint == 0) or joint sampling level by level, as in the float64 step
+    __shared__ int s_lv;
+    const double* Lbi = a.Lb_inv;
+    const int nlv = a.joint ? a.max_tries + 1 : 1;
+    if (tid == 0) s_lv = -1;
     __syncthreads();
-    // (3) M = Sigma_qq - bl bl^T
-    for (int p = tid; p < q * q; p += kBsThreads) {
-        const int i = p / q, j = p % q;
-        double acc = 0.0;
-        for (int k = 0; k < r; ++k) acc += Lq[i * D + k] * Lq[j * D + k];
-        M[p] -= acc;
-    }
-    __syncthreads();
-    // (4) br = psd_safe_cholesky(M) for this t-batch (warp 0)
-    if (warp == 0) {
-        const int st = psd_chol_warp(M, scr, q, a.max_tries, a.jitter, lane);
-        for (int p = lane; p < q * q; p += 32) {
-            const int i = p / q, j = p % q;
-            Lq[i * D + r + j] = (j <= i) ? scr[p] : 0.0;
+    for (int lv = 0; lv < nlv; ++lv) {
+        if (a.joint) {
+            Lbi = a.Lb_inv_lv + (int64_t)lv * r * r;
+            if (r > 0 && isnan(Lbi[0])) continue;  // chol(Sigma_bb + j_t I) failed at this level
+            if (lv > 0) {  // M holds the previous level's attempt
+                for (int p = tid; p < q * q; p += kBsThreads) M[p] = sy2 * a.sig[bidx * q * q + p];
+                __syncthreads();
+            }
         }
-        if (lane == 0) s_status = st;
+        const double jit = (a.joint && lv > 0) ? a.jitter * pow(10.0, (double)(lv - 1)) : 0.0;
+        // (2) bl = Sigma_qb Lb^-T (Lb^-1 lower triangular)
+        for (int p = tid; p < q * r; p += kBsThreads) {
+            const int i = p / r, k = p % r;
+            double acc = 0.0;
+            for (int kk = 0; kk <= k; ++kk) acc += sy2 * a.sqb[(bidx * q + i) * r + kk] * Lbi[k * r + kk];
+            Lq[i * D + k] = acc;
+        }
+        __syncthreads();
+        // (3) M = Sigma_qq (+ j_t I) - bl bl^T
+        for (int p = tid; p < q * q; p += kBsThreads) {
+            const int i = p / q, j = p % q;
+            double acc = 0.0;
+            for (int k = 0; k < r; ++k) acc += Lq[i * D + k] * Lq[j * D + k];
+            M[p] += (i == j ? jit : 0.0) - acc;
+        }
+        __syncthreads();
+        // (4) br = psd_safe_cholesky(M) for this t-batch (warp 0); joint: plain at this level
+        if (warp == 0) {
+            const int st = psd_chol_warp(M, scr, q, a.joint ? 0 : a.max_tries, a.jitter, lane);
+            for (int p = lane; p < q * q; p += 32) {
+                const int i = p / q, j = p % q;
+                Lq[i * D + r + j] = (j <= i) ? scr[p] : 0.0;
+            }
+            if (lane == 0) {
+                s_status = st;
+                if (st == 0) s_lv = lv;
+            }
+        }
+        __syncthreads();
+        if (s_status != BGB_NOT_PSD) break;  // factorised, or NaN (no jitter helps)
     }
-    __syncthreads();
+    if (a.joint && s_lv < 0 && s_status == 0) {  // every level's chol(Sigma_bb + j_t I) failed
+        __syncthreads();
+        if (tid == 0) s_status = BGB_NOT_PSD;
+        __syncthreads();
+    }
     if (s_status != 0) {
         fail(s_status);
         return;
     }
+    if (a.joint) Lbi = a.Lb_inv_lv + (int64_t)s_lv * r * r;
     for (int p = tid; p < D * QMAX; p += kBsThreads) {
         const int k = p / QMAX, i = p % QMAX;
         Lf[p] = (i < q) ? (float)Lq[i * D + k] : 0.f;
@@ -947,7 +1006,8 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     const float log_tau = (float)log(a.tau_relu);
     const float taum = (float)a.tau_max, inv_taum = (float)(1.0 / a.tau_max);
     const float* __restrict__ z32 = a.z32;
-    const float* __restrict__ bf32 = a.bf32;
+    // best_f per sample as float pairs: per jitter level for cache_root=False
+    const float* __restrict__ bf32 = a.joint == 2 ? a.bf32 + 2 * (int64_t)s_lv * S : a.bf32;
     // (5) forward: t_s per sample
     int local_bad = 0;
     for (int s = tid; s < S; s += kBsThreads) {
@@ -1144,7 +1204,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     for (int p = tid; p < q * r; p += kBsThreads) {
         const int i = p / r, kp = p % r;
         double acc2 = 0.0;
-        for (int k = kp; k < r; ++k) acc2 += dLq[i * D + k] * a.Lb_inv[k * r + kp];
+        for (int k = kp; k < r; ++k) acc2 += dLq[i * D + k] * Lbi[k * r + kp];
         a.gqb[(bidx * q + i) * r + kp] = sy2 * acc2;
     }
     for (int p = tid; p < q * q; p += kBsThreads) a.gqq[bidx * q * q + p] = sy2 * gA[p];
@@ -1170,12 +1230,13 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
 }
 
 #if defined(BGB_QB_STEP)
+// Z in float32, and nbf best_f values (S, or S per jitter level) as float pairs.
 __global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
-                                    const double* __restrict__ best_f, int S, int qei,
+                                    const double* __restrict__ best_f, int64_t nbf, int qei,
                                     float* __restrict__ z32, float* __restrict__ bf32) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx < nz) z32[idx] = (float)Z[idx];
-    if (idx < S) {
+    if (idx < nbf) {
         const double bf = best_f[qei ? 0 : idx];
         const float h = (float)bf;
         bf32[2 * idx] = h;
@@ -1610,9 +1671,10 @@ int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bo
     const size_t smem = batch_step_f32_smem_bytes(a.q, a.r, a.S);
     if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
     const int64_t nz = (int64_t)a.S * (a.r + a.q);
-    const int64_t np = nz > a.S ? nz : a.S;
+    const int64_t nbf = a.joint == 2 ? (int64_t)a.S * (a.max_tries + 1) : a.S;
+    const int64_t np = nz > nbf ? nz : nbf;
     prep_samples_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, stream>>>(
-        a.Z, nz, a.best_f, a.S, a.acqf == BGB_ACQF_QEI, a.z32, a.bf32);
+        a.Z, nz, a.joint == 2 ? a.best_f_lv : a.best_f, nbf, a.acqf == BGB_ACQF_QEI, a.z32, a.bf32);
     BGB_CHECK_LAUNCH();
 #define BGB_BS(QM)                                                                               \
     do {                                                                                        \

@@ -20,3 +20,8 @@ class NotPSDError(RuntimeError):
 
 class NanError(RuntimeError):
     """NaN input to a Cholesky or non-finite posterior samples."""
+
+
+class BotorchWarning(Warning):
+    """Base warning (botorch/exceptions/warnings.py:12); issued, as in the reference, when
+    the cached-root sampling of qLogNEI falls back to joint sampling."""

@@ -60,6 +60,18 @@ extern "C" {
  * training points into slabs (0: 16); a schedule knob for autotuners */
 #define BGB_FLAG_ADJ_CTAS_SHIFT 8
 #define BGB_FLAG_ADJ_CTAS_MASK 0xFF00
+/* qLogNEI sampling without the cached root (needs Lb_inv_lv, from
+ * bgb_qlognei_joint_levels): the q new rows of the Cholesky factor of the whole
+ * (r+q) x (r+q) joint covariance, psd_safe_cholesky jitter applied to the whole
+ * diagonal per t-batch.
+ * JOINT_SAMPLING: best_f stays the cached baseline incumbent -- the reference's
+ *   fallback to standard sampling when the low-rank update fails
+ *   (botorch/acquisition/cached_cholesky.py:143-158);
+ * UNCACHED_ROOT (with JOINT_SAMPLING): best_f from the joint draw's own baseline
+ *   samples (needs best_f_lv) -- qLogNoisyExpectedImprovement(cache_root=False)
+ *   (botorch/acquisition/logei.py:543-553, acquisition/utils.py:97-141). */
+#define BGB_FLAG_JOINT_SAMPLING 2
+#define BGB_FLAG_UNCACHED_ROOT 4
 
 /* An exact GP with fixed hyperparameters (SingleTaskGP, gp_regression.py:108-214).
  * Hyperparameters live in the standardised outcome space; y_mean / y_std
@@ -126,6 +138,9 @@ typedef struct bgb_acq {
     const double* best_f;    /* S values (qLogNEI) or 1 value (qEI) */
     double tau_relu;         /* logei.py:67 */
     double tau_max;          /* logei.py:68 */
+    const double* Lb_inv_lv; /* 7 x r x r (BGB_FLAG_JOINT_SAMPLING): per jitter level, from
+                                bgb_qlognei_joint_levels */
+    const double* best_f_lv; /* 7 x S (BGB_FLAG_UNCACHED_ROOT) */
 } bgb_acq_t;
 
 /* Library version (major * 10000 + minor * 100 + patch). */
@@ -261,6 +276,23 @@ int bgb_qlognei_baseline(const bgb_gp_t* gp, const double* Linv, const double* a
                          double* jitter_host, void* workspace, size_t workspace_bytes,
                          void* stream);
 size_t bgb_qlognei_baseline_workspace_bytes(int64_t n, int32_t r, int32_t S);
+
+/* Joint-sampling operands of qLogNEI (BGB_FLAG_JOINT_SAMPLING, BGB_FLAG_UNCACHED_ROOT):
+ * the untransformed baseline posterior (mean_b, Sigma_bb) at X_baseline (r x d)
+ * and, for each of the 7 jitter levels t of psd_safe_cholesky (total jitter 0,
+ * then 1e-8 x 10^(t-1)), L_t = chol(Sigma_bb + j_t I), Lb_inv_lv[t] = L_t^-1
+ * (r x r) and best_f_lv[t][s] = max_j (mean_b + Zb L_t^T)[s][j] (S values). A
+ * level whose factorisation fails has NaN in Lb_inv_lv[t][0] and in best_f_lv[t].
+ * The levels are those the reference's psd_safe_cholesky tries on the joint
+ * covariance inside MultivariateNormal.rsample, reached from
+ * get_posterior_samples (botorch/acquisition/acquisition.py:128-138) on the
+ * fallback path of cached_cholesky.py:143-158 and for cache_root=False
+ * (logei.py:543-553). Synchronises. */
+int bgb_qlognei_joint_levels(const bgb_gp_t* gp, const double* Linv, const double* alpha,
+                             const double* X_baseline, int32_t r, const double* Zb, int32_t S,
+                             double* Lb_inv_lv, double* best_f_lv, void* workspace,
+                             size_t workspace_bytes, void* stream);
+size_t bgb_qlognei_joint_levels_workspace_bytes(int64_t n, int32_t r, int32_t S);
 
 /* Workspace for bgb_acq_forward / bgb_acq_forward_backward / bgb_posterior at b t-batches. */
 size_t bgb_acq_workspace_bytes(const bgb_acq_t* acq, int64_t b);

@@ -92,6 +92,7 @@ def test_header_constants_match_the_bindings():
     defs = dict(re.findall(r"#define (BGB_[A-Z0-9_]+)\s+(\S[^/\n]*?)\s*(?:/\*.*)?$", text, flags=re.M))
     for name in ("BGB_OK", "BGB_NOT_PSD", "BGB_NAN", "BGB_DEVICE_TIMEOUT", "BGB_ERR_ARG",
                  "BGB_ERR_WORKSPACE", "BGB_ERR_CUDA", "BGB_ERR_UNSUPPORTED", "BGB_ERR_SCRATCH_LIMIT",
-                 "BGB_FLAG_SIMT", "BGB_FLAG_ADJ_CTAS_SHIFT", "BGB_FLAG_ADJ_CTAS_MASK"):
+                 "BGB_FLAG_SIMT", "BGB_FLAG_ADJ_CTAS_SHIFT", "BGB_FLAG_ADJ_CTAS_MASK",
+                 "BGB_FLAG_JOINT_SAMPLING", "BGB_FLAG_UNCACHED_ROOT"):
         assert int(eval(defs[name])) == getattr(_native, name), name
     assert eval(defs["BGB_NOALLOC_SCRATCH_BYTES"].replace("(size_t)", "")) == _native.BGB_NOALLOC_SCRATCH_BYTES
