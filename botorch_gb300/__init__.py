@@ -10,8 +10,8 @@ from botorch_gb300.acquisition import (qExpectedImprovement, qLogNoisyExpectedIm
                                        prune_inferior_points)
 from botorch_gb300.exceptions import BotorchWarning, NanError, NotPSDError, UnsupportedError
 from botorch_gb300.gp_regression import GPyTorchPosterior, SingleTaskGP, Standardize
-from botorch_gb300.kernels import (ConstantMean, GaussianLikelihood, MaternKernel, RBFKernel,
-                                   ScaleKernel)
+from botorch_gb300.kernels import (ConstantMean, GammaPrior, GaussianLikelihood, LogNormalPrior,
+                                   MaternKernel, RBFKernel, ScaleKernel)
 from botorch_gb300.sampling import SobolQMCNormalSampler, draw_sobol_normal_samples
 
 __all__ = [
@@ -19,4 +19,5 @@ __all__ = [
     "qLogNoisyExpectedImprovement", "prune_inferior_points", "SobolQMCNormalSampler",
     "draw_sobol_normal_samples", "MaternKernel", "RBFKernel", "ScaleKernel", "GaussianLikelihood",
     "ConstantMean", "NotPSDError", "NanError", "UnsupportedError", "BotorchWarning",
+    "LogNormalPrior", "GammaPrior",
 ]

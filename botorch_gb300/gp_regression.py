@@ -18,8 +18,8 @@ from torch import Tensor
 
 from botorch_gb300 import _native as nat
 from botorch_gb300.exceptions import UnsupportedError
-from botorch_gb300.kernels import (ConstantMean, GaussianLikelihood, RBFKernel,
-                                   unpack_covar_module)
+from botorch_gb300.kernels import (ConstantMean, GaussianLikelihood, default_covar_module,
+                                   default_likelihood, unpack_covar_module)
 
 _DEFAULT = object()
 
@@ -107,8 +107,10 @@ class SingleTaskGP:
             raise UnsupportedError("botorch_gb300 runs on CUDA devices only")
         n, d = train_X.shape
         self.n, self.d = n, d
-        self.likelihood = likelihood if likelihood is not None else GaussianLikelihood()
-        self.covar_module = covar_module if covar_module is not None else RBFKernel(ard_num_dims=d)
+        # the reference's defaults: LogNormal-prior noise and a dimension-scaled-prior RBF
+        # kernel (botorch/models/gp_regression.py:173-201)
+        self.likelihood = likelihood if likelihood is not None else default_likelihood()
+        self.covar_module = covar_module if covar_module is not None else default_covar_module(d)
         self.mean_module = mean_module if mean_module is not None else ConstantMean()
         kind, ls, outputscale = unpack_covar_module(self.covar_module)
         if ls.numel() not in (1, d):
