@@ -110,6 +110,7 @@ _SIGNATURES = {
     "bgb_qlognei_joint_levels_workspace_bytes": (c_size, [c_i64, c_i32, c_i32]),
     "bgb_posterior": (c_i32, [ctypes.POINTER(BgbAcq), c_vp, c_i64, c_vp, c_vp, c_vp, c_size,
                               c_vp]),
+    "bgb_mvn_rsample": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "bgb_acq_workspace_bytes": (c_size, [ctypes.POINTER(BgbAcq), c_i64]),
     "bgb_acq_forward": (c_i32, [ctypes.POINTER(BgbAcq), c_vp, c_i64, c_vp, c_vp, c_vp, c_size,
                                 c_vp]),

@@ -50,7 +50,8 @@ class Standardize:
 
 
 class GPyTorchPosterior:
-    """Posterior over ``batch x q`` points: mean, variance, covariance (posteriors/gpytorch.py)."""
+    """Posterior over ``batch x q`` points: mean, variance, covariance and reparameterised
+    samples (botorch/posteriors/gpytorch.py:33-127)."""
 
     def __init__(self, mean: Tensor, covariance: Tensor) -> None:
         self._mean = mean            # batch x q
@@ -69,15 +70,64 @@ class GPyTorchPosterior:
         return self._covar
 
     @property
+    def device(self) -> torch.device:
+        return self._mean.device
+
+    @property
+    def dtype(self) -> torch.dtype:
+        return self._mean.dtype
+
+    @property
     def base_sample_shape(self) -> torch.Size:
-        return self._mean.shape
+        return self._mean.shape + torch.Size([1])
 
     @property
     def batch_range(self) -> tuple[int, int]:
-        return (0, -1)
+        return (0, -2)
 
     def _extended_shape(self, sample_shape: torch.Size = torch.Size()) -> torch.Size:  # noqa: B008
         return sample_shape + self._mean.shape + torch.Size([1])
+
+    def rsample_from_base_samples(self, sample_shape: torch.Size, base_samples: Tensor) -> Tensor:
+        """``sample_shape x batch x q x 1`` samples mean + L z, L = psd_safe_cholesky of each
+        batch member's covariance (botorch/posteriors/gpytorch.py:86-127, gpytorch
+        MultivariateNormal.rsample), computed by ``bgb_mvn_rsample``. ``base_samples``:
+        ``sample_shape x (1 ...) x q x 1`` (batch dimensions collapsed to 1, as the
+        reference's QMC samplers draw them) or ``sample_shape x q x 1``."""
+        sample_shape = torch.Size(sample_shape)
+        if base_samples.shape[: len(sample_shape)] != sample_shape:
+            raise RuntimeError("sample_shape disagrees with shape of base_samples.")
+        q = self._mean.shape[-1]
+        batch_shape = self._mean.shape[:-1]
+        rest = base_samples.shape[len(sample_shape):]
+        if rest[-2:] != torch.Size([q, 1]) or any(s != 1 for s in rest[:-2]):
+            raise UnsupportedError("base samples must be sample_shape x (1 ...) x q x 1: the same "
+                                   "base samples for every batch member")
+        S = int(sample_shape.numel())
+        b = int(batch_shape.numel())
+        dev = self._mean.device
+        Z = base_samples.detach().reshape(S, q).to(dev, torch.float64).contiguous()
+        mean = self._mean.detach().reshape(b, q).to(torch.float64).contiguous()
+        cov = self._covar.detach().reshape(b, q, q).to(torch.float64).contiguous()
+        out = torch.empty(S, b, q, dtype=torch.float64, device=dev)
+        status = torch.empty(b, dtype=torch.int32, device=dev)
+        lib = nat.lib()
+        with torch.cuda.device(dev):
+            rc = lib.bgb_mvn_rsample(nat.ptr(mean), nat.ptr(cov), b, q, nat.ptr(Z), S, 6,
+                                     nat.ptr(out), nat.ptr(status), nat.stream_handle(dev))
+        nat.check(rc, "posterior samples")
+        worst = int(status.max().item()) if b > 0 else 0
+        if worst != nat.BGB_OK:
+            nat.check(worst, "posterior samples (psd_safe_cholesky)")
+        return out.reshape(*sample_shape, *batch_shape, q, 1).to(self._mean.dtype)
+
+    def rsample(self, sample_shape: torch.Size | None = None) -> Tensor:
+        """Samples from i.i.d. standard normal base samples (torch.randn on the device)."""
+        sample_shape = torch.Size([1]) if sample_shape is None else torch.Size(sample_shape)
+        q = self._mean.shape[-1]
+        z = torch.randn(*sample_shape, *([1] * (self._mean.dim() - 1)), q, 1, dtype=torch.float64,
+                        device=self._mean.device)
+        return self.rsample_from_base_samples(sample_shape, z)
 
 
 class SingleTaskGP:
@@ -293,8 +343,8 @@ class SingleTaskGP:
         """
         if output_indices not in (None, [0]) or posterior_transform is not None:
             raise UnsupportedError("output_indices / posterior_transform are not supported")
-        if observation_noise is not False:
-            raise UnsupportedError("observation_noise is not supported")
+        if observation_noise is not False and observation_noise is not True:
+            raise UnsupportedError("observation_noise must be a bool (a noise tensor is not supported)")
         squeeze = X.dim() == 2
         Xb = X.unsqueeze(0) if squeeze else X
         batch_shape = Xb.shape[:-2]
@@ -311,6 +361,10 @@ class SingleTaskGP:
             rc = lib.bgb_posterior(ctypes.byref(acq), nat.ptr(Xf), b, nat.ptr(mean), nat.ptr(cov),
                                    wp, wb, nat.stream_handle(self.device))
         nat.check(rc, "posterior")
+        if observation_noise:
+            # the likelihood's noise on the diagonal, then the outcome untransform
+            # (gpytorch likelihood(mvn) followed by Standardize.untransform_posterior)
+            cov.diagonal(dim1=-2, dim2=-1).add_(self.noise * self.y_std * self.y_std)
         mean = mean.reshape(*batch_shape, q)
         cov = cov.reshape(*batch_shape, q, q)
         if squeeze:

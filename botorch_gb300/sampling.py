@@ -49,6 +49,19 @@ class SobolQMCNormalSampler:
     def num_samples(self) -> int:
         return int(self.sample_shape[0])
 
+    def forward(self, posterior) -> Tensor:
+        """Samples ``sample_shape x batch x q x 1`` from the posterior with this sampler's
+        base samples (botorch/sampling/normal.py:34-50): one q-dimensional Sobol draw,
+        shared by every batch member (the batch dimensions of the base sample shape
+        collapsed, botorch/sampling/normal.py:182-213)."""
+        q = posterior.base_sample_shape[-2]
+        nbatch = len(posterior.base_sample_shape) - 2
+        base = self.base_samples(q).to(posterior.device).reshape(
+            self.num_samples, *([1] * nbatch), q, 1)
+        return posterior.rsample_from_base_samples(self.sample_shape, base)
+
+    __call__ = forward
+
     def base_samples(self, dim: int) -> Tensor:
         """S x dim base samples of this sampler (host, float64), cached per dim."""
         if dim > SobolEngine.MAXDIM:

@@ -294,6 +294,19 @@ int bgb_qlognei_joint_levels(const bgb_gp_t* gp, const double* Linv, const doubl
                              size_t workspace_bytes, void* stream);
 size_t bgb_qlognei_joint_levels_workspace_bytes(int64_t n, int32_t r, int32_t S);
 
+/* Reparameterised samples of the batched posterior MVN (float64): per batch member
+ * L = psd_safe_cholesky(covar[b]) (jitter 1e-8 x 10^t for t < max_tries, this
+ * member only) and samples[s][b][i] = mean[b][i] + sum_j L[i][j] Z[s][j], for
+ * mean (b x q), covar (b x q x q), base samples Z (S x q, shared by every member)
+ * and samples (S x b x q). status (b): 0, BGB_NOT_PSD or BGB_NAN (samples NaN
+ * there). q <= 64 (BGB_ERR_UNSUPPORTED above). Replaces
+ * GPyTorchPosterior.rsample_from_base_samples (botorch/posteriors/gpytorch.py:86-127;
+ * gpytorch MultivariateNormal.rsample) as called by MCSampler.forward
+ * (botorch/sampling/normal.py:34-50). */
+int bgb_mvn_rsample(const double* mean, const double* covar, int64_t b, int32_t q,
+                    const double* Z, int32_t S, int32_t max_tries, double* samples,
+                    int32_t* status, void* stream);
+
 /* Workspace for bgb_acq_forward / bgb_acq_forward_backward / bgb_posterior at b t-batches. */
 size_t bgb_acq_workspace_bytes(const bgb_acq_t* acq, int64_t b);
 
