@@ -342,34 +342,53 @@ def _lbfgsb_rc():
     return rc
 
 
-def _per_restart_rc(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape, maxiter: int,
-                    options: dict, use_graph: bool, rc):
-    """Each restart's own L-BFGS-B through scipy's reverse-communication routine, all
-    restarts that need f and g evaluated in one call per round, on this thread (the
-    reference's batched driver, botorch/optim/batched_lbfgs_b.py:169-636, does the
-    same). Returns per-restart results and the rounds."""
-    b, q, d = shape
-    lo_r, hi_r = np.tile(lo, q), np.tile(hi, q)
-    opts = {**options, "maxiter": maxiter}
-    states = [_RCRestart(*rc, x0[i], lo_r, hi_r, opts) for i in range(b)]
-    rounds = _RestartRounds(acqf, shape, use_graph)
+def batched_lbfgsb(fg_batched, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, options: dict,
+                   rc=None) -> list[dict]:
+    """Independent L-BFGS-B runs, one per row of x0 (b x n), through scipy's
+    reverse-communication routine: every round, the rows that ask for f and g are
+    evaluated in one call ``fg_batched(X_rows, rows) -> (f, g)`` (X_rows k x n).
+    The semantics of the reference's batched driver ``fmin_l_bfgs_b_batched``
+    (botorch/optim/batched_lbfgs_b.py:169-636); per row, the same iterates as
+    scipy's ``minimize(method="L-BFGS-B")``. Needs the routine (``_lbfgsb_rc()``)."""
+    rc = rc if rc is not None else _lbfgsb_rc()
+    if rc is None:
+        raise RuntimeError("scipy's reverse-communication L-BFGS-B (scipy >= 1.15) is not available")
+    b = x0.shape[0]
+    states = [_RCRestart(*rc, x0[i], lo, hi, options) for i in range(b)]
     active = [i for i in range(b) if states[i].advance()]
     while active:
         for i in active:
             if np.isnan(states[i].x).any():
                 raise RuntimeError(f"{int(np.isnan(states[i].x).sum())} elements of x are NaN")
-            rounds.host_x.numpy()[i].reshape(-1)[:] = states[i].x
+        f, g = fg_batched(np.stack([states[i].x for i in active]), active)
+        for k, i in enumerate(active):
+            gi = np.array(g[k], dtype=np.float64)
+            if np.isnan(gi).any():
+                raise RuntimeError(f"{int(np.isnan(gi).sum())} elements of the gradient are NaN")
+            states[i].f, states[i].g = float(f[k]), gi
+            states[i].nfev += 1
+        active = [i for i in active if states[i].advance()]
+    return [s.result() for s in states]
+
+
+def _per_restart_rc(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape, maxiter: int,
+                    options: dict, use_graph: bool, rc):
+    """Each restart's own L-BFGS-B (``batched_lbfgsb``), all restarts that need f and g
+    evaluated in one acquisition call per round, on this thread. Returns per-restart
+    results and the rounds."""
+    b, q, d = shape
+    rounds = _RestartRounds(acqf, shape, use_graph)
+
+    def fg(X_rows: np.ndarray, rows: list[int]):
+        for k, i in enumerate(rows):
+            rounds.host_x.numpy()[i].reshape(-1)[:] = X_rows[k]
         rounds._run()
         if rounds.error is not None:
             raise RuntimeError("batched acquisition evaluation failed") from rounds.error
-        for i in active:
-            g = rounds.fg[i].copy()
-            if np.isnan(g).any():
-                raise RuntimeError(f"{int(np.isnan(g).sum())} elements of the gradient are NaN")
-            states[i].f, states[i].g = float(rounds.fv[i]), g
-            states[i].nfev += 1
-        active = [i for i in active if states[i].advance()]
-    return [s.result() for s in states], rounds.calls
+        return rounds.fv[rows], rounds.fg[rows]
+
+    results = batched_lbfgsb(fg, x0, np.tile(lo, q), np.tile(hi, q), {**options, "maxiter": maxiter}, rc)
+    return results, rounds.calls
 
 
 def _per_restart_lbfgsb(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape, maxiter: int,

@@ -131,3 +131,31 @@ def test_per_restart_thread_driver_raises_without_hanging(monkeypatch):
     with pytest.raises(RuntimeError, match="batched acquisition evaluation failed"):
         O.gen_candidates_scipy(torch.rand(5, 2, 2, dtype=torch.float64), _FakeAcqf(5, 2, 2, fail_at=4), 0.0, 1.0,
                                {"maxiter": 50}, use_parallel_mode=True)
+
+
+def test_batched_lbfgsb_reproduces_the_reference_batched_driver():
+    """botorch_gb300.optim.batched_lbfgsb against the reference's fmin_l_bfgs_b_batched
+    (botorch/optim/batched_lbfgs_b.py:169) on the objective of
+    tests/golden/make_lbfgsb_golden.py: the same per-row iterates (bit for bit with the
+    scipy version the fixture was made with, to 1e-10 with another)."""
+    from pathlib import Path
+
+    import numpy as np
+    import pytest
+    import scipy
+
+    from botorch_gb300.optim import _lbfgsb_rc, batched_lbfgsb
+    from tests.golden.make_lbfgsb_golden import fg_batched, problem
+
+    if _lbfgsb_rc() is None:
+        pytest.skip("scipy's reverse-communication L-BFGS-B is not available")
+    fx = np.load(Path(__file__).resolve().parent / "golden" / "lbfgsb_golden.npz")
+    c, w, x0, lo, hi = problem()
+    assert np.array_equal(x0, fx["x0"])
+    res = batched_lbfgsb(lambda X, rows: fg_batched(X, rows, c, w), x0, lo, hi, {"maxiter": 40})
+    xs = np.stack([r["x"] for r in res])
+    nit = np.array([r["nit"] for r in res])
+    if str(fx["scipy_version"]) == scipy.__version__:
+        assert np.array_equal(xs, fx["x"]) and np.array_equal(nit, fx["nit"])
+    else:
+        assert np.allclose(xs, fx["x"], rtol=0, atol=1e-10)
