@@ -431,11 +431,11 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
     """L-BFGS-B from the ``b x q x d`` initial conditions on the box; returns the
     candidates and their acquisition values.
 
-    ``use_parallel_mode`` True (the reference's fast path,
-    botorch/generation/gen.py:226-247): every restart runs its own L-BFGS-B on
-    minus its own value, with one batched evaluation per round. None or False
-    (the default here): one L-BFGS-B on minus the sum of all restarts' values
-    (the reference's aggregated mode, gen.py:249-395)."""
+    ``use_parallel_mode`` None (the default) or True: the reference's fast path
+    (botorch/generation/gen.py:226-247, taken unless use_parallel_mode is False):
+    every restart runs its own L-BFGS-B on minus its own value, with one batched
+    evaluation per round (``batched_lbfgsb``). False: one L-BFGS-B on minus the
+    sum of all restarts' values (the reference's aggregated mode, gen.py:249-395)."""
     from scipy.optimize import minimize
 
     options = dict(options or {})
@@ -445,7 +445,7 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
     lo = torch.as_tensor(lower_bounds, dtype=torch.float64).expand(d).cpu().numpy()
     hi = torch.as_tensor(upper_bounds, dtype=torch.float64).expand(d).cpu().numpy()
     x0 = np.clip(X0.cpu().numpy(), lo, hi).reshape(-1)
-    if use_parallel_mode:
+    if use_parallel_mode is not False:
         v0, _ = acquisition_function.value_and_grad_raw(
             torch.from_numpy(x0.reshape(b, q, d)).to(acquisition_function.device), False)
         f0 = -float(v0.sum())
