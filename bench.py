@@ -157,8 +157,9 @@ def gemm_flops(rows: int, n: int, r: int) -> float:
 
 
 def traffic_from_profiles() -> float | None:
-    """DRAM bytes per GEMM launch at the bench workload, from the committed ncu summary."""
-    f = ROOT / "profiles" / "crosscov_gemm_f16_b1024.md"
+    """DRAM bytes per GEMM launch at the bench workload, from the committed ncu summary
+    of the kernel form the library runs (the two-SM pair)."""
+    f = ROOT / "profiles" / "crosscov_gemm_pair_b1024.md"
     if f.exists():
         for line in f.read_text().splitlines():
             if line.startswith("traffic_bytes_per_launch_b4096:"):
