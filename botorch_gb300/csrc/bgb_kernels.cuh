@@ -38,6 +38,16 @@ int gemm_f64(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int
              int64_t ldc, int kmode, int lower_only, const int* abort_flag, cudaStream_t stream,
              int64_t n_tri = 0);
 
+// gemm_f64 over `batch` equal-shape products, member z at A + z sA, B + z sB, C + z sC.
+int gemm_f64_batched(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                     int64_t sA, int transA, const double* B, int64_t ldb, int64_t sB, int transB,
+                     double beta, double* C, int64_t ldc, int64_t sC, int kmode, int lower_only,
+                     const int* abort_flag, int64_t batch, cudaStream_t stream, int64_t n_tri = 0);
+// y = alpha * A^T x + beta * y (A: m x n row-major, y: n), float64
+int gemv_t_f64(int64_t m, int64_t n, double alpha, const double* A, int64_t lda, const double* x,
+               double beta, double* y, cudaStream_t stream);
+int64_t tri_inverse_ws_doubles(int64_t n);
+
 // y = alpha * A x + beta * y (A: m x n row-major), float64
 int gemv_f64(int64_t m, int64_t n, double alpha, const double* A, int64_t lda, const double* x,
              double beta, double* y, cudaStream_t stream);

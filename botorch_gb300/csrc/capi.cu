@@ -469,8 +469,7 @@ int bgb_psd_safe_cholesky(const double* A, int64_t n, int64_t lda, double* L, in
 }
 
 size_t bgb_tri_inverse_workspace_bytes(int64_t n) {
-    const int64_t nb = ceil_div(n, 64);
-    return align_up(sizeof(double) * (nb * 64 * 64 + 64 * n));
+    return align_up(sizeof(double) * (size_t)tri_inverse_ws_doubles(n));
 }
 
 int bgb_tri_inverse(double* L, int64_t n, int64_t lda, void* workspace, size_t workspace_bytes,
@@ -523,7 +522,7 @@ int bgb_gp_fit(const bgb_gp_t* gp, const double* y, double noise, int32_t max_tr
     BGB_CHECK_LAUNCH();
     rc = gemv_f64(n, n, 1.0, Linv, n, yc, 0.0, t, st);
     if (rc) return rc;
-    rc = gemm_f64(n, 1, n, 1.0, Linv, n, 1, t, 1, 0, 0.0, alpha, 1, KFULL, 0, nullptr, st);
+    rc = gemv_t_f64(n, n, 1.0, Linv, n, t, 0.0, alpha, st);
     if (rc) return rc;
     if (jit > 0.0) {
         rc = launch_kernel_matrix<double, double, double>(gp->train_X, n, gp->train_X, n, gp->d,
@@ -537,10 +536,10 @@ int bgb_gp_fit(const bgb_gp_t* gp, const double* y, double noise, int32_t max_tr
     if (rc) return rc;
     rc = gemv_f64(n, n, 1.0, Linv, n, res, 0.0, t, st);
     if (rc) return rc;
-    rc = gemm_f64(n, 1, n, 1.0, Linv, n, 1, t, 1, 0, 1.0, alpha, 1, KFULL, 0, nullptr, st);
+    rc = gemv_t_f64(n, n, 1.0, Linv, n, t, 1.0, alpha, st);
     if (rc) return rc;
     // beta = L^T alpha (= L^-1 (y - m) for the refined alpha)
-    rc = gemm_f64(n, 1, n, 1.0, L, n, 1, alpha, 1, 0, 0.0, beta, 1, KFULL, 0, nullptr, st);
+    rc = gemv_t_f64(n, n, 1.0, L, n, alpha, 0.0, beta, st);
     if (rc) return rc;
     BGB_CUDA_TRY(cudaStreamSynchronize(st));
     return BGB_OK;

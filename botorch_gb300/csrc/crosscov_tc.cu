@@ -36,6 +36,11 @@
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
 
 #include "bgb_common.cuh"
 #include "bgb_kernels.cuh"
@@ -257,6 +262,20 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// t[v] += r[v] (v < 32, round-to-nearest) as 16 packed float32-pair adds.
+__device__ __forceinline__ void add_f32x2_32(float* t, const uint32_t (&r)[32]) {
+#pragma unroll
+    for (int v = 0; v < 32; v += 2) {
+        asm("{\n\t.reg .b64 x, y;\n\t"
+            "mov.b64 x, {%0, %1};\n\t"
+            "mov.b64 y, {%2, %3};\n\t"
+            "add.rn.f32x2 x, x, y;\n\t"
+            "mov.b64 {%0, %1}, x;\n\t}"
+            : "+f"(t[v]), "+f"(t[v + 1])
+            : "r"(r[v]), "r"(r[v + 1]));
+    }
+}
+
 struct TcMaps {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
     CUtensorMap c;  // float32 output, 32 x 32 boxes, 128-byte swizzle
@@ -279,11 +298,11 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void*
 // k range of the two runs first.
 struct TileSched {
     int n_tiles, P, total, kmode;
-    __device__ TileSched(int m_tiles, int n_tiles_, int kmode_)
+    __host__ __device__ TileSched(int m_tiles, int n_tiles_, int kmode_)
         : n_tiles(n_tiles_), P((n_tiles_ + 1) / 2), total(m_tiles * ((n_tiles_ + 1) / 2)),
           kmode(kmode_) {}
     // tile h (0, 1) of super-tile s; false when s holds a single (middle) column block
-    __device__ bool tile(int s, int h, int& m_tile, int& n_tile) const {
+    __host__ __device__ bool tile(int s, int h, int& m_tile, int& n_tile) const {
         const int p = s % P;
         m_tile = s / P;
         const int lo = p, hi = n_tiles - 1 - p;
@@ -292,13 +311,54 @@ struct TileSched {
         n_tile = ((h == 0) == hi_first) ? hi : lo;
         return true;
     }
-    __device__ void k_range(int n_tile, int K, int& kbeg, int& nkb) const {
+    __host__ __device__ void k_range(int n_tile, int K, int& kbeg, int& nkb) const {
         const int n0 = n_tile * TC_BN;
         int kend = K;
         kbeg = 0;
-        if (kmode == KB_UPPER) kend = min(K, n0 + TC_BN);
+        if (kmode == KB_UPPER) kend = K < n0 + TC_BN ? K : n0 + TC_BN;
         else if (kmode == KB_LOWER) kbeg = (n0 / TC_BK) * TC_BK;
         nkb = kend > kbeg ? (kend - kbeg + TC_BK - 1) / TC_BK : 0;
+    }
+};
+
+// The last rounds of the round-robin leave clusters idle while others finish
+// (1024 super-tiles on 76 clusters: 40 clusters wait out the 14th round). So
+// only the first static_rounds rounds are round-robin; the tiles of the
+// remaining one to two rounds' super-tiles (all from the last few row blocks,
+// whose A rows stay in L2) are dealt out largest first to the least-loaded
+// cluster (LPT), computed on the host and passed as a kernel parameter:
+// cluster c then runs tiles[off[c] .. off[c + 1]) in that order.
+constexpr int TC_MAX_CLUSTERS = 160;
+constexpr int TC_MAX_TAIL = 640;
+struct TcTail {
+    int static_rounds;
+    uint16_t off[TC_MAX_CLUSTERS + 1];
+    uint32_t tiles[TC_MAX_TAIL];  // m_tile << 8 | n_tile
+};
+
+// The tiles of one cluster, in order: the static rounds (both tiles of each
+// super-tile), then the cluster's share of the tail.
+struct TileIter {
+    const TileSched& sched;
+    const TcTail& tail;
+    int cluster, ncl, i;
+    __device__ TileIter(const TileSched& s, const TcTail& t, int c, int n)
+        : sched(s), tail(t), cluster(c), ncl(n), i(0) {}
+    __device__ bool next(int& m_tile, int& n_tile) {
+        const int nst = 2 * tail.static_rounds;
+        while (i < nst) {
+            const int r = i >> 1, h = i & 1;
+            ++i;
+            const int s = cluster + r * ncl;
+            if (s < sched.total && sched.tile(s, h, m_tile, n_tile)) return true;
+        }
+        const int e = (int)tail.off[cluster] + (i - nst);
+        if (e >= (int)tail.off[cluster + 1]) return false;
+        ++i;
+        const uint32_t t = tail.tiles[e];
+        m_tile = (int)(t >> 8);
+        n_tile = (int)(t & 255u);
+        return true;
     }
 };
 
@@ -309,7 +369,8 @@ struct TileSched {
 // loads and MMAs proceed while the epilogue warps store the previous tile.
 template <int PAIR>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_gemm_kernel(const __grid_constant__ TcMaps maps, int M, int N, int K, int kmode,
+    tc_gemm_kernel(const __grid_constant__ TcMaps maps, const __grid_constant__ TcTail tail,
+                   int M, int N, int K, int kmode,
                    int m_tiles, int n_tiles, const float* __restrict__ row_mul,
                    float row_mul_const, const float* __restrict__ col_mul, int* __restrict__ err) {
     using Cfg = TcCfg<PAIR>;
@@ -354,10 +415,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // ---------------- TMA producer (each CTA loads its own rows of A and of B)
         int g = 0;  // k-blocks issued by this CTA
         bool stop = false;
-        for (int s = cluster; s < sched.total && !stop; s += nclusters) {
-            for (int h = 0; h < 2 && !stop; ++h) {
-                int m_tile, n_tile, kbeg, nkb;
-                if (!sched.tile(s, h, m_tile, n_tile)) continue;
+        TileIter it(sched, tail, cluster, nclusters);
+        int m_tile, n_tile;
+        while (!stop && it.next(m_tile, n_tile)) {
+            {
+                int kbeg, nkb;
                 sched.k_range(n_tile, K, kbeg, nkb);
                 const int arow = m_tile * TC_BM * PAIR + (int)rank * TC_BM;
                 const int brow = n_tile * TC_BN + (int)rank * Cfg::B_ROWS;
@@ -396,10 +458,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // ---------------- MMA issuer (the leader CTA of the pair)
         int g = 0, cg = 0;  // k-blocks consumed, accumulator chunks started
         bool stop = false;
-        for (int s = cluster; s < sched.total && !stop; s += nclusters) {
-            for (int h = 0; h < 2 && !stop; ++h) {
-                int m_tile, n_tile, kbeg, nkb;
-                if (!sched.tile(s, h, m_tile, n_tile)) continue;
+        TileIter it(sched, tail, cluster, nclusters);
+        int m_tile, n_tile;
+        while (!stop && it.next(m_tile, n_tile)) {
+            {
+                int kbeg, nkb;
                 sched.k_range(n_tile, K, kbeg, nkb);
                 const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
                 for (int c = 0; c < nch && !stop; ++c, ++cg) {
@@ -423,12 +486,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         const uint32_t sa = smem_u32(base + st * Cfg::STAGE_BYTES);
                         const uint32_t a_hi = sa, a_lo = sa + A_TILE, b_hi = sa + 2 * A_TILE,
                                        b_lo = sa + 2 * A_TILE + Cfg::B_TILE;
+                        // the two small cross products first, the hi x hi product last:
+                        // each MMA truncates its sum to the accumulator's scale, so
+                        // issuing the small terms while the accumulator is still small
+                        // leaves fewer full-scale truncations per chunk
 #pragma unroll
                         for (int kk = 0; kk < TC_BK / TC_UMMA_K; ++kk) {
                             const uint32_t off = kk * TC_UMMA_K * 2;  // bytes along K in the 128-B row
                             const uint32_t acc = (kb > c * TC_FLUSH || kk > 0) ? 1u : 0u;
                             umma_f16<PAIR>(tacc, sdesc(a_lo + off), sdesc(b_hi + off), acc);
                             umma_f16<PAIR>(tacc, sdesc(a_hi + off), sdesc(b_lo + off), 1u);
+                        }
+#pragma unroll
+                        for (int kk = 0; kk < TC_BK / TC_UMMA_K; ++kk) {
+                            const uint32_t off = kk * TC_UMMA_K * 2;
                             umma_f16<PAIR>(tacc, sdesc(a_hi + off), sdesc(b_hi + off), 1u);
                         }
                         umma_commit<PAIR>(&empty[st]);
@@ -444,10 +515,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         float* stg = staging + (warp - 2) * 32 * 32;
         int cg = 0;
         bool good = true;
-        for (int s = cluster; s < sched.total && good; s += nclusters) {
-            for (int h = 0; h < 2 && good; ++h) {
-                int m_tile, n_tile, kbeg, nkb;
-                if (!sched.tile(s, h, m_tile, n_tile)) continue;
+        TileIter it(sched, tail, cluster, nclusters);
+        int m_tile, n_tile;
+        while (good && it.next(m_tile, n_tile)) {
+            {
+                int kbeg, nkb;
                 sched.k_range(n_tile, K, kbeg, nkb);
                 const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
                 const int row0 = m_tile * TC_BM * PAIR + (int)rank * TC_BM + quarter * 32;
@@ -469,16 +541,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) +
                                            (uint32_t)(a * TC_BN + half * (TC_BN / 2));
+                    // the adds sit on the path from one chunk's completion to the MMAs
+                    // that reuse its accumulator, so they run as packed float32 pairs
+                    // and the last group's adds follow the release of the accumulator
+                    uint32_t r[32];
 #pragma unroll
-                    for (int j = 0; j < TC_BN / 2 / 32; ++j) {
-                        uint32_t r[32];
+                    for (int j = 0; j < TC_BN / 2 / 32 - 1; ++j) {
                         tmem_ld32(tbase + (uint32_t)(j * 32), r);
-#pragma unroll
-                        for (int v = 0; v < 32; ++v) tot[j * 32 + v] += __uint_as_float(r[v]);
+                        add_f32x2_32(tot + j * 32, r);
                     }
+                    tmem_ld32(tbase + (uint32_t)((TC_BN / 2 / 32 - 1) * 32), r);
                     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                     __syncwarp();
                     if (lane == 0) mbar_arrive<PAIR>(&acce[a], 0);
+                    add_f32x2_32(tot + (TC_BN / 2 / 32 - 1) * 32, r);
                 }
                 if (!good) break;
                 // undo the operand scales (row multiplier times column multiplier) and
@@ -653,6 +729,72 @@ int resident_clusters() {
     return cached[dev];
 }
 
+// Tail schedule for ncl clusters (see TcTail). Without room for it (more
+// clusters or tail tiles than the parameter holds, or n_tiles > 256) every
+// round is round-robin.
+void build_tail(int m_tiles, int n_tiles, int K, int kmode, int ncl, TcTail& t) {
+    const TileSched sched(m_tiles, n_tiles, kmode);
+    memset(&t, 0, sizeof(t));
+    t.static_rounds = (sched.total + ncl - 1) / ncl;
+    if (ncl <= 0 || ncl > TC_MAX_CLUSTERS || n_tiles > 256 || m_tiles >= (1 << 24)) return;
+    const int rounds = sched.total / ncl;
+    const int rs = rounds >= 2 ? rounds - 1 : 0;
+    struct Item { int nkb, m, n; };
+    std::vector<Item> items;
+    for (int sidx = rs * ncl; sidx < sched.total; ++sidx) {
+        for (int h = 0; h < 2; ++h) {
+            int m, n, kbeg, nkb;
+            if (!sched.tile(sidx, h, m, n)) continue;
+            sched.k_range(n, K, kbeg, nkb);
+            items.push_back({nkb, m, n});
+        }
+    }
+    if ((int)items.size() > TC_MAX_TAIL) return;
+    std::stable_sort(items.begin(), items.end(),
+                     [](const Item& a, const Item& b) { return a.nkb > b.nkb; });
+    // a tile costs its k-blocks plus about two k-blocks of exposed epilogue
+    constexpr int kTileCost = 2;
+    std::vector<long> load(ncl, 0);
+    std::vector<std::vector<uint32_t>> lists(ncl);
+    for (const Item& it : items) {
+        int c = 0;
+        for (int j = 1; j < ncl; ++j)
+            if (load[j] < load[c]) c = j;
+        lists[c].push_back(((uint32_t)it.m << 8) | (uint32_t)it.n);
+        load[c] += it.nkb + kTileCost;
+    }
+    t.static_rounds = rs;
+    int e = 0;
+    for (int c = 0; c < ncl; ++c) {
+        t.off[c] = (uint16_t)e;
+        for (uint32_t v : lists[c]) t.tiles[e++] = v;
+    }
+    t.off[ncl] = (uint16_t)e;
+}
+
+// build_tail, memoised over the last few shapes (the schedule is a pure function
+// of its arguments; graph capture and repeated calls reuse it).
+void tail_for(int m_tiles, int n_tiles, int K, int kmode, int ncl, TcTail& out) {
+    struct Entry { int key[5]; TcTail tail; };
+    static std::mutex mu;
+    static Entry cache[8];
+    static int used = 0, next = 0;
+    const int key[5] = {m_tiles, n_tiles, K, kmode, ncl};
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < used; ++i) {
+        if (memcmp(cache[i].key, key, sizeof(key)) == 0) {
+            out = cache[i].tail;
+            return;
+        }
+    }
+    Entry& en = cache[next];
+    next = (next + 1) % 8;
+    if (used < 8) ++used;
+    memcpy(en.key, key, sizeof(key));
+    build_tail(m_tiles, n_tiles, K, kmode, ncl, en.tail);
+    out = en.tail;
+}
+
 // One persistent launch of the GEMM in form PAIR over m_tiles x n_tiles tiles:
 // as many clusters of PAIR CTAs as are resident at once, or fewer when there are
 // fewer super-tiles (pairs of column blocks of one row block).
@@ -685,8 +827,10 @@ int launch_tc(const TcMaps& maps, int64_t M, int64_t N, int64_t K, int kmode, in
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    BGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, tc_gemm_kernel<PAIR>, maps, (int)M, (int)N, (int)K, kmode,
-                                    m_tiles, n_tiles, row_mul, row_mul_const, col_mul, err));
+    TcTail tail;
+    tail_for(m_tiles, n_tiles, (int)K, kmode, (int)clusters, tail);
+    BGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, tc_gemm_kernel<PAIR>, maps, tail, (int)M, (int)N, (int)K,
+                                    kmode, m_tiles, n_tiles, row_mul, row_mul_const, col_mul, err));
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }

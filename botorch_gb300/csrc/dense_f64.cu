@@ -13,12 +13,16 @@ namespace {
 constexpr int GT = 64;   // output tile
 constexpr int GK = 16;   // k step
 
+// blockIdx.z: member of a batch of equal-shape products at element strides sA, sB, sC
 __global__ void __launch_bounds__(256) gemm_f64_kernel(
     int64_t M, int64_t N, int64_t K, double alpha, const double* __restrict__ A, int64_t lda,
     int transA, const double* __restrict__ B, int64_t ldb, int transB, double beta,
     double* __restrict__ C, int64_t ldc, int kmode, int lower_only, const int* abort_flag,
-    int64_t n_tri) {
+    int64_t n_tri, int64_t sA, int64_t sB, int64_t sC) {
     if (abort_flag != nullptr && *abort_flag != 0) return;
+    A += (int64_t)blockIdx.z * sA;
+    B += (int64_t)blockIdx.z * sB;
+    C += (int64_t)blockIdx.z * sC;
     const int64_t row0 = (int64_t)blockIdx.y * GT, col0 = (int64_t)blockIdx.x * GT;
     if (lower_only && col0 > row0 + GT - 1) return;
     __shared__ double As[GK][GT + 1];
@@ -78,38 +82,58 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(
 }
 
 // Unblocked Cholesky of one diagonal block (kb <= 64) in shared memory, plus
-// the inverse of the resulting triangular block (for the panel solve).
+// the inverse of the resulting triangular block (for the panel solve). Thread
+// (r, cq) = (tid / 4, tid % 4) works on row r, columns cq, cq + 4, ...; both
+// passes are right-looking with the pivot work (square root and reciprocal of
+// the next diagonal entry; scaling of the next finished row of the inverse)
+// done by the thread that updates that entry last, so each column costs two
+// barriers (factor) and one (inverse). float64 runs at a small fraction of
+// the float32 rate here, so the passes issue no redundant float64 work.
 __global__ void __launch_bounds__(256) potrf_diag_kernel(double* A, int64_t lda, int kb,
                                                          int64_t k0, int* info, double* dinv) {
     if (info[1] != 0) return;  // an earlier block already failed
     __shared__ double S[64][65];
     __shared__ double X[64][65];
+    __shared__ double rd[64];
     __shared__ int fail;
     const int tid = threadIdx.x;
-    if (tid == 0) fail = 0;
+    const int r = tid >> 2, cq = tid & 3;
     for (int idx = tid; idx < 64 * 64; idx += 256) {
-        int i = idx / 64, j = idx % 64;
+        const int i = idx >> 6, j = idx & 63;
         S[i][j] = (i < kb && j <= i) ? A[(int64_t)i * lda + j] : 0.0;
+        X[i][j] = (i == j) ? 1.0 : 0.0;
     }
     __syncthreads();
-    for (int j = 0; j < kb; ++j) {
-        if (tid == 0) {
-            double v = S[j][j];
-            if (!(v > 0.0)) {
-                fail = j + 1;
-            } else {
-                S[j][j] = sqrt(v);
-            }
+    if (tid == 0) {
+        fail = 0;
+        const double v = S[0][0];
+        if (!(v > 0.0)) {
+            fail = 1;
+        } else {
+            const double d = sqrt(v);
+            S[0][0] = d;
+            rd[0] = 1.0 / d;
         }
+    }
+    __syncthreads();
+    for (int j = 0; j < kb && !fail; ++j) {
+        // column j below the diagonal: L[r][j] = S[r][j] / L[j][j]
+        if (cq == 0 && r > j && r < kb) S[r][j] *= rd[j];
         __syncthreads();
-        if (fail) break;
-        const double djj = S[j][j];
-        for (int i = j + 1 + tid; i < kb; i += 256) S[i][j] /= djj;
-        __syncthreads();
-        const int rem = kb - j - 1;
-        for (int idx = tid; idx < rem * rem; idx += 256) {
-            int i = j + 1 + idx / rem, k = j + 1 + idx % rem;
-            if (k <= i) S[i][k] = fma(-S[i][j], S[k][j], S[i][k]);
+        // trailing update of the lower triangle; the thread of (j+1, j+1) then pivots
+        if (r > j && r < kb) {
+            const double lrj = S[r][j];
+            for (int k = j + 1 + cq; k <= r; k += 4) S[r][k] = fma(-lrj, S[k][j], S[r][k]);
+            if (r == j + 1 && cq == 0) {
+                const double v = S[r][r];
+                if (!(v > 0.0)) {
+                    fail = r + 1;
+                } else {
+                    const double d = sqrt(v);
+                    S[r][r] = d;
+                    rd[r] = 1.0 / d;
+                }
+            }
         }
         __syncthreads();
     }
@@ -120,50 +144,63 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double* A, int64_t lda,
         }
         return;
     }
-    // inverse of the lower-triangular block: column t by forward substitution
-    if (tid < 64) {
-        const int t = tid;
-        for (int i = 0; i < 64; ++i) X[i][t] = 0.0;
-        if (t < kb) {
-            for (int i = t; i < kb; ++i) {
-                double s = (i == t) ? 1.0 : 0.0;
-                for (int k = t; k < i; ++k) s = fma(-S[i][k], X[k][t], s);
-                X[i][t] = s / S[i][i];
-            }
-        }
-    }
+    // X = L^-1 by rows: row k is final once rows < k are eliminated from it and it
+    // is scaled by 1 / L[k][k]; eliminating row k from rows i > k finishes row k + 1
+    if (tid == 0) X[0][0] = rd[0];
     __syncthreads();
+    for (int k = 0; k + 1 < kb; ++k) {
+        if (r > k && r < kb) {
+            const double lrk = S[r][k];
+            for (int c = cq; c <= k; c += 4) X[r][c] = fma(-lrk, X[k][c], X[r][c]);
+            if (r == k + 1)
+                for (int c = cq; c <= r; c += 4) X[r][c] *= rd[r];
+        }
+        __syncthreads();
+    }
     for (int idx = tid; idx < kb * kb; idx += 256) {
         int i = idx / kb, j = idx % kb;
         A[(int64_t)i * lda + j] = (j <= i) ? S[i][j] : 0.0;
-        dinv[i * 64 + j] = X[i][j];
+        dinv[i * 64 + j] = (j <= i) ? X[i][j] : 0.0;
     }
 }
 
-// In-place: P (rows x kb) := P * Dinv^T (Dinv lower triangular kb x kb).
-// Each CTA owns 32 rows, so reading and writing the same rows is safe.
+// In-place: P (rows x kb) := P * Dinv^T (Dinv lower triangular kb x kb, staged in
+// shared memory). Each CTA owns 16 rows, so reading and writing the same rows is safe.
+constexpr int kTrsmRows = 16;
 __global__ void __launch_bounds__(256) panel_trsm_kernel(double* P, int64_t ldp, int64_t rows,
                                                          int kb, const double* __restrict__ dinv,
                                                          const int* info) {
     if (info[1] != 0) return;
-    __shared__ double R[32][65];
-    const int64_t r0 = (int64_t)blockIdx.x * 32;
-    for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
-        int i = idx / 64, j = idx % 64;
+    __shared__ double R[kTrsmRows][65];
+    __shared__ double D[64][65];
+    const int64_t r0 = (int64_t)blockIdx.x * kTrsmRows;
+    for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+        const int i = idx >> 6, j = idx & 63;
+        D[i][j] = (i < kb && j <= i) ? dinv[i * 64 + j] : 0.0;
+    }
+    for (int idx = threadIdx.x; idx < kTrsmRows * 64; idx += 256) {
+        const int i = idx >> 6, j = idx & 63;
         R[i][j] = (r0 + i < rows && j < kb) ? P[(r0 + i) * ldp + j] : 0.0;
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
-        int i = idx / 64, c = idx % 64;
+    for (int idx = threadIdx.x; idx < kTrsmRows * 64; idx += 256) {
+        const int i = idx >> 6, c = idx & 63;
         if (r0 + i >= rows || c >= kb) continue;
-        double s = 0.0;
-        for (int k = 0; k <= c; ++k) s = fma(R[i][k], dinv[c * 64 + k], s);
-        P[(r0 + i) * ldp + c] = s;
+        double s0 = 0.0, s1 = 0.0;
+        int k = 0;
+        for (; k + 1 <= c; k += 2) {
+            s0 = fma(R[i][k], D[c][k], s0);
+            s1 = fma(R[i][k + 1], D[c][k + 1], s1);
+        }
+        if (k <= c) s0 = fma(R[i][k], D[c][k], s0);
+        P[(r0 + i) * ldp + c] = s0 + s1;
     }
 }
 
-__global__ void diag_inverse_blocks_kernel(const double* L, int64_t lda, int64_t n, double* D) {
-    // one CTA per 64 x 64 diagonal block; D[blk] = inverse of L's diagonal block
+// In place: every 64 x 64 diagonal block of the lower-triangular L (n x n) is
+// replaced by its inverse (zeros above its diagonal); one CTA per block, 64
+// threads, thread t solving column t by forward substitution.
+__global__ void diag_inverse_inplace_kernel(double* L, int64_t lda, int64_t n) {
     __shared__ double S[64][65];
     const int64_t k0 = (int64_t)blockIdx.x * 64;
     const int kb = (int)((n - k0) < 64 ? (n - k0) : 64);
@@ -173,18 +210,43 @@ __global__ void diag_inverse_blocks_kernel(const double* L, int64_t lda, int64_t
     }
     __syncthreads();
     const int t = threadIdx.x;
-    if (t < 64) {
-        double* out = D + (int64_t)blockIdx.x * 64 * 64;
-        double col[64];
-        for (int i = 0; i < 64; ++i) col[i] = 0.0;
-        if (t < kb) {
-            for (int i = t; i < kb; ++i) {
-                double s = (i == t) ? 1.0 : 0.0;
-                for (int k = t; k < i; ++k) s = fma(-S[i][k], col[k], s);
-                col[i] = s / S[i][i];
-            }
+    if (t >= kb) return;
+    double col[64];
+    for (int i = 0; i < 64; ++i) col[i] = 0.0;
+    for (int i = t; i < kb; ++i) {
+        double s = (i == t) ? 1.0 : 0.0;
+        for (int k = t; k < i; ++k) s = fma(-S[i][k], col[k], s);
+        col[i] = s / S[i][i];
+    }
+    for (int i = 0; i < kb; ++i) L[(k0 + i) * lda + k0 + t] = col[i];
+}
+
+// y = alpha * A^T x + beta * y, A m x n row-major: one CTA per 32 columns, its
+// 8 warps taking every 8th row (lane = column, so each row read is one 256-byte
+// segment), the 8 partial sums added in a fixed order.
+__global__ void __launch_bounds__(256) gemv_t_f64_kernel(int64_t m, int64_t n, double alpha,
+                                                         const double* __restrict__ A, int64_t lda,
+                                                         const double* __restrict__ x, double beta,
+                                                         double* __restrict__ y) {
+    __shared__ double part[8][33];
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+    const int64_t j = (int64_t)blockIdx.x * 32 + lane;
+    double s0 = 0.0, s1 = 0.0;
+    if (j < n) {
+        int64_t i = w;
+        for (; i + 8 < m; i += 16) {
+            s0 = fma(A[i * lda + j], x[i], s0);
+            s1 = fma(A[(i + 8) * lda + j], x[i + 8], s1);
         }
-        for (int i = 0; i < 64; ++i) out[i * 64 + t] = col[i];
+        if (i < m) s0 = fma(A[i * lda + j], x[i], s0);
+    }
+    part[w][lane] = s0 + s1;
+    __syncthreads();
+    if (w == 0 && j < n) {
+        double t = 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t += part[u][lane];
+        y[j] = alpha * t + (beta != 0.0 ? beta * y[j] : 0.0);
     }
 }
 
@@ -237,10 +299,29 @@ int gemm_f64(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int
              int transA, const double* B, int64_t ldb, int transB, double beta, double* C,
              int64_t ldc, int kmode, int lower_only, const int* abort_flag, cudaStream_t stream,
              int64_t n_tri) {
-    if (M <= 0 || N <= 0) return BGB_OK;
-    dim3 grid((unsigned)ceil_div(N, GT), (unsigned)ceil_div(M, GT));
+    return gemm_f64_batched(M, N, K, alpha, A, lda, 0, transA, B, ldb, 0, transB, beta, C, ldc, 0,
+                            kmode, lower_only, abort_flag, 1, stream, n_tri);
+}
+
+int gemm_f64_batched(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                     int64_t sA, int transA, const double* B, int64_t ldb, int64_t sB, int transB,
+                     double beta, double* C, int64_t ldc, int64_t sC, int kmode, int lower_only,
+                     const int* abort_flag, int64_t batch, cudaStream_t stream, int64_t n_tri) {
+    if (M <= 0 || N <= 0 || batch <= 0) return BGB_OK;
+    if (batch > 65535) return BGB_ERR_ARG;
+    dim3 grid((unsigned)ceil_div(N, GT), (unsigned)ceil_div(M, GT), (unsigned)batch);
     gemm_f64_kernel<<<grid, 256, 0, stream>>>(M, N, K, alpha, A, lda, transA, B, ldb, transB,
-                                              beta, C, ldc, kmode, lower_only, abort_flag, n_tri);
+                                              beta, C, ldc, kmode, lower_only, abort_flag, n_tri,
+                                              sA, sB, sC);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+int gemv_t_f64(int64_t m, int64_t n, double alpha, const double* A, int64_t lda, const double* x,
+               double beta, double* y, cudaStream_t stream) {
+    if (n <= 0) return BGB_OK;
+    gemv_t_f64_kernel<<<(unsigned)ceil_div(n, 32), 256, 0, stream>>>(m, n, alpha, A, lda, x, beta,
+                                                                     y);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
@@ -266,8 +347,8 @@ int cholesky_f64(double* A, int64_t n, int64_t lda, int* dev_info, double* ws,
         const int64_t rest = n - k0 - kb;
         if (rest <= 0) break;
         double* P = A + (k0 + kb) * lda + k0;
-        panel_trsm_kernel<<<(unsigned)ceil_div(rest, 32), 256, 0, stream>>>(P, lda, rest, kb, ws,
-                                                                            dev_info);
+        panel_trsm_kernel<<<(unsigned)ceil_div(rest, (int64_t)kTrsmRows), 256, 0, stream>>>(
+            P, lda, rest, kb, ws, dev_info);
         BGB_CHECK_LAUNCH();
         double* T = A + (k0 + kb) * lda + (k0 + kb);
         int rc = gemm_f64(rest, rest, kb, -1.0, P, lda, 0, P, lda, 1, 1.0, T, lda, KFULL, 1,
@@ -277,32 +358,64 @@ int cholesky_f64(double* A, int64_t n, int64_t lda, int* dev_info, double* ws,
     return zero_upper_f64(A, n, lda, stream);
 }
 
-// In-place inverse of a lower-triangular matrix, blocked by 64 rows.
-// ws: (n/64 + 1) * 64*64 diagonal inverses + 64 * n temporary.
-int tri_inverse_f64(double* L, int64_t n, int64_t lda, double* ws, cudaStream_t stream) {
-    const int64_t nb = ceil_div(n, 64);
-    double* D = ws;
-    double* T = ws + nb * 64 * 64;
-    diag_inverse_blocks_kernel<<<(unsigned)nb, 64, 0, stream>>>(L, lda, n, D);
-    BGB_CHECK_LAUNCH();
-    for (int64_t ib = 0; ib < nb; ++ib) {
-        const int64_t i0 = ib * 64;
-        const int64_t kb = (n - i0) < 64 ? (n - i0) : 64;
-        if (ib > 0) {
-            // T = L[i-block, 0:i0] * Y[0:i0, 0:i0] (Y lower triangular, already in place)
-            int rc = gemm_f64(kb, i0, i0, 1.0, L + i0 * lda, lda, 0, L, lda, 0, 0.0, T, i0,
-                              KB_LOWER, 0, nullptr, stream);
-            if (rc != BGB_OK) return rc;
-            // Y[i-block, 0:i0] = -D_i * T
-            rc = gemm_f64(kb, i0, kb, -1.0, D + ib * 64 * 64, 64, 0, T, i0, 0, 0.0, L + i0 * lda,
-                          lda, KFULL, 0, nullptr, stream);
-            if (rc != BGB_OK) return rc;
+// Workspace (doubles) of tri_inverse_f64: the largest level's products T.
+int64_t tri_inverse_ws_doubles(int64_t n) {
+    int64_t best = 64 * 64;
+    for (int64_t s = 64; s < n; s *= 2) {
+        int64_t need = 0;
+        for (int64_t a0 = 0; a0 + s < n; a0 += 2 * s) {
+            const int64_t sc = (n - a0 - s) < s ? (n - a0 - s) : s;
+            need += sc * s;
         }
-        copy_block_kernel<<<(unsigned)ceil_div(kb * kb, 256), 256, 0, stream>>>(
-            D + ib * 64 * 64, 64, L + i0 * lda + i0, lda, kb, kb, 0.0);
-        BGB_CHECK_LAUNCH();
+        best = need > best ? need : best;
     }
-    return zero_upper_f64(L, n, lda, stream);
+    return best;
+}
+
+// In-place inverse of a lower-triangular matrix (upper triangle zero), bottom up
+// over block sizes s = 64, 128, ...: every 64 x 64 diagonal block is inverted,
+// then at each level the pairs of adjacent inverted blocks [A 0; B C] become
+//   [A^-1 0; -C^-1 (B A^-1)  C^-1]
+// through two triangular GEMMs batched over all pairs of the level (one
+// launch each for the pairs of full size, one each for a ragged last pair), so
+// every level but the first few fills the GPU. ws: tri_inverse_ws_doubles(n).
+int tri_inverse_f64(double* L, int64_t n, int64_t lda, double* ws, cudaStream_t stream) {
+    if (n <= 0) return BGB_OK;
+    int rc = zero_upper_f64(L, n, lda, stream);
+    if (rc) return rc;
+    diag_inverse_inplace_kernel<<<(unsigned)ceil_div(n, 64), 64, 0, stream>>>(L, lda, n);
+    BGB_CHECK_LAUNCH();
+    for (int64_t s = 64; s < n; s *= 2) {
+        const int64_t full = n / (2 * s);               // pairs whose C block has s rows
+        const int64_t a_last = full * 2 * s;            // A block of a ragged last pair
+        const int64_t sc_last = n - a_last - s;         // its C rows (<= 0: no such pair)
+        const int64_t step = 2 * s * lda + 2 * s;       // from one pair to the next
+        // T_p = B_p A_p^-1  (A^-1 lower triangular: k >= column)
+        if (full > 0) {
+            rc = gemm_f64_batched(s, s, s, 1.0, L + s * lda, lda, step, 0, L, lda, step, 0, 0.0, ws,
+                                  s, s * s, KB_LOWER, 0, nullptr, full, stream);
+            if (rc) return rc;
+        }
+        if (sc_last > 0) {
+            rc = gemm_f64(sc_last, s, s, 1.0, L + (a_last + s) * lda + a_last, lda, 0,
+                          L + a_last * lda + a_last, lda, 0, 0.0, ws + full * s * s, s, KB_LOWER, 0,
+                          nullptr, stream);
+            if (rc) return rc;
+        }
+        // B_p := -C_p^-1 T_p  (C^-1 lower triangular: k <= row)
+        if (full > 0) {
+            rc = gemm_f64_batched(s, s, s, -1.0, L + s * lda + s, lda, step, 0, ws, s, s * s, 0, 0.0,
+                                  L + s * lda, lda, step, KA_LOWER, 0, nullptr, full, stream);
+            if (rc) return rc;
+        }
+        if (sc_last > 0) {
+            rc = gemm_f64(sc_last, s, sc_last, -1.0, L + (a_last + s) * lda + a_last + s, lda, 0,
+                          ws + full * s * s, s, 0, 0.0, L + (a_last + s) * lda + a_last, lda,
+                          KA_LOWER, 0, nullptr, stream);
+            if (rc) return rc;
+        }
+    }
+    return BGB_OK;
 }
 
 int copy_matrix_f64(const double* src, int64_t lds, double* dst, int64_t ldd, int64_t m, int64_t n,

@@ -171,13 +171,15 @@ int bgb_psd_safe_cholesky(const double* A, int64_t n, int64_t lda, double* L, in
                           int32_t max_tries, double jitter, double* jitter_host,
                           void* workspace, size_t workspace_bytes, void* stream);
 
-/* (b) Lower-triangular inverse in place (blocked). */
+/* (b) Lower-triangular inverse in place (recursive: 64 x 64 diagonal blocks,
+ * then pairs of adjacent blocks joined level by level with batched float64
+ * GEMMs). The upper triangle of L is set to zero. */
 int bgb_tri_inverse(double* L, int64_t n, int64_t lda, void* workspace, size_t workspace_bytes,
                     void* stream);
 size_t bgb_tri_inverse_workspace_bytes(int64_t n);
 
 /* (b) Exact-GP training cache: L = psd_safe_cholesky(K + noise I), Linv = L^-1
- * (blocked triangular inverse), alpha = K^-1 (y - mean_constant) = L^-T L^-1
+ * (recursive triangular inverse), alpha = K^-1 (y - mean_constant) = L^-T L^-1
  * (y - m) with one step of iterative refinement, and beta = L^T alpha. y is the
  * standardised training target (n). Synchronises `stream`. Replaces the
  * training-side caches of gpytorch's exact prediction strategy (mean cache and
