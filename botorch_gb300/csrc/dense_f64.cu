@@ -3,6 +3,8 @@
 // inverse, GEMV. GB300 runs float64 at a small fraction of its float32 rate,
 // so every routine here is DFMA-bound; the tiles are sized for register
 // reuse, not for HBM traffic.
+#include <mutex>
+
 #include "bgb_common.cuh"
 #include "bgb_kernels.cuh"
 
@@ -23,7 +25,19 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(
     A += (int64_t)blockIdx.z * sA;
     B += (int64_t)blockIdx.z * sB;
     C += (int64_t)blockIdx.z * sC;
-    const int64_t row0 = (int64_t)blockIdx.y * GT, col0 = (int64_t)blockIdx.x * GT;
+    // tile order: CTAs start in launch order, so with a triangular k range the
+    // tiles with the longest range go first (KB_LOWER: the first columns;
+    // KA_LOWER: the last rows), and the last wave holds short tiles only
+    const int64_t lin = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+    int64_t tr = blockIdx.y, tc = blockIdx.x;
+    if (kmode == KB_LOWER) {
+        tc = lin / gridDim.y;
+        tr = lin % gridDim.y;
+    } else if (kmode == KA_LOWER) {
+        tr = gridDim.y - 1 - lin / gridDim.x;
+        tc = lin % gridDim.x;
+    }
+    const int64_t row0 = tr * GT, col0 = tc * GT;
     if (lower_only && col0 > row0 + GT - 1) return;
     __shared__ double As[GK][GT + 1];
     __shared__ double Bs[GK][GT + 1];
@@ -334,26 +348,95 @@ int gemv_f64(int64_t m, int64_t n, double alpha, const double* A, int64_t lda, c
     return BGB_OK;
 }
 
-// Right-looking blocked Cholesky (block 64). dev_info[0] = failing pivot
-// (1-based, 0 if none), dev_info[1] = abort flag read by the later launches.
-// ws: 64*64 doubles (diagonal-block inverse).
+// A high-priority side stream and two events per device for the lookahead of
+// cholesky_f64; the mutex keeps each call's record / wait pairs together.
+struct Lookahead {
+    std::mutex mu;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ready = nullptr, panel = nullptr;
+};
+
+Lookahead* lookahead_for_current_device() {
+    static Lookahead per_dev[64];
+    static std::mutex init_mu;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(init_mu);
+    Lookahead& la = per_dev[dev];
+    if (la.side == nullptr) {
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&la.side, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+            cudaEventCreateWithFlags(&la.ready, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&la.panel, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            la.side = nullptr;
+            return nullptr;
+        }
+    }
+    return &la;
+}
+
+// Right-looking blocked Cholesky (block 64) with a lookahead of one panel: after
+// panel k is solved, the next panel's column block is updated first, so the
+// next panel's diagonal factor (one CTA) and panel solve run on a high-priority
+// side stream while the rest of the trailing matrix is updated on `stream`.
+// dev_info[0] = failing pivot (1-based, 0 if none), dev_info[1] = abort flag
+// read by the later launches. ws: 64*64 doubles (diagonal-block inverse; panel
+// k + 1's factor writes it after panel k's solve has read it, both on the side
+// stream or in stream order before the first fork).
 int cholesky_f64(double* A, int64_t n, int64_t lda, int* dev_info, double* ws,
                  cudaStream_t stream) {
     BGB_CUDA_TRY(cudaMemsetAsync(dev_info, 0, 2 * sizeof(int), stream));
-    for (int64_t k0 = 0; k0 < n; k0 += 64) {
+    Lookahead* la = lookahead_for_current_device();
+    std::unique_lock<std::mutex> lock;
+    if (la != nullptr) lock = std::unique_lock<std::mutex>(la->mu);
+    auto factor_panel = [&](int64_t k0, cudaStream_t st) -> int {
         const int kb = (int)((n - k0) < 64 ? (n - k0) : 64);
-        potrf_diag_kernel<<<1, 256, 0, stream>>>(A + k0 * lda + k0, lda, kb, k0, dev_info, ws);
+        potrf_diag_kernel<<<1, 256, 0, st>>>(A + k0 * lda + k0, lda, kb, k0, dev_info, ws);
         BGB_CHECK_LAUNCH();
         const int64_t rest = n - k0 - kb;
+        if (rest > 0) {
+            panel_trsm_kernel<<<(unsigned)ceil_div(rest, (int64_t)kTrsmRows), 256, 0, st>>>(
+                A + (k0 + kb) * lda + k0, lda, rest, kb, ws, dev_info);
+            BGB_CHECK_LAUNCH();
+        }
+        return BGB_OK;
+    };
+    int rc = factor_panel(0, stream);
+    if (rc) return rc;
+    for (int64_t k0 = 0; k0 < n; k0 += 64) {
+        const int kb = (int)((n - k0) < 64 ? (n - k0) : 64);
+        const int64_t rest = n - k0 - kb;
         if (rest <= 0) break;
-        double* P = A + (k0 + kb) * lda + k0;
-        panel_trsm_kernel<<<(unsigned)ceil_div(rest, (int64_t)kTrsmRows), 256, 0, stream>>>(
-            P, lda, rest, kb, ws, dev_info);
-        BGB_CHECK_LAUNCH();
-        double* T = A + (k0 + kb) * lda + (k0 + kb);
-        int rc = gemm_f64(rest, rest, kb, -1.0, P, lda, 0, P, lda, 1, 1.0, T, lda, KFULL, 1,
+        const double* P = A + (k0 + kb) * lda + k0;  // panel k below its diagonal block
+        double* T = A + (k0 + kb) * lda + (k0 + kb);  // trailing matrix
+        const int kb1 = (int)(rest < 64 ? rest : 64);
+        if (la == nullptr) {
+            rc = gemm_f64(rest, rest, kb, -1.0, P, lda, 0, P, lda, 1, 1.0, T, lda, KFULL, 1,
                           dev_info + 1, stream);
-        if (rc != BGB_OK) return rc;
+            if (rc) return rc;
+            rc = factor_panel(k0 + kb, stream);
+            if (rc) return rc;
+            continue;
+        }
+        // next panel's column block, then its factor on the side stream
+        rc = gemm_f64(rest, kb1, kb, -1.0, P, lda, 0, P, lda, 1, 1.0, T, lda, KFULL, 1,
+                      dev_info + 1, stream);
+        if (rc) return rc;
+        BGB_CUDA_TRY(cudaEventRecord(la->ready, stream));
+        BGB_CUDA_TRY(cudaStreamWaitEvent(la->side, la->ready, 0));
+        rc = factor_panel(k0 + kb, la->side);
+        if (rc) return rc;
+        BGB_CUDA_TRY(cudaEventRecord(la->panel, la->side));
+        // the rest of the trailing matrix meanwhile
+        const int64_t rest2 = rest - kb1;
+        if (rest2 > 0) {
+            rc = gemm_f64(rest2, rest2, kb, -1.0, P + kb1 * lda, lda, 0, P + kb1 * lda, lda, 1, 1.0,
+                          T + kb1 * lda + kb1, lda, KFULL, 1, dev_info + 1, stream);
+            if (rc) return rc;
+        }
+        BGB_CUDA_TRY(cudaStreamWaitEvent(stream, la->panel, 0));
     }
     return zero_upper_f64(A, n, lda, stream);
 }
