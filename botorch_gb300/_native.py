@@ -121,6 +121,13 @@ _SIGNATURES = {
                                                c_vp]),
     "bgb_acq_forward_backward_noalloc": (c_i32, [ctypes.POINTER(BgbAcq), c_vp, c_i64, c_vp, c_vp,
                                                  c_vp, c_vp]),
+    "bgb_group_workspace_bytes": (c_size, [ctypes.POINTER(BgbAcq), ctypes.POINTER(c_i64), c_i32]),
+    "bgb_group_create": (c_i32, [ctypes.POINTER(BgbAcq), ctypes.POINTER(c_i64), c_i32,
+                                 ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), ctypes.POINTER(c_vp),
+                                 ctypes.POINTER(c_vp), c_vp, c_size, c_vp, ctypes.POINTER(c_vp)]),
+    "bgb_group_run": (c_i32, [c_vp, c_vp]),
+    "bgb_group_launches": (c_i32, [c_vp]),
+    "bgb_group_destroy": (None, [c_vp]),
     "bgb_log_areas_forward": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64, c_i64,
                                       c_f64, c_f64, c_vp, c_vp]),
     "bgb_log_areas_forward_f32": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64,

@@ -17,12 +17,14 @@ model per ``optimize_acqf`` call); this module batches those evaluations.
 
 from __future__ import annotations
 
+import ctypes
 from dataclasses import dataclass, field
 
 import torch
 from torch import Tensor
 
 from botorch_gb300 import _native as nat
+from botorch_gb300.exceptions import UnsupportedError
 
 # (tensor-core GEMMs, adjoint CTAs per SM); 0 = the library default
 SCHEDULES: tuple[tuple[bool, int], ...] = ((True, 0), (True, 8), (True, 32), (False, 0), (False, 8))
@@ -178,3 +180,112 @@ class ModelBatch:
             if worst != 0:
                 self.acqfs[0]._raise_for_status(torch.tensor([worst]))
         return [(o[0], o[1]) for o in self.out]
+
+
+class ModelGroup:
+    """Value + gradient of many acquisition problems with one launch per stage.
+
+    A native group plan (``bgb_group_*``) runs every problem's kernel build,
+    forward tensor-core GEMM, covariance reduction, batch step, row mix, adjoint
+    GEMM and adjoint as one launch each over all problems (about ten kernels
+    for the whole group, captured in one CUDA graph), instead of ~11 launches
+    per problem. Members must be mixed-precision tensor-core problems with a
+    cached root, q <= 8 and r <= 4; ``ModelGroup.supported`` says whether a set
+    qualifies. ``value_and_grad(Xs)`` copies the candidates into the plan's
+    inputs, replays the graph and returns ``[(value_i, grad_i)]`` (views that the
+    next call overwrites). With ``check`` (default), a problem whose status
+    reports a failed low-rank update is evaluated again on its own, through its
+    acquisition function's fallback to joint sampling.
+    """
+
+    def __init__(self, acqfs: list, shapes: list[tuple[int, int, int]]) -> None:
+        if len(acqfs) != len(shapes) or not acqfs:
+            raise ValueError("one candidate shape per acquisition function is required")
+        self.acqfs = acqfs
+        self.shapes = [tuple(int(v) for v in s) for s in shapes]
+        self.device = acqfs[0].device
+        self.handle = None
+        self.graph = None
+        self.launches = 0
+        self._build()
+
+    @staticmethod
+    def _structs(acqfs, shapes):
+        return [a._call_struct(s[1])[0] for a, s in zip(acqfs, shapes)]
+
+    @classmethod
+    def supported(cls, acqfs: list, shapes: list[tuple[int, int, int]]) -> bool:
+        structs = cls._structs(acqfs, shapes)
+        arr = (nat.BgbAcq * len(structs))(*structs)
+        b = (ctypes.c_int64 * len(shapes))(*[int(s[0]) for s in shapes])
+        return nat.lib().bgb_group_workspace_bytes(arr, b, len(structs)) > 0
+
+    def _build(self) -> None:
+        dev, lib = self.device, nat.lib()
+        self.close()
+        self.structs = self._structs(self.acqfs, self.shapes)
+        count = len(self.structs)
+        self._arr = (nat.BgbAcq * count)(*self.structs)
+        self._b = (ctypes.c_int64 * count)(*[s[0] for s in self.shapes])
+        wsb = lib.bgb_group_workspace_bytes(self._arr, self._b, count)
+        if wsb == 0:
+            raise UnsupportedError("ModelGroup members must be mixed-precision tensor-core problems "
+                                   "with a cached root, q <= 8 and r <= 4")
+        self.X = [torch.zeros(s, dtype=torch.float64, device=dev) for s in self.shapes]
+        self.out = [(torch.empty(b, dtype=torch.float64, device=dev),
+                     torch.empty(b, q, d, dtype=torch.float64, device=dev),
+                     torch.empty(b, dtype=torch.int32, device=dev)) for b, q, d in self.shapes]
+        self.ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        ptrs = lambda ts: (ctypes.c_void_p * count)(*[t.data_ptr() for t in ts])  # noqa: E731
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(dev):
+            rc = lib.bgb_group_create(self._arr, self._b, count, ptrs(self.X),
+                                      ptrs([o[0] for o in self.out]), ptrs([o[1] for o in self.out]),
+                                      ptrs([o[2] for o in self.out]), self.ws.data_ptr(), wsb,
+                                      nat.stream_handle(dev), ctypes.byref(handle))
+        nat.check(rc, "model group plan")
+        self.handle = handle
+        self.launches = int(lib.bgb_group_launches(handle))
+        # the base samples the structs point to stay alive with the plan
+        self._keep = [a._Z.get(s[1]) for a, s in zip(self.acqfs, self.shapes)]
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            nat.check(lib.bgb_group_run(self.handle, nat.stream_handle(dev)), "model group run")
+        self.graph = graph
+
+    def _stale(self) -> bool:
+        return any(a._call_struct(s[1])[0] is not st
+                   for a, s, st in zip(self.acqfs, self.shapes, self.structs))
+
+    def value_and_grad(self, Xs: list[Tensor], check: bool = True) -> list[tuple[Tensor, Tensor]]:
+        if len(Xs) != len(self.acqfs):
+            raise ValueError("one candidate tensor per acquisition function is required")
+        for x, s in zip(Xs, self.shapes):
+            if tuple(x.shape) != s:
+                raise ValueError(f"candidate shape {tuple(x.shape)} differs from the plan's {s}")
+        if self._stale():
+            self._build()
+        for dst, x in zip(self.X, Xs):
+            dst.copy_(x)
+        self.graph.replay()
+        res = [(o[0], o[1]) for o in self.out]
+        if check:
+            bad = [i for i, o in enumerate(self.out) if int(o[2].max().item()) != 0]
+            for i in bad:  # the problem's own path: fallback to joint sampling, or the error
+                res[i] = self.acqfs[i].value_and_grad_raw(self.X[i], True)
+        return res
+
+    def close(self) -> None:
+        if self.handle is not None:
+            if self.graph is not None:
+                torch.cuda.synchronize(self.device)
+            nat.lib().bgb_group_destroy(self.handle)
+            self.handle = None
+            self.graph = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # pragma: no cover - interpreter shutdown
+            pass

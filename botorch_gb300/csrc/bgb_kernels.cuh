@@ -1,5 +1,7 @@
 // Internal launchers shared between the translation units of the library.
 #pragma once
+
+#include <vector>
 #include <cuda_fp16.h>
 
 #include <cuda_runtime.h>
@@ -79,6 +81,31 @@ int gp_mll(const double* X, int64_t n, int d, const double* inv_ls, double outpu
 
 // crosscov_tc.cu ------------------------------------------------------------
 bool tc_gemm_available();
+// One GEMM of a grouped tensor-core launch (the operands of tc_gemm_f16x3).
+struct TcGroupGemm {
+    int64_t M, N, K;
+    const __half* A_hi;
+    const __half* A_lo;
+    int64_t lda;
+    const __half* B_hi;
+    const __half* B_lo;
+    int64_t ldbs;
+    float* C;
+    int64_t ldc;
+    int kmode;
+    const float* row_mul;
+    float row_mul_const;
+    const float* col_mul;
+};
+size_t tc_group_entry_bytes();
+// Device tables of a grouped launch: `entries` (tc_group_entry_bytes() per GEMM,
+// to be copied to dev_entries, 64-byte aligned), per-cluster tile ranges `off`
+// (clusters + 1) and the tile list `tiles`.
+int tc_group_build(const TcGroupGemm* gemms, int count, uintptr_t dev_entries,
+                   std::vector<unsigned char>& entries, std::vector<int>& off,
+                   std::vector<uint64_t>& tiles, int& clusters);
+int tc_group_launch(const void* dev_entries, const int* dev_off, const uint64_t* dev_tiles,
+                    int clusters, int* err, cudaStream_t stream);
 // C = diag(row_mul) A op(B) diag(col_mul) on tcgen05 tensor cores from float16
 // hi/lo splits (ah*bh + ah*bl + al*bh, float32 accumulation). A: hi/lo (M x K,
 // lda); B given by its K-major storage Bs (N x K, hi/lo, ldbs), op(B)[k][j] =

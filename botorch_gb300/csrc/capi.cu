@@ -2,7 +2,11 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
+#include <memory>
+#include <new>
+#include <vector>
 #include <cmath>
 #include <mutex>
 
@@ -166,6 +170,11 @@ void fill_qargs(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa) 
     qa->y_std = a->gp.y_std;
     qa->tau_relu = a->tau_relu;
     qa->tau_max = a->tau_max;
+    qa->inv_tau_relu_f = (float)(1.0 / a->tau_relu);
+    qa->log_tau_relu_f = (float)log(a->tau_relu);
+    qa->inv_tau_max_f = (float)(1.0 / a->tau_max);
+    qa->log_S = log((double)a->n_samples);
+    qa->sqrt_outputscale = sqrt(a->gp.outputscale);
     qa->X = X;
     qa->Xt = a->gp.train_X;
     qa->Xb = a->X_baseline;
@@ -403,6 +412,312 @@ int noalloc_scratch(cudaStream_t stream, void** out) {
     }
     *out = g_noalloc_ptr[dev];
     return BGB_OK;
+}
+
+// ---------------------------------------------------------------- grouped plans
+// Stages of a grouped run, in launch order (each one launch over all models).
+enum GroupStage : int { GS_SCALE, GS_KM, GS_QSTATS, GS_BSTEP, GS_MIX, GS_ADJ, GS_SUM, GS_FIN, GS_N };
+
+// The adjoint's register arrays are sized by a compile-time bound on d: models
+// are launched in buckets of equal bound (as their own calls would run them).
+constexpr int kDBuckets = 7;
+constexpr int kDBound[kDBuckets] = {8, 12, 16, 20, 24, 32, 64};
+inline int d_bucket(int d) {
+    for (int i = 0; i < kDBuckets; ++i)
+        if (d <= kDBound[i]) return i;
+    return -1;
+}
+
+
+// Requirements of a grouped problem: the mixed tensor-core path with a cached
+// root, q <= 8 and r <= 4 (the one-pass covariance reduction).
+int group_member_ok(const bgb_acq_t* a, int64_t b) {
+    if (!valid_acq(a) || b <= 0) return BGB_ERR_ARG;
+    if (a->n_samples <= 0 || a->Z == nullptr || a->best_f == nullptr) return BGB_ERR_ARG;
+    if (a->precision != BGB_PREC_MIXED || !use_tc(a) || joint_mode(a) != 0 || a->q > 8 ||
+        a->gp.d > 64 ||
+        a->r > 4 || a->Xs32 == nullptr || a->beta32 == nullptr || (a->r > 0 && a->Vb32 == nullptr))
+        return BGB_ERR_UNSUPPORTED;
+    return BGB_OK;
+}
+
+struct GroupSizes {
+    size_t arenas = 0, tables = 0, total = 0;
+    int64_t tiles_fwd = 0, tiles_adj = 0;
+};
+
+GroupSizes group_sizes(const bgb_acq_t* acqs, const int64_t* b, int count) {
+    GroupSizes z;
+    for (int i = 0; i < count; ++i) {
+        z.arenas += align_up(acq_ws_layout(&acqs[i], b[i], nullptr, nullptr, nullptr, nullptr, nullptr));
+        const int64_t rows = b[i] * acqs[i].q, n = acqs[i].gp.n;
+        const int64_t t = ceil_div(rows, (int64_t)256) * ceil_div(n, (int64_t)256);
+        z.tiles_fwd += t;
+        z.tiles_adj += t;
+    }
+    const size_t cnt = (size_t)count;
+    z.tables = align_up(sizeof(int)) + align_up(cnt * sizeof(KmG)) +
+               align_up(cnt * sizeof(QstatsG<float>)) + align_up(cnt * sizeof(BstepG)) +
+               align_up(cnt * sizeof(MixG<float>)) + align_up(cnt * sizeof(AdjG<float>)) +
+               GS_N * align_up((cnt + 1) * sizeof(int)) +
+               2 * kDBuckets * align_up((cnt + 1) * sizeof(int)) +
+               2 * (align_up(cnt * tc_group_entry_bytes()) + align_up(sizeof(int) * 256)) +
+               align_up(sizeof(uint64_t) * (size_t)z.tiles_fwd) +
+               align_up(sizeof(uint64_t) * (size_t)z.tiles_adj);
+    z.total = z.arenas + z.tables;
+    return z;
+}
+
+}  // namespace
+
+// The plan of a grouped run (opaque to C callers).
+struct bgb_group {
+    int count = 0;
+    int launches = 0;
+    int* err = nullptr;
+    GroupTab tab[GS_N];
+    int64_t ctas[GS_N] = {};
+    // adjoint and its finish, per d bucket (models in bucket order in the AdjG table)
+    GroupTab adj_tab[kDBuckets], fin_tab[kDBuckets];
+    int64_t adj_ctas[kDBuckets] = {}, fin_ctas[kDBuckets] = {};
+    int qmax = 0, rmax = 0, dmax = 0;
+    size_t bs_smem = 0, mix_smem = 0;
+    bool partials = false;
+    const void* tc_entries[2] = {nullptr, nullptr};
+    const int* tc_off[2] = {nullptr, nullptr};
+    const uint64_t* tc_tiles[2] = {nullptr, nullptr};
+    int tc_clusters[2] = {0, 0};
+};
+
+namespace {
+
+// Host tables of a plan, copied to the workspace in one pass.
+struct GroupBuild {
+    std::vector<KmG> km;
+    std::vector<QstatsG<float>> qs;
+    std::vector<BstepG> bs;
+    std::vector<MixG<float>> mix;
+    std::vector<AdjG<float>> adj;
+    std::vector<int> off[GS_N];
+    std::vector<TcGroupGemm> gemm[2];
+};
+
+int group_create(const bgb_acq_t* acqs, const int64_t* b, int count, const double* const* X,
+                 double* const* value, double* const* grad, int32_t* const* status,
+                 void* workspace, size_t workspace_bytes, cudaStream_t st, bgb_group** out) {
+    if (acqs == nullptr || b == nullptr || count <= 0 || X == nullptr || value == nullptr ||
+        grad == nullptr || status == nullptr || out == nullptr)
+        return BGB_ERR_ARG;
+    for (int i = 0; i < count; ++i) {
+        int rc = group_member_ok(&acqs[i], b[i]);
+        if (rc) return rc;
+        if (X[i] == nullptr || value[i] == nullptr || grad[i] == nullptr || status[i] == nullptr)
+            return BGB_ERR_ARG;
+    }
+    const GroupSizes z = group_sizes(acqs, b, count);
+    if (workspace == nullptr || workspace_bytes < z.total) return BGB_ERR_WORKSPACE;
+    char* base = static_cast<char*>(workspace);
+    auto g = std::make_unique<bgb_group>();
+    g->count = count;
+    GroupBuild hb;
+    for (int s = 0; s < GS_N; ++s) hb.off[s].assign((size_t)count + 1, 0);
+    // tables after the arenas
+    Arena tar{base + z.arenas, z.total - z.arenas, 0};
+    g->err = tar.take<int>(1);
+    KmG* d_km = tar.take<KmG>(count);
+    QstatsG<float>* d_qs = tar.take<QstatsG<float>>(count);
+    BstepG* d_bs = tar.take<BstepG>(count);
+    MixG<float>* d_mix = tar.take<MixG<float>>(count);
+    AdjG<float>* d_adj = tar.take<AdjG<float>>(count);
+    int* d_off[GS_N];
+    for (int s = 0; s < GS_N; ++s) d_off[s] = tar.take<int>(count + 1);
+    void* d_tc_ent[2];
+    int* d_tc_off[2];
+    for (int k = 0; k < 2; ++k) {
+        d_tc_ent[k] = tar.take<unsigned char>(count * tc_group_entry_bytes());
+        d_tc_off[k] = tar.take<int>(256);
+    }
+    uint64_t* d_tc_tiles[2] = {tar.take<uint64_t>(z.tiles_fwd), tar.take<uint64_t>(z.tiles_adj)};
+    int* d_boff[2][kDBuckets];
+    for (int j = 0; j < 2; ++j)
+        for (int k = 0; k < kDBuckets; ++k) d_boff[j][k] = tar.take<int>(count + 1);
+    if (d_boff[1][kDBuckets - 1] == nullptr) return BGB_ERR_WORKSPACE;
+    // per model: arena, arguments, CTA counts
+    size_t aoff = 0;
+    int64_t c[GS_N] = {};
+    for (int i = 0; i < count; ++i) {
+        const bgb_acq_t* a = &acqs[i];
+        const size_t asz = align_up(acq_ws_layout(a, b[i], nullptr, nullptr, nullptr, nullptr, nullptr));
+        Arena ar{base + aoff, asz, 0};
+        aoff += asz;
+        QBatchArgs qa;
+        memset(&qa, 0, sizeof(qa));
+        void *Kc = nullptr, *C = nullptr, *P = nullptr;
+        if (acq_ws_layout(a, b[i], &ar, &qa, &Kc, &C, &P, nullptr) == 0) return BGB_ERR_WORKSPACE;
+        fill_qargs(a, X[i], b[i], &qa);
+        qa.dev_err = g->err;
+        qa.value = value[i];
+        qa.grad = grad[i];
+        qa.status = status[i];
+        const int64_t n = a->gp.n, rows = b[i] * a->q;
+        const int d = a->gp.d;
+        __half* Khi = static_cast<__half*>(Kc);
+        __half* Klo = Khi + rows * a->ldl;
+        const float ks = kc_scale(a->gp.outputscale);
+        // base samples and incumbents in float32 once: they are fixed for the plan
+        int rc = launch_prep_samples(qa, st);
+        if (rc) return rc;
+        hb.km.push_back(KmG{X[i], a->gp.inv_lengthscale, qa.zt, rows, d, a->gp.kernel, a->Xs32, n,
+                            a->gp.outputscale, Khi, Klo, ks, a->ldl, kernel_matrix_col_tiles(n)});
+        const int64_t km_ctas = kernel_matrix_col_tiles(n) * kernel_matrix_row_tiles(rows);
+        hb.gemm[0].push_back(TcGroupGemm{rows, n, n, Khi, Klo, a->ldl,
+                                         reinterpret_cast<const __half*>(a->Lhi),
+                                         reinterpret_cast<const __half*>(a->Llo), a->ldl,
+                                         static_cast<float*>(C), a->ldb, KB_UPPER, nullptr, 1.f / ks,
+                                         a->Lmul});
+        auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) % 16) == 0; };
+        const int vec_ok = (a->ldb % 4 == 0) && (n % 4 == 0) && al16(C) && al16(a->beta32) &&
+                           (a->r == 0 || al16(a->Vb32));
+        hb.qs.push_back(QstatsG<float>{qa, static_cast<const float*>(C), a->ldb, a->beta32,
+                                       a->Vb32, vec_ok});
+        hb.bs.push_back(BstepG{qa, 1});
+        const int64_t mgx = mix_rows_groups(qa, 1);
+        hb.mix.push_back(MixG<float>{qa, static_cast<const float*>(C), a->ldb, a->Vb32, a->beta32,
+                                     nullptr, Khi, Klo, a->ldl, mgx});
+        hb.gemm[1].push_back(TcGroupGemm{rows, n, n, Khi, Klo, a->ldl,
+                                         reinterpret_cast<const __half*>(a->LThi),
+                                         reinterpret_cast<const __half*>(a->LTlo), a->ldl,
+                                         static_cast<float*>(C), a->ldb, KB_LOWER, qa.hmul, 1.f,
+                                         a->LTmul});
+        int64_t rb, nslab, slab;
+        adjoint_split(qa, kc_region_elems(a, rows), &rb, &nslab, &slab);
+        // slab partials (d x rows per slab) go to the Kc region, which holds rows x ldl
+        if ((int64_t)d * rows > kc_region_elems(a, rows)) return BGB_ERR_UNSUPPORTED;
+        hb.adj.push_back(AdjG<float>{qa, static_cast<const float*>(C), a->ldb, a->Xs32, slab,
+                                     static_cast<float*>(Kc), rb, (int)nslab});
+        if (nslab > 1) g->partials = true;
+        const int64_t per[GS_N] = {ceil_div(rows * d, (int64_t)256), km_ctas, b[i], b[i], mgx * b[i],
+                                   rb * nslab, ceil_div((int64_t)d * rows, (int64_t)256),
+                                   ceil_div(rows, (int64_t)128)};
+        for (int s = 0; s < GS_N; ++s) {
+            c[s] += per[s];
+            hb.off[s][i + 1] = (int)c[s];
+            if (c[s] > 0x7fffffff) return BGB_ERR_UNSUPPORTED;
+        }
+        g->qmax = std::max(g->qmax, a->q);
+        g->rmax = std::max(g->rmax, a->r);
+        g->dmax = std::max(g->dmax, d);
+        g->bs_smem = std::max(g->bs_smem, batch_step_f32_smem(a->q, a->r, a->n_samples));
+        g->mix_smem = std::max(g->mix_smem, mix_rows_smem_bytes(qa));
+    }
+    if (!g->partials) {  // one slab everywhere: the adjoint finishes its rows itself
+        c[GS_SUM] = c[GS_FIN] = 0;
+        for (auto& e : hb.adj) e.part = nullptr;
+    }
+    // adjoint tables in d-bucket order: one launch per bucket
+    std::vector<int> order((size_t)count);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return d_bucket(acqs[x].gp.d) < d_bucket(acqs[y].gp.d);
+    });
+    std::vector<AdjG<float>> adj_sorted;
+    std::vector<int> sum_off(1, 0);
+    std::vector<int> boff[2][kDBuckets];
+    int bstart[kDBuckets + 1] = {};
+    for (int k = 0, pos = 0; k < kDBuckets; ++k) {
+        bstart[k] = pos;
+        boff[0][k].assign(1, 0);
+        boff[1][k].assign(1, 0);
+        for (; pos < count && d_bucket(acqs[order[pos]].gp.d) == k; ++pos) {
+            const AdjG<float>& e = hb.adj[order[pos]];
+            const int64_t rows = e.a.b * e.a.q;
+            adj_sorted.push_back(e);
+            boff[0][k].push_back(boff[0][k].back() + (int)(e.gx * e.nslab));
+            boff[1][k].push_back(boff[1][k].back() + (int)ceil_div(rows, (int64_t)128));
+            sum_off.push_back(sum_off.back() + (int)ceil_div((int64_t)e.a.d * rows, (int64_t)256));
+        }
+        bstart[k + 1] = pos;
+    }
+    hb.adj.swap(adj_sorted);
+    hb.off[GS_SUM] = sum_off;
+    // tensor-core tile schedules
+    std::vector<unsigned char> ent[2];
+    std::vector<int> toff[2];
+    std::vector<uint64_t> tiles[2];
+    for (int k = 0; k < 2; ++k) {
+        int rc = tc_group_build(hb.gemm[k].data(), count, reinterpret_cast<uintptr_t>(d_tc_ent[k]),
+                                ent[k], toff[k], tiles[k], g->tc_clusters[k]);
+        if (rc) return rc;
+        if ((int64_t)tiles[k].size() > (k == 0 ? z.tiles_fwd : z.tiles_adj) || toff[k].size() > 256)
+            return BGB_ERR_UNSUPPORTED;
+    }
+    // upload (pageable host memory: the copies complete before the synchronise below)
+    auto up = [&](void* dst, const void* src, size_t bytes) -> int {
+        if (bytes == 0) return BGB_OK;
+        BGB_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+        return BGB_OK;
+    };
+    int rc = up(d_km, hb.km.data(), sizeof(KmG) * count);
+    if (!rc) rc = up(d_qs, hb.qs.data(), sizeof(QstatsG<float>) * count);
+    if (!rc) rc = up(d_bs, hb.bs.data(), sizeof(BstepG) * count);
+    if (!rc) rc = up(d_mix, hb.mix.data(), sizeof(MixG<float>) * count);
+    if (!rc) rc = up(d_adj, hb.adj.data(), sizeof(AdjG<float>) * count);
+    for (int s = 0; !rc && s < GS_N; ++s) rc = up(d_off[s], hb.off[s].data(), sizeof(int) * (count + 1));
+    for (int k = 0; !rc && k < 2; ++k) {
+        rc = up(d_tc_ent[k], ent[k].data(), ent[k].size());
+        if (!rc) rc = up(d_tc_off[k], toff[k].data(), sizeof(int) * toff[k].size());
+        if (!rc) rc = up(d_tc_tiles[k], tiles[k].data(), sizeof(uint64_t) * tiles[k].size());
+    }
+    for (int j = 0; !rc && j < 2; ++j)
+        for (int k = 0; !rc && k < kDBuckets; ++k)
+            rc = up(d_boff[j][k], boff[j][k].data(), sizeof(int) * boff[j][k].size());
+    if (rc) return rc;
+    BGB_CUDA_TRY(cudaStreamSynchronize(st));
+    const void* args[GS_N] = {d_km, d_km, d_qs, d_bs, d_mix, d_adj, d_adj, d_adj};
+    for (int s = 0; s < GS_N; ++s) {
+        g->tab[s] = GroupTab{count, d_off[s], args[s]};
+        g->ctas[s] = c[s];
+    }
+    for (int k = 0; k < 2; ++k) {
+        g->tc_entries[k] = d_tc_ent[k];
+        g->tc_off[k] = d_tc_off[k];
+        g->tc_tiles[k] = d_tc_tiles[k];
+    }
+    int nb = 0;
+    for (int k = 0; k < kDBuckets; ++k) {
+        const int nm = bstart[k + 1] - bstart[k];
+        g->adj_tab[k] = GroupTab{nm, d_boff[0][k], d_adj + bstart[k]};
+        g->fin_tab[k] = GroupTab{nm, d_boff[1][k], d_adj + bstart[k]};
+        g->adj_ctas[k] = nm > 0 ? boff[0][k].back() : 0;
+        g->fin_ctas[k] = nm > 0 && g->partials ? boff[1][k].back() : 0;
+        nb += nm > 0 ? 1 : 0;
+    }
+    g->ctas[GS_SUM] = g->partials ? sum_off.back() : 0;
+    g->launches = 7 + nb + (g->partials ? 1 + nb : 0);
+    *out = g.release();
+    return BGB_OK;
+}
+
+int group_run(const bgb_group* g, cudaStream_t st) {
+    BGB_CUDA_TRY(cudaMemsetAsync(g->err, 0, sizeof(int), st));
+    int rc = launch_kernel_matrix_group(g->tab[GS_SCALE], g->ctas[GS_SCALE], g->tab[GS_KM],
+                                        g->ctas[GS_KM], st);
+    if (!rc) rc = tc_group_launch(g->tc_entries[0], g->tc_off[0], g->tc_tiles[0], g->tc_clusters[0],
+                                  g->err, st);
+    if (!rc) rc = launch_qstats_group(g->tab[GS_QSTATS], g->qmax, g->rmax, g->ctas[GS_QSTATS], st);
+    if (!rc) rc = launch_batch_step_group(g->tab[GS_BSTEP], g->qmax, g->bs_smem, g->ctas[GS_BSTEP], st);
+    if (!rc) rc = launch_mix_rows_group(g->tab[GS_MIX], g->qmax, g->mix_smem, g->ctas[GS_MIX], st);
+    if (!rc) rc = tc_group_launch(g->tc_entries[1], g->tc_off[1], g->tc_tiles[1], g->tc_clusters[1],
+                                  g->err, st);
+    for (int k = 0; !rc && k < kDBuckets; ++k)
+        rc = launch_adjoint_group(g->adj_tab[k], kDBound[k], g->partials, g->adj_ctas[k], st);
+    for (int k = 0, first = 1; !rc && g->partials && k < kDBuckets; ++k) {
+        if (g->fin_ctas[k] == 0) continue;
+        rc = launch_adjoint_finish_group(g->tab[GS_SUM], first ? g->ctas[GS_SUM] : 0, g->fin_tab[k],
+                                         kDBound[k], g->fin_ctas[k], st);
+        first = 0;
+    }
+    return rc;
 }
 
 }  // namespace
@@ -732,5 +1047,33 @@ int bgb_acq_forward_backward_timed(const bgb_acq_t* acq, const double* X, int64_
     for (int i = 0; i <= kStages; ++i) cudaEventDestroy(ev[i]);
     return rc;
 }
+
+size_t bgb_group_workspace_bytes(const bgb_acq_t* acqs, const int64_t* b, int32_t count) {
+    if (acqs == nullptr || b == nullptr || count <= 0) return 0;
+    for (int i = 0; i < count; ++i)
+        if (group_member_ok(&acqs[i], b[i]) != BGB_OK) return 0;
+    return group_sizes(acqs, b, count).total;
+}
+
+int bgb_group_create(const bgb_acq_t* acqs, const int64_t* b, int32_t count,
+                     const double* const* X, double* const* value, double* const* grad,
+                     int32_t* const* status, void* workspace, size_t workspace_bytes, void* stream,
+                     bgb_group_t** out) {
+    try {
+        return group_create(acqs, b, count, X, value, grad, status, workspace, workspace_bytes,
+                            as_stream(stream), out);
+    } catch (const std::bad_alloc&) {
+        return BGB_ERR_ARG;
+    }
+}
+
+int bgb_group_run(const bgb_group_t* group, void* stream) {
+    if (group == nullptr) return BGB_ERR_ARG;
+    return group_run(group, as_stream(stream));
+}
+
+int32_t bgb_group_launches(const bgb_group_t* group) { return group ? group->launches : 0; }
+
+void bgb_group_destroy(bgb_group_t* group) { delete group; }
 
 }  // extern "C"

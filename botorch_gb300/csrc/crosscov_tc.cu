@@ -336,15 +336,34 @@ struct TcTail {
     uint32_t tiles[TC_MAX_TAIL];  // m_tile << 8 | n_tile
 };
 
-// The tiles of one cluster, in order: the static rounds (both tiles of each
-// super-tile), then the cluster's share of the tail.
-struct TileIter {
+// One GEMM of a launch: its operand maps, sizes and scale vectors. A single
+// GEMM's record is a kernel parameter; a group's records sit in device memory.
+struct TcProblem {
+    const TcMaps* maps;
+    const float* row_mul;  // nullptr: row_mul_const for every row
+    const float* col_mul;
+    float row_mul_const;
+    int M, N, K, kmode;
+};
+
+// k-blocks of column block n_tile of a problem (its kmode's triangular range)
+__device__ __forceinline__ void problem_k_range(const TcProblem* p, int n_tile, int& kbeg,
+                                                int& nkb) {
+    const TileSched ks(1, 1, p->kmode);
+    ks.k_range(n_tile, p->K, kbeg, nkb);
+}
+
+// The tiles of one cluster of a single GEMM, in order: the static rounds (both
+// tiles of each super-tile), then the cluster's share of the tail.
+struct SingleIter {
     const TileSched& sched;
     const TcTail& tail;
+    const TcProblem* prob;
     int cluster, ncl, i;
-    __device__ TileIter(const TileSched& s, const TcTail& t, int c, int n)
-        : sched(s), tail(t), cluster(c), ncl(n), i(0) {}
-    __device__ bool next(int& m_tile, int& n_tile) {
+    __device__ SingleIter(const TileSched& s, const TcTail& t, const TcProblem* p, int c, int n)
+        : sched(s), tail(t), prob(p), cluster(c), ncl(n), i(0) {}
+    __device__ bool next(int& m_tile, int& n_tile, const TcProblem*& p) {
+        p = prob;
         const int nst = 2 * tail.static_rounds;
         while (i < nst) {
             const int r = i >> 1, h = i & 1;
@@ -362,17 +381,58 @@ struct TileIter {
     }
 };
 
+// A group of independent GEMMs in one launch (many models of uneven size): the
+// host deals every (problem, row block, column block) tile out to the clusters
+// (largest k range first, to the least-loaded cluster); cluster c runs
+// tiles[off[c] .. off[c + 1]).
+struct TcGroupEntry {
+    TcMaps maps;
+    TcProblem p;  // p.maps points at this entry's maps
+};
+struct TcGroupDev {
+    const TcGroupEntry* entries;
+    const int* off;
+    const uint64_t* tiles;  // problem << 40 | m_tile << 16 | n_tile
+};
+
+struct GroupIter {
+    const TcGroupDev& g;
+    int e, end;
+    int last = -1;
+    __device__ GroupIter(const TcGroupDev& gd, int c) : g(gd), e(gd.off[c]), end(gd.off[c + 1]) {}
+    __device__ bool next(int& m_tile, int& n_tile, const TcProblem*& p) {
+        if (e >= end) return false;
+        const uint64_t t = g.tiles[e++];
+        const int prob = (int)(t >> 40);
+        m_tile = (int)((t >> 16) & 0xFFFFFFull);
+        n_tile = (int)(t & 0xFFFFull);
+        p = &g.entries[prob].p;
+        if (prob != last) {
+            // the maps were written through the generic proxy (a copy from the host)
+            const TcMaps* mp = &g.entries[prob].maps;
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&mp->a_hi)
+                         : "memory");
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&mp->a_lo)
+                         : "memory");
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&mp->b_hi)
+                         : "memory");
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&mp->b_lo)
+                         : "memory");
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&mp->c)
+                         : "memory");
+            last = prob;
+        }
+        return true;
+    }
+};
+
 // kmode: KB_UPPER (forward, k < n0 + BN), KB_LOWER (adjoint, k >= n0) or KFULL.
 // Persistent: each CTA (PAIR = 2: each cluster of two CTAs, rank 0 issuing the
 // MMAs) walks the tiles of the static schedule above. TMEM is allocated once;
 // the stage and accumulator counters run on across tiles, so the next tile's
 // loads and MMAs proceed while the epilogue warps store the previous tile.
-template <int PAIR>
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_gemm_kernel(const __grid_constant__ TcMaps maps, const __grid_constant__ TcTail tail,
-                   int M, int N, int K, int kmode,
-                   int m_tiles, int n_tiles, const float* __restrict__ row_mul,
-                   float row_mul_const, const float* __restrict__ col_mul, int* __restrict__ err) {
+template <int PAIR, class MakeIter>
+__device__ __forceinline__ void tc_gemm_body(const MakeIter& make_iter, int* __restrict__ err) {
     using Cfg = TcCfg<PAIR>;
     constexpr int STAGES = Cfg::STAGES;
     extern __shared__ __align__(1024) uint8_t smraw[];
@@ -389,8 +449,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const uint32_t rank = (PAIR == 2) ? cluster_rank() : 0u;
     const bool leader = (rank == 0);
-    const int cluster = blockIdx.x / PAIR, nclusters = gridDim.x / PAIR;
-    const TileSched sched(m_tiles, n_tiles, kmode);
+    const int cluster = blockIdx.x / PAIR;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -415,12 +474,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // ---------------- TMA producer (each CTA loads its own rows of A and of B)
         int g = 0;  // k-blocks issued by this CTA
         bool stop = false;
-        TileIter it(sched, tail, cluster, nclusters);
+        auto it = make_iter(cluster);
         int m_tile, n_tile;
-        while (!stop && it.next(m_tile, n_tile)) {
+        const TcProblem* pr;
+        while (!stop && it.next(m_tile, n_tile, pr)) {
             {
                 int kbeg, nkb;
-                sched.k_range(n_tile, K, kbeg, nkb);
+                problem_k_range(pr, n_tile, kbeg, nkb);
                 const int arow = m_tile * TC_BM * PAIR + (int)rank * TC_BM;
                 const int brow = n_tile * TC_BN + (int)rank * Cfg::B_ROWS;
                 for (int kb = 0; kb < nkb; ++kb, ++g) {
@@ -440,10 +500,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     if (leader) mbar_expect_tx(&full[st], Cfg::TX_BYTES);
                     const uint32_t bar =
                         (PAIR == 2) ? peer_addr(smem_u32(&full[st]), 0) : smem_u32(&full[st]);
-                    tma_load_2d<PAIR>(sp, &maps.a_hi, bar, k, arow);
-                    tma_load_2d<PAIR>(sp + A_TILE, &maps.a_lo, bar, k, arow);
-                    tma_load_2d<PAIR>(sp + 2 * A_TILE, &maps.b_hi, bar, k, brow);
-                    tma_load_2d<PAIR>(sp + 2 * A_TILE + Cfg::B_TILE, &maps.b_lo, bar, k, brow);
+                    const TcMaps* mp = pr->maps;
+                    tma_load_2d<PAIR>(sp, &mp->a_hi, bar, k, arow);
+                    tma_load_2d<PAIR>(sp + A_TILE, &mp->a_lo, bar, k, arow);
+                    tma_load_2d<PAIR>(sp + 2 * A_TILE, &mp->b_hi, bar, k, brow);
+                    tma_load_2d<PAIR>(sp + 2 * A_TILE + Cfg::B_TILE, &mp->b_lo, bar, k, brow);
                 }
             }
         }
@@ -458,12 +519,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // ---------------- MMA issuer (the leader CTA of the pair)
         int g = 0, cg = 0;  // k-blocks consumed, accumulator chunks started
         bool stop = false;
-        TileIter it(sched, tail, cluster, nclusters);
+        auto it = make_iter(cluster);
         int m_tile, n_tile;
-        while (!stop && it.next(m_tile, n_tile)) {
+        const TcProblem* pr;
+        while (!stop && it.next(m_tile, n_tile, pr)) {
             {
                 int kbeg, nkb;
-                sched.k_range(n_tile, K, kbeg, nkb);
+                problem_k_range(pr, n_tile, kbeg, nkb);
                 const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
                 for (int c = 0; c < nch && !stop; ++c, ++cg) {
                     const int a = cg & 1;
@@ -515,12 +577,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         float* stg = staging + (warp - 2) * 32 * 32;
         int cg = 0;
         bool good = true;
-        TileIter it(sched, tail, cluster, nclusters);
+        auto it = make_iter(cluster);
         int m_tile, n_tile;
-        while (good && it.next(m_tile, n_tile)) {
+        const TcProblem* pr;
+        while (good && it.next(m_tile, n_tile, pr)) {
             {
                 int kbeg, nkb;
-                sched.k_range(n_tile, K, kbeg, nkb);
+                problem_k_range(pr, n_tile, kbeg, nkb);
                 const int nch = (nkb + TC_FLUSH - 1) / TC_FLUSH;
                 const int row0 = m_tile * TC_BM * PAIR + (int)rank * TC_BM + quarter * 32;
                 const int row = row0 + lane;
@@ -563,7 +626,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 // v ^ (i % 8)) and one lane issues a TMA store of it, so global writes are
                 // whole 128-byte row segments; the TMA clips rows >= M and columns >= N
                 const int c0 = n_tile * TC_BN + half * (TC_BN / 2);
-                const float rm = row < M ? (row_mul != nullptr ? row_mul[row] : row_mul_const) : 0.f;
+                const int M = pr->M, N = pr->N;
+                const float* row_mul = pr->row_mul;
+                const float* col_mul = pr->col_mul;
+                const float rm = row < M ? (row_mul != nullptr ? row_mul[row] : pr->row_mul_const) : 0.f;
 #pragma unroll
                 for (int j = 0; j < TC_BN / 2 / 32; ++j) {
                     if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
@@ -588,7 +654,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
                     if (lane == 0) {
-                        tma_store_2d(&maps.c, stg, c0 + j * 32, row0);
+                        tma_store_2d(&pr->maps->c, stg, c0 + j * 32, row0);
                         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                     }
                 }
@@ -615,6 +681,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tmem_dealloc<PAIR>(tmem);
     }
     if (threadIdx.x == 0 && *fail) atomicExch(err, *fail);
+}
+
+// One GEMM: the maps, the tail schedule and the problem record are parameters.
+template <int PAIR>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_gemm_kernel(const __grid_constant__ TcMaps maps, const __grid_constant__ TcTail tail,
+                   int M, int N, int K, int kmode, int m_tiles, int n_tiles,
+                   const float* __restrict__ row_mul, float row_mul_const,
+                   const float* __restrict__ col_mul, int* __restrict__ err) {
+    const TileSched sched(m_tiles, n_tiles, kmode);
+    const TcProblem prob{&maps, row_mul, col_mul, row_mul_const, M, N, K, kmode};
+    const int ncl = gridDim.x / PAIR;
+    auto make_iter = [&](int cluster) { return SingleIter(sched, tail, &prob, cluster, ncl); };
+    tc_gemm_body<PAIR>(make_iter, err);
+}
+
+// A group of GEMMs: records, maps and the tile list in device memory.
+template <int PAIR>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_gemm_group_kernel(const __grid_constant__ TcGroupDev grp, int* __restrict__ err) {
+    auto make_iter = [&](int cluster) { return GroupIter(grp, cluster); };
+    tc_gemm_body<PAIR>(make_iter, err);
 }
 
 // Power-of-two scale that brings the largest magnitude m of a row to at most
@@ -835,7 +923,140 @@ int launch_tc(const TcMaps& maps, int64_t M, int64_t N, int64_t K, int kmode, in
     return BGB_OK;
 }
 
+// Clusters of two that can be resident at once for the grouped kernel, per device
+// (after its shared-memory opt-in).
+int group_resident_clusters() {
+    static int cached[64] = {};
+    static bool attr_set[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kNumSMs / 2;
+    if (!attr_set[dev]) {
+        if (cudaFuncSetAttribute(tc_gemm_group_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)TcCfg<2>::SMEM) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        attr_set[dev] = true;
+    }
+    if (cached[dev] == 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2 * 64);
+        cfg.blockDim = dim3(TC_THREADS);
+        cfg.dynamicSmemBytes = TcCfg<2>::SMEM;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, tc_gemm_group_kernel<2>, &cfg) != cudaSuccess ||
+            n <= 0) {
+            cudaGetLastError();
+            n = kNumSMs / 2;
+        }
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
 }  // namespace
+
+size_t tc_group_entry_bytes() { return sizeof(TcGroupEntry); }
+
+// Device tables of a grouped launch (two-SM form) into host buffers: one entry
+// per GEMM (its maps and record; the record's maps pointer is the entry's
+// address in dev_entries), and every (GEMM, row block, column block) tile dealt
+// out largest k range first to the least-loaded of `clusters` clusters.
+int tc_group_build(const TcGroupGemm* gemms, int count, uintptr_t dev_entries,
+                   std::vector<unsigned char>& entries, std::vector<int>& off,
+                   std::vector<uint64_t>& tiles, int& clusters) {
+    if (count <= 0 || count >= (1 << 23)) return BGB_ERR_ARG;
+    if (!tc_gemm_available()) return BGB_ERR_UNSUPPORTED;
+    std::vector<TcGroupEntry> ent((size_t)count);
+    struct Item { int nkb; uint64_t code; };
+    std::vector<Item> items;
+    for (int i = 0; i < count; ++i) {
+        const TcGroupGemm& g = gemms[i];
+        if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.col_mul == nullptr ||
+            (reinterpret_cast<uintptr_t>(g.col_mul) & 15) != 0)
+            return BGB_ERR_ARG;
+        if (g.kmode != KB_UPPER && g.kmode != KB_LOWER && g.kmode != KFULL) return BGB_ERR_ARG;
+        TcMaps& mp = ent[i].maps;
+        const int b_rows = TC_BN / 2;
+        if (!make_map(&mp.a_hi, g.A_hi, g.M, g.K, g.lda, TC_BM) ||
+            !make_map(&mp.a_lo, g.A_lo, g.M, g.K, g.lda, TC_BM) ||
+            !make_map(&mp.b_hi, g.B_hi, g.N, g.K, g.ldbs, b_rows) ||
+            !make_map(&mp.b_lo, g.B_lo, g.N, g.K, g.ldbs, b_rows) ||
+            !make_map_f32(&mp.c, g.C, g.M, g.N, g.ldc))
+            return BGB_ERR_UNSUPPORTED;
+        ent[i].p = TcProblem{reinterpret_cast<const TcMaps*>(dev_entries + (uintptr_t)i * sizeof(TcGroupEntry)),
+                             g.row_mul, g.col_mul, g.row_mul_const, (int)g.M, (int)g.N, (int)g.K,
+                             g.kmode};
+        const int64_t m_tiles = ceil_div(g.M, (int64_t)TC_BM * 2);
+        const int64_t n_tiles = ceil_div(g.N, (int64_t)TC_BN);
+        if (m_tiles >= (1 << 24) || n_tiles >= (1 << 16)) return BGB_ERR_UNSUPPORTED;
+        const TileSched ks(1, 1, g.kmode);
+        for (int64_t mt = 0; mt < m_tiles; ++mt) {
+            for (int64_t nt = 0; nt < n_tiles; ++nt) {
+                int kbeg, nkb;
+                ks.k_range((int)nt, (int)g.K, kbeg, nkb);
+                items.push_back({nkb, ((uint64_t)i << 40) | ((uint64_t)mt << 16) | (uint64_t)nt});
+            }
+        }
+    }
+    const int resident = group_resident_clusters();
+    if (resident <= 0) return BGB_ERR_UNSUPPORTED;
+    clusters = (int)items.size() < resident ? (int)items.size() : resident;
+    std::stable_sort(items.begin(), items.end(),
+                     [](const Item& a, const Item& b) { return a.nkb > b.nkb; });
+    constexpr int kTileCost = 2;  // about two k-blocks of exposed epilogue per tile
+    std::vector<long> load((size_t)clusters, 0);
+    std::vector<std::vector<uint64_t>> lists((size_t)clusters);
+    for (const Item& it : items) {
+        int c = 0;
+        for (int j = 1; j < clusters; ++j)
+            if (load[j] < load[c]) c = j;
+        lists[c].push_back(it.code);
+        load[c] += it.nkb + kTileCost;
+    }
+    off.assign((size_t)clusters + 1, 0);
+    tiles.clear();
+    for (int c = 0; c < clusters; ++c) {
+        off[c] = (int)tiles.size();
+        tiles.insert(tiles.end(), lists[c].begin(), lists[c].end());
+    }
+    off[clusters] = (int)tiles.size();
+    entries.resize(sizeof(TcGroupEntry) * (size_t)count);
+    memcpy(entries.data(), ent.data(), entries.size());
+    return BGB_OK;
+}
+
+int tc_group_launch(const void* dev_entries, const int* dev_off, const uint64_t* dev_tiles,
+                    int clusters, int* err, cudaStream_t stream) {
+    if (clusters <= 0) return BGB_OK;
+    if (dev_entries == nullptr || dev_off == nullptr || dev_tiles == nullptr ||
+        (reinterpret_cast<uintptr_t>(dev_entries) & 63) != 0)
+        return BGB_ERR_ARG;
+    if (group_resident_clusters() <= 0) return BGB_ERR_UNSUPPORTED;
+    TcGroupDev grp{static_cast<const TcGroupEntry*>(dev_entries), dev_off, dev_tiles};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(clusters * 2));
+    cfg.blockDim = dim3(TC_THREADS);
+    cfg.dynamicSmemBytes = TcCfg<2>::SMEM;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    BGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, tc_gemm_group_kernel<2>, grp, err));
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
 
 bool tc_gemm_available() { return encode_fn() != nullptr; }
 

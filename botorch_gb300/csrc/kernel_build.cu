@@ -9,6 +9,7 @@
 // per output = sizeof(TOut).
 #include "bgb_common.cuh"
 #include "bgb_kernels.cuh"
+#include "bgb_qbatch.cuh"
 
 namespace bgb {
 
@@ -22,19 +23,19 @@ constexpr int KB_DCHUNK = 32;
 // is the scaled float16 split for the tensor-core GEMM: with w = k16_scale * v,
 // K16 = f16(w), K16_lo = f16(w - K16) (K is not written).
 template <typename TIn, typename TAcc, typename TOut>
-__global__ void __launch_bounds__(256) kernel_matrix_kernel(
+__device__ __forceinline__ void kernel_matrix_body(
     const TIn* __restrict__ X1, int64_t m, const TIn* __restrict__ X2, int64_t n2, int d,
     const double* __restrict__ inv_ls, double outputscale, int kind, double diag_add,
     int same, TOut* __restrict__ K, int64_t ldk, __half* __restrict__ K16,
     __half* __restrict__ K16_lo, float k16_scale, const float* __restrict__ Z1T, int64_t ldz1,
-    const float* __restrict__ Z2T, int64_t ldz2) {
+    const float* __restrict__ Z2T, int64_t ldz2, int64_t bx, int64_t by) {
     __shared__ __align__(16) TAcc s1[KB_DCHUNK][KB_TILE];
     __shared__ __align__(16) TAcc s2[KB_DCHUNK][KB_TILE];
     // thread (tx, ty): rows 4 ty + u, columns 4 tx + v (u, v < 4): the row and
     // column coordinates are 16-byte shared loads per k (broadcast within a
     // half-warp) and the outputs are vector stores of 4 consecutive entries
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int64_t row0 = (int64_t)blockIdx.y * KB_TILE, col0 = (int64_t)blockIdx.x * KB_TILE;
+    const int64_t row0 = by * KB_TILE, col0 = bx * KB_TILE;
     TAcc acc[4][4];
     float2 acc2[4][2];  // packed accumulators of the float32 form
 #pragma unroll
@@ -156,7 +157,71 @@ __global__ void __launch_bounds__(256) kernel_matrix_kernel(
     }
 }
 
+template <typename TIn, typename TAcc, typename TOut>
+__global__ void __launch_bounds__(256) kernel_matrix_kernel(
+    const TIn* __restrict__ X1, int64_t m, const TIn* __restrict__ X2, int64_t n2, int d,
+    const double* __restrict__ inv_ls, double outputscale, int kind, double diag_add,
+    int same, TOut* __restrict__ K, int64_t ldk, __half* __restrict__ K16,
+    __half* __restrict__ K16_lo, float k16_scale, const float* __restrict__ Z1T, int64_t ldz1,
+    const float* __restrict__ Z2T, int64_t ldz2) {
+    kernel_matrix_body<TIn, TAcc, TOut>(X1, m, X2, n2, d, inv_ls, outputscale, kind, diag_add,
+                                        same, K, ldk, K16, K16_lo, k16_scale, Z1T, ldz1, Z2T, ldz2,
+                                        blockIdx.x, blockIdx.y);
+}
+
+// Model of this CTA in a grouped launch: the largest m with off[m] <= blockIdx.x.
+__device__ __forceinline__ int km_group_model(const GroupTab& t) {
+    int lo = 0, hi = t.nm - 1;
+    const int b = (int)blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (t.off[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// grouped: candidates scaled by 1 / lengthscale into k-major float32 (zt)
+__global__ void scale_rows_group_kernel(const GroupTab t) {
+    const int m = km_group_model(t);
+    const KmG& g = static_cast<const KmG*>(t.args)[m];
+    const int64_t idx = ((int64_t)blockIdx.x - t.off[m]) * blockDim.x + threadIdx.x;
+    if (idx >= g.rows * g.d) return;
+    const int64_t i = idx / g.d;
+    const int k = (int)(idx % g.d);
+    g.zt[(int64_t)k * g.rows + i] = (float)(g.X[idx] * g.inv_ls[k]);
+}
+
+// grouped: K(X, Xt) of every model as its scaled float16 split; model m's CTAs
+// cover its (column tile, row tile) grid row-major in row tiles
+__global__ void __launch_bounds__(256) kernel_matrix_group_kernel(const GroupTab t) {
+    const int m = km_group_model(t);
+    const KmG& g = static_cast<const KmG*>(t.args)[m];
+    const int64_t lb = (int64_t)blockIdx.x - t.off[m];
+    kernel_matrix_body<float, float, float>(nullptr, g.rows, nullptr, g.n, g.d, nullptr,
+                                            g.outputscale, g.kind, 0.0, 0, nullptr, g.ldk, g.K16,
+                                            g.K16_lo, g.k16_scale, g.zt, g.rows, g.Xs32, g.n,
+                                            lb % g.gx, lb / g.gx);
+}
+
 }  // namespace
+
+int64_t kernel_matrix_col_tiles(int64_t n) { return ceil_div(n, (int64_t)KB_TILE); }
+int64_t kernel_matrix_row_tiles(int64_t m) { return ceil_div(m, (int64_t)KB_TILE); }
+
+int launch_kernel_matrix_group(const GroupTab& t_scale, int64_t total_scale, const GroupTab& t_km,
+                               int64_t total_km, cudaStream_t stream) {
+    if (total_scale > 0x7fffffff || total_km > 0x7fffffff) return BGB_ERR_UNSUPPORTED;
+    if (total_scale > 0) {
+        scale_rows_group_kernel<<<(unsigned)total_scale, 256, 0, stream>>>(t_scale);
+        BGB_CHECK_LAUNCH();
+    }
+    if (total_km > 0) {
+        kernel_matrix_group_kernel<<<(unsigned)total_km, 256, 0, stream>>>(t_km);
+        BGB_CHECK_LAUNCH();
+    }
+    return BGB_OK;
+}
 
 template <typename TIn, typename TAcc, typename TOut>
 int launch_kernel_matrix(const TIn* X1, int64_t m, const TIn* X2, int64_t n2, int d,

@@ -253,21 +253,37 @@ __device__ __forceinline__ void add_pair(T& h, T& l, T bh, T bl) {
     l = l + bl + e;
 }
 
+// Model of this CTA in a grouped launch: the largest m with off[m] <= blockIdx.x.
+__device__ __forceinline__ int group_model(const GroupTab& t) {
+    int lo = 0, hi = t.nm - 1;
+    const int b = (int)blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (t.off[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 constexpr int kQstatsThreads = 128;  // 8 columns of 4 per thread at n = 4096: the tail reduction is paid per 128 threads
 
 // outputscale * kappa between row `ri` of X and row `rj` of X (rj >= 0) or
 // baseline point `kb` (rj < 0). Float path (T = float with a.zt set): float32
 // over the scaled candidate coordinates a.zt, like the float32 kernel build;
 // otherwise float64.
+// zb: the baseline points' scaled coordinates (float, r x d) when staged by the
+// caller, else nullptr.
 template <typename T>
-__device__ __forceinline__ double kernel_pair(const QBatchArgs& a, int64_t ri, int64_t rj, int kb) {
+__device__ __forceinline__ double kernel_pair(const QBatchArgs& a, int64_t ri, int64_t rj, int kb,
+                                              const float* zb = nullptr) {
     const int d = a.d;
     if (sizeof(T) == 4 && a.zt != nullptr) {
         const int64_t rows = a.b * a.q;
         float r2 = 0.f;
         for (int k = 0; k < d; ++k) {
             const float zj = rj >= 0 ? a.zt[(int64_t)k * rows + rj]
-                                     : (float)(a.Xb[(int64_t)kb * d + k] * a.inv_ls[k]);
+                                     : (zb != nullptr ? zb[kb * d + k]
+                                                      : (float)(a.Xb[(int64_t)kb * d + k] * a.inv_ls[k]));
             const float df = a.zt[(int64_t)k * rows + ri] - zj;
             r2 = fmaf(df, df, r2);
         }
@@ -289,9 +305,9 @@ struct PadPow2 {
 };
 
 template <typename T, int QMAX, int RM>
-__global__ void __launch_bounds__(kQstatsThreads) qstats_kernel(QBatchArgs a, const T* __restrict__ V,
-                                                                int64_t ldv, const T* __restrict__ beta,
-                                                                const T* __restrict__ Vb, int vec_ok) {
+__device__ __forceinline__ void qstats_body(const QBatchArgs& a, const T* __restrict__ V,
+                                            int64_t ldv, const T* __restrict__ beta,
+                                            const T* __restrict__ Vb, int vec_ok, int64_t bidx_) {
     using VT = typename Vec16<T>::type;
     constexpr int E = Vec16<T>::E;
     constexpr int NG = QMAX * (QMAX + 1) / 2;
@@ -299,7 +315,7 @@ __global__ void __launch_bounds__(kQstatsThreads) qstats_kernel(QBatchArgs a, co
     constexpr int NPAD = PadPow2<NV>::value;
     constexpr int NPL = NPAD / 32;  // totals per lane after the butterfly
     const int q = a.q, r = a.r, tid = threadIdx.x;
-    const int64_t n = a.n, bidx = blockIdx.x, rbase = bidx * q;
+    const int64_t n = a.n, bidx = bidx_, rbase = bidx * q;
     T g[NG], ms[QMAX], mc[QMAX], pv[QMAX * RM];
 #pragma unroll
     for (int p = 0; p < NG; ++p) g[p] = T(0);
@@ -380,6 +396,15 @@ __global__ void __launch_bounds__(kQstatsThreads) qstats_kernel(QBatchArgs a, co
     __shared__ double red[kQstatsThreads / 32][NPAD];
 #pragma unroll
     for (int i = 0; i < NPL; ++i) red[warp][base + i] = (double)h[i] + (double)l[i];
+    // the baseline's scaled coordinates for the cross terms, computed once across
+    // the CTA (float64 products are scarce: a handful of warp instructions in
+    // place of d per cross-term lane)
+    constexpr int kZb = 4 * 64;
+    __shared__ float s_zb[kZb];
+    const bool stage_zb = sizeof(T) == 4 && a.zt != nullptr && r * a.d <= kZb;
+    if (stage_zb)
+        for (int p = tid; p < r * a.d; p += kQstatsThreads)
+            s_zb[p] = (float)(a.Xb[p] * a.inv_ls[p % a.d]);
     __syncthreads();
     if (tid >= NV) return;
     double tot = 0.0;
@@ -400,8 +425,23 @@ __global__ void __launch_bounds__(kQstatsThreads) qstats_kernel(QBatchArgs a, co
         const int i = (tid - NG - QMAX) / RM, kb = (tid - NG - QMAX) % RM;
         if (i >= q || kb >= r) return;
         // P rounded to T as the two-kernel path stores it
-        a.sqb[(bidx * q + i) * r + kb] = kernel_pair<T>(a, rbase + i, -1, kb) - (double)(T)tot;
+        a.sqb[(bidx * q + i) * r + kb] =
+            kernel_pair<T>(a, rbase + i, -1, kb, stage_zb ? s_zb : nullptr) - (double)(T)tot;
     }
+}
+
+template <typename T, int QMAX, int RM>
+__global__ void __launch_bounds__(kQstatsThreads)
+    qstats_kernel(const __grid_constant__ QBatchArgs a, const T* __restrict__ V, int64_t ldv,
+                  const T* __restrict__ beta, const T* __restrict__ Vb, int vec_ok) {
+    qstats_body<T, QMAX, RM>(a, V, ldv, beta, Vb, vec_ok, blockIdx.x);
+}
+
+template <typename T, int QMAX, int RM>
+__global__ void __launch_bounds__(kQstatsThreads) qstats_group_kernel(const GroupTab t) {
+    const int m = group_model(t);
+    const QstatsG<T>& g = static_cast<const QstatsG<T>*>(t.args)[m];
+    qstats_body<T, QMAX, RM>(g.a, g.V, g.ldv, g.beta, g.Vb, g.vec_ok, blockIdx.x - t.off[m]);
 }
 
 // ---------------------------------------------------------------- smooth pieces
@@ -891,11 +931,12 @@ __device__ int psd_chol_warp(double* M, double* scr, int q, int max_tries, doubl
 }
 
 template <int QMAX>
-__global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a, int backward) {
+__device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int backward,
+                                                    int64_t bidx_) {
     extern __shared__ double smd[];
     constexpr int NW = kBsThreads / 32;
     const int q = a.q, r = a.r, S = a.S, D = r + q;
-    const int64_t bidx = blockIdx.x;
+    const int64_t bidx = bidx_;
     const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
     double* M = smd;                 // q x q
     double* Lq = M + q * q;          // q x D: [bl, br]
@@ -1002,9 +1043,9 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
     }
     __syncthreads();
     const bool qei = (a.acqf == BGB_ACQF_QEI);
-    const float inv_tau = (float)(1.0 / a.tau_relu);
-    const float log_tau = (float)log(a.tau_relu);
-    const float taum = (float)a.tau_max, inv_taum = (float)(1.0 / a.tau_max);
+    const float inv_tau = a.inv_tau_relu_f;
+    const float log_tau = a.log_tau_relu_f;
+    const float taum = (float)a.tau_max, inv_taum = a.inv_tau_max_f;
     const float* __restrict__ z32 = a.z32;
     // best_f per sample as float pairs: per jitter level for cache_root=False
     const float* __restrict__ bf32 = a.joint == 2 ? a.bf32 + 2 * (int64_t)s_lv * S : a.bf32;
@@ -1072,7 +1113,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
             lse = mx;
         } else {
             lse = (double)mx + log(tot);
-            v = lse - log((double)S);
+            v = lse - a.log_S;
         }
         a.value[bidx] = v;
         a.status[bidx] = 0;
@@ -1218,7 +1259,7 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
         double sv = 0.0;
         for (int j = 0; j < q; ++j) sv += 2.0 * fabs(a.gqq[(bidx * q + i) * q + j]);
         for (int k = 0; k < r; ++k) sv += fabs(a.gqb[(bidx * q + i) * r + k]);
-        const double bound = fabs(a.gmu[bidx * q + i]) * a.beta_absmax + sqrt(a.outputscale) * sv;
+        const double bound = fabs(a.gmu[bidx * q + i]) * a.beta_absmax + a.sqrt_outputscale * sv;
         float sc = 1.f;
         if (bound > 0.0 && !isinf(bound)) {
             int e;
@@ -1227,6 +1268,19 @@ __global__ void __launch_bounds__(kBsThreads) batch_step_f32_kernel(QBatchArgs a
         }
         a.hmul[bidx * q + i] = 1.f / sc;
     }
+}
+
+template <int QMAX>
+__global__ void __launch_bounds__(kBsThreads)
+    batch_step_f32_kernel(const __grid_constant__ QBatchArgs a, int backward) {
+    batch_step_f32_body<QMAX>(a, backward, blockIdx.x);
+}
+
+template <int QMAX>
+__global__ void __launch_bounds__(kBsThreads) batch_step_f32_group_kernel(const GroupTab t) {
+    const int m = group_model(t);
+    const BstepG& g = static_cast<const BstepG*>(t.args)[m];
+    batch_step_f32_body<QMAX>(g.a, g.backward, blockIdx.x - t.off[m]);
 }
 
 #if defined(BGB_QB_STEP)
@@ -1257,15 +1311,15 @@ __global__ void prep_samples_kernel(const double* __restrict__ Z, int64_t nz,
 //   |H[i,c]| <= |gmu_i| max|beta| + sqrt(outputscale) (sum_j 2|Gqq[i,j]| + sum_k |Gqb[i,k]|)
 // (every row of V and Vb has 2-norm <= sqrt(outputscale) since V V^T <= K(X,X)).
 template <typename T, int QM, int E>
-__global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T* __restrict__ V,
-                                                       int64_t ldv, const T* __restrict__ Vb,
-                                                       const T* __restrict__ beta,
-                                                       T* __restrict__ H, __half* __restrict__ H16,
-                                                       __half* __restrict__ H16_lo, int64_t ldh) {
+__device__ __forceinline__ void mix_rows_body(const QBatchArgs& a, const T* __restrict__ V,
+                                              int64_t ldv, const T* __restrict__ Vb,
+                                              const T* __restrict__ beta, T* __restrict__ H,
+                                              __half* __restrict__ H16, __half* __restrict__ H16_lo,
+                                              int64_t ldh, int64_t bx, int64_t by, int64_t gx) {
     extern __shared__ __align__(16) unsigned char gsraw[];  // q*q + q*r + q seeds (as T), q scales
     T* gq = reinterpret_cast<T*>(gsraw);
     const int q = a.q, r = a.r;
-    const int64_t n = a.n, bidx = blockIdx.y, rbase = bidx * q;
+    const int64_t n = a.n, bidx = by, rbase = bidx * q;
     T* gqb = gq + q * q;
     T* gm = gqb + q * r;
     float* hs = reinterpret_cast<float*>(gm + q);
@@ -1279,8 +1333,7 @@ __global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T*
     }
     using VT = typename Vec16<T>::type;
     // column groups of blockDim.x * E, strided over grid.x
-    for (int64_t cg = (int64_t)blockIdx.x * blockDim.x * E; cg < n;
-         cg += (int64_t)gridDim.x * blockDim.x * E) {
+    for (int64_t cg = bx * blockDim.x * E; cg < n; cg += gx * blockDim.x * E) {
     const int64_t c0 = cg + (int64_t)threadIdx.x * E;
     if (c0 >= n) continue;
     T v[QM][E], bc[E];
@@ -1372,6 +1425,25 @@ __global__ void __launch_bounds__(256, 3) mix_rows_kernel(QBatchArgs a, const T*
     }
 }
 
+template <typename T, int QM, int E>
+__global__ void __launch_bounds__(256, 3)
+    mix_rows_kernel(const __grid_constant__ QBatchArgs a, const T* __restrict__ V, int64_t ldv,
+                    const T* __restrict__ Vb, const T* __restrict__ beta, T* __restrict__ H,
+                    __half* __restrict__ H16, __half* __restrict__ H16_lo, int64_t ldh) {
+    mix_rows_body<T, QM, E>(a, V, ldv, Vb, beta, H, H16, H16_lo, ldh, blockIdx.x, blockIdx.y,
+                            gridDim.x);
+}
+
+// grouped: model m's CTAs cover its (column group, t-batch) grid row-major in t-batches
+template <typename T, int QM, int E>
+__global__ void __launch_bounds__(256, 3) mix_rows_group_kernel(const GroupTab t) {
+    const int m = group_model(t);
+    const MixG<T>& g = static_cast<const MixG<T>*>(t.args)[m];
+    const int64_t lb = (int64_t)blockIdx.x - t.off[m];
+    mix_rows_body<T, QM, E>(g.a, g.V, g.ldv, g.Vb, g.beta, g.H, g.H16, g.H16_lo, g.ldh,
+                            lb % g.gx, lb / g.gx, g.gx);
+}
+
 // ---------------------------------------------------------------- adjoint
 // d value / d X through K(X, Xt): one thread per row of X, kAdjRows rows per CTA.
 // The training points are split into grid.y slabs, since the rows alone give
@@ -1449,9 +1521,9 @@ __device__ __forceinline__ float dkappa_dr2_fast(int kind, float r2) {
 }
 
 template <typename T, int DMAX, bool FINISH>
-__global__ void __launch_bounds__(kAdjRows, (sizeof(T) == 4 && DMAX <= 24) ? 5 : 1) adjoint_kernel(QBatchArgs a, const T* __restrict__ Dm,
-                                                           int64_t ldd, const T* __restrict__ XsT,
-                                                           int64_t slab, T* __restrict__ part) {
+__device__ __forceinline__ void adjoint_body(const QBatchArgs& a, const T* __restrict__ Dm,
+                                             int64_t ldd, const T* __restrict__ XsT, int64_t slab,
+                                             T* __restrict__ part, int64_t bx, int64_t by) {
     using VT = typename Vec16<T>::type;
     constexpr int E = Vec16<T>::E;
     static_assert(DMAX % E == 0, "DMAX must hold whole 16-byte vectors");
@@ -1462,10 +1534,10 @@ __global__ void __launch_bounds__(kAdjRows, (sizeof(T) == 4 && DMAX <= 24) ? 5 :
     const int d = a.d, kind = a.kernel;
     const int64_t n = a.n, rows = a.b * a.q;
     const int tid = threadIdx.x;
-    const int64_t row0 = (int64_t)blockIdx.x * kAdjRows;
+    const int64_t row0 = bx * kAdjRows;
     const int64_t row = row0 + tid;
     const bool active = row < rows;
-    const int64_t cbeg = (int64_t)blockIdx.y * slab;
+    const int64_t cbeg = by * slab;
     const int64_t cend = (cbeg + slab < n) ? cbeg + slab : n;
     T zx[DMAX], g[DMAX];
     float2 zx2[DMAX / 2], g2[DMAX / 2];  // packed copies for the float32 sweep
@@ -1570,7 +1642,7 @@ __global__ void __launch_bounds__(kAdjRows, (sizeof(T) == 4 && DMAX <= 24) ? 5 :
         return;
     }
     if constexpr (!FINISH) {
-    T* pp = part + (int64_t)blockIdx.y * d * rows;
+    T* pp = part + by * d * rows;
 #pragma unroll
     for (int k = 0; k < DMAX; ++k)
         if (k < d) pp[(int64_t)k * rows + row] = g[k];
@@ -1579,6 +1651,24 @@ __global__ void __launch_bounds__(kAdjRows, (sizeof(T) == 4 && DMAX <= 24) ? 5 :
 
 // Sum of the slab partials, one thread per (k, row) element (coalesced over
 // rows), compensated; the total overwrites slab 0.
+
+template <typename T, int DMAX, bool FINISH>
+__global__ void __launch_bounds__(kAdjRows, (sizeof(T) == 4 && DMAX <= 24) ? 5 : 1)
+    adjoint_kernel(const __grid_constant__ QBatchArgs a, const T* __restrict__ Dm, int64_t ldd,
+                   const T* __restrict__ XsT, int64_t slab, T* __restrict__ part) {
+    adjoint_body<T, DMAX, FINISH>(a, Dm, ldd, XsT, slab, part, blockIdx.x, blockIdx.y);
+}
+
+// grouped: model m's CTAs cover its (row block, slab) grid row-major in slabs
+template <typename T, int DMAX, bool FINISH>
+__global__ void __launch_bounds__(kAdjRows, (sizeof(T) == 4 && DMAX <= 24) ? 5 : 1)
+    adjoint_group_kernel(const GroupTab t) {
+    const int m = group_model(t);
+    const AdjG<T>& g = static_cast<const AdjG<T>*>(t.args)[m];
+    const int64_t lb = (int64_t)blockIdx.x - t.off[m];
+    adjoint_body<T, DMAX, FINISH>(g.a, g.D, g.ldd, g.XsT, g.slab, g.part, lb % g.gx, lb / g.gx);
+}
+
 template <typename T>
 __global__ void adjoint_slab_sum_kernel(T* __restrict__ part, int64_t elems, int nslab) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1589,15 +1679,42 @@ __global__ void adjoint_slab_sum_kernel(T* __restrict__ part, int64_t elems, int
 }
 
 template <typename T, int DMAX>
-__global__ void __launch_bounds__(128) adjoint_finalize_kernel(QBatchArgs a, const T* __restrict__ part) {
+__device__ __forceinline__ void adjoint_finalize_body(const QBatchArgs& a, const T* __restrict__ part,
+                                                      int64_t bx) {
     const int64_t rows = a.b * a.q;
-    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t row = bx * blockDim.x + threadIdx.x;
     if (row >= rows) return;
     const int d = a.d;
     T gx[DMAX];
 #pragma unroll
     for (int k = 0; k < DMAX; ++k) gx[k] = (k < d) ? part[(int64_t)k * rows + row] : T(0);
     adjoint_finish_row<T, DMAX>(a, row, gx);
+}
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(128)
+    adjoint_finalize_kernel(const __grid_constant__ QBatchArgs a, const T* __restrict__ part) {
+    adjoint_finalize_body<T, DMAX>(a, part, blockIdx.x);
+}
+
+// grouped slab sum and finish (models with a single slab have no CTAs here)
+template <typename T>
+__global__ void adjoint_slab_sum_group_kernel(const GroupTab t) {
+    const int m = group_model(t);
+    const AdjG<T>& g = static_cast<const AdjG<T>*>(t.args)[m];
+    const int64_t elems = (int64_t)g.a.d * g.a.b * g.a.q;
+    const int64_t e = ((int64_t)blockIdx.x - t.off[m]) * blockDim.x + threadIdx.x;
+    if (e >= elems) return;
+    T acc = T(0), c = T(0);
+    for (int s = 0; s < g.nslab; ++s) comp_add<T>(acc, c, g.part[(int64_t)s * elems + e]);
+    g.part[e] = acc - c;
+}
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(128) adjoint_finalize_group_kernel(const GroupTab t) {
+    const int m = group_model(t);
+    const AdjG<T>& g = static_cast<const AdjG<T>*>(t.args)[m];
+    adjoint_finalize_body<T, DMAX>(g.a, g.part, (int64_t)blockIdx.x - t.off[m]);
 }
 
 #if defined(BGB_QB_STATS)
@@ -1670,12 +1787,8 @@ int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bo
     if (a.z32 == nullptr || a.bf32 == nullptr) return BGB_ERR_ARG;
     const size_t smem = batch_step_f32_smem_bytes(a.q, a.r, a.S);
     if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
-    const int64_t nz = (int64_t)a.S * (a.r + a.q);
-    const int64_t nbf = a.joint == 2 ? (int64_t)a.S * (a.max_tries + 1) : a.S;
-    const int64_t np = nz > nbf ? nz : nbf;
-    prep_samples_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, stream>>>(
-        a.Z, nz, a.joint == 2 ? a.best_f_lv : a.best_f, nbf, a.acqf == BGB_ACQF_QEI, a.z32, a.bf32);
-    BGB_CHECK_LAUNCH();
+    int rc = launch_prep_samples(a, stream);
+    if (rc) return rc;
 #define BGB_BS(QM)                                                                               \
     do {                                                                                        \
         if (smem > 48 * 1024)                                                                   \
@@ -1689,6 +1802,41 @@ int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bo
     else if (a.q <= 16) BGB_BS(16);
     else BGB_BS(32);
 #undef BGB_BS
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+// Z as float32 and best_f as float pairs (a.z32, a.bf32), the mixed batch step's inputs.
+int launch_prep_samples(const QBatchArgs& a, cudaStream_t stream) {
+    if (a.z32 == nullptr || a.bf32 == nullptr) return BGB_ERR_ARG;
+    const int64_t nz = (int64_t)a.S * (a.r + a.q);
+    const int64_t nbf = a.joint == 2 ? (int64_t)a.S * (a.max_tries + 1) : a.S;
+    const int64_t np = nz > nbf ? nz : nbf;
+    prep_samples_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, stream>>>(
+        a.Z, nz, a.joint == 2 ? a.best_f_lv : a.best_f, nbf, a.acqf == BGB_ACQF_QEI, a.z32, a.bf32);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+size_t batch_step_f32_smem(int q, int r, int S) { return batch_step_f32_smem_bytes(q, r, S); }
+
+int launch_batch_step_group(const GroupTab& t, int qmax, size_t smem, int64_t total,
+                            cudaStream_t stream) {
+    if (total <= 0) return BGB_OK;
+    if (qmax > kMaxQ || smem > 200 * 1024 || total > 0x7fffffff) return BGB_ERR_UNSUPPORTED;
+#define BGB_BSG(QM)                                                                              \
+    do {                                                                                        \
+        if (smem > 48 * 1024)                                                                   \
+            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_f32_group_kernel<QM>,                  \
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                              (int)smem));                                      \
+        batch_step_f32_group_kernel<QM><<<(unsigned)total, kBsThreads, smem, stream>>>(t);      \
+    } while (0)
+    if (qmax <= 4) BGB_BSG(4);
+    else if (qmax <= 8) BGB_BSG(8);
+    else if (qmax <= 16) BGB_BSG(16);
+    else BGB_BSG(32);
+#undef BGB_BSG
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
@@ -1713,6 +1861,22 @@ int launch_qstats(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, c
         qstats_kernel<T, 8, 2><<<grid, kQstatsThreads, 0, stream>>>(a, V, ldv, beta, Vb, vec_ok);
     else
         qstats_kernel<T, 8, 4><<<grid, kQstatsThreads, 0, stream>>>(a, V, ldv, beta, Vb, vec_ok);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+int launch_qstats_group(const GroupTab& t, int qmax, int rmax, int64_t total, cudaStream_t stream) {
+    if (total <= 0) return BGB_OK;
+    if (qmax > 8 || rmax > 4 || total > 0x7fffffff) return BGB_ERR_UNSUPPORTED;
+    const unsigned grid = (unsigned)total;
+    if (qmax <= 4 && rmax <= 2)
+        qstats_group_kernel<float, 4, 2><<<grid, kQstatsThreads, 0, stream>>>(t);
+    else if (qmax <= 4)
+        qstats_group_kernel<float, 4, 4><<<grid, kQstatsThreads, 0, stream>>>(t);
+    else if (rmax <= 2)
+        qstats_group_kernel<float, 8, 2><<<grid, kQstatsThreads, 0, stream>>>(t);
+    else
+        qstats_group_kernel<float, 8, 4><<<grid, kQstatsThreads, 0, stream>>>(t);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
@@ -1744,13 +1908,7 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
     const bool vec = (a.n % E == 0) && (ldv % E == 0) && (ld % E == 0) && al(V, 16) &&
                      al(beta, 16) && (a.r == 0 || al(Vb, 16)) &&
                      (H16 != nullptr ? (al(H16, 8) && al(H16_lo, 8)) : al(H, 16));
-    // column groups per t-batch: enough CTAs for ~6 per SM, each CTA loads its
-    // t-batch's seeds once and strides over the rest
-    auto groups = [&](int64_t per) {
-        const int64_t all = ceil_div(a.n, per);
-        const int64_t want = ceil_div((int64_t)sm_count() * 6, a.b);
-        return (unsigned)(want < 1 ? 1 : (want > all ? all : want));
-    };
+    auto groups = [&](int64_t per) { return (unsigned)mix_rows_groups(a, (int)(per / 256)); };
 #define BGB_MIX(QM)                                                                              \
     do {                                                                                        \
         if (vec) {                                                                              \
@@ -1771,6 +1929,31 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
+// column groups per t-batch for vector width E: enough CTAs for ~6 per SM, each
+// CTA loads its t-batch's seeds once and strides over the rest
+int64_t mix_rows_groups(const QBatchArgs& a, int E) {
+    const int64_t all = ceil_div(a.n, (int64_t)256 * E);
+    const int64_t want = ceil_div((int64_t)sm_count() * 6, a.b > 0 ? a.b : 1);
+    return want < 1 ? 1 : (want > all ? all : want);
+}
+
+size_t mix_rows_smem_bytes(const QBatchArgs& a) {
+    return sizeof(float) * (size_t)(a.q * a.q + a.q * a.r + a.q) + sizeof(float) * a.q;
+}
+
+// float32, scalar columns (E = 1: the models' n and strides need not be multiples of 4)
+int launch_mix_rows_group(const GroupTab& t, int qmax, size_t smem, int64_t total,
+                          cudaStream_t stream) {
+    if (total <= 0) return BGB_OK;
+    if (qmax > kMaxQ || smem > 48 * 1024 || total > 0x7fffffff) return BGB_ERR_UNSUPPORTED;
+    const unsigned grid = (unsigned)total;
+    if (qmax <= 4) mix_rows_group_kernel<float, 4, 1><<<grid, 256, smem, stream>>>(t);
+    else if (qmax <= 8) mix_rows_group_kernel<float, 8, 1><<<grid, 256, smem, stream>>>(t);
+    else if (qmax <= 16) mix_rows_group_kernel<float, 16, 1><<<grid, 256, smem, stream>>>(t);
+    else mix_rows_group_kernel<float, 32, 1><<<grid, 256, smem, stream>>>(t);
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
 #endif  // BGB_QB_MIX
 
 #if defined(BGB_QB_ADJ_F64) || defined(BGB_QB_ADJ_F32)
@@ -1787,20 +1970,8 @@ int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T
                    int64_t part_cap, cudaStream_t stream) {
     const int64_t rows = a.b * a.q;
     if (rows <= 0) return BGB_OK;
-    const int64_t row_blocks = ceil_div(rows, kAdjRows);
-    // slabs: a.adj_ctas_per_sm CTAs per SM (default 16: about four waves of four
-    // resident CTAs), slabs of whole chunks, partials within part_cap
-    const int num_sms = sm_count();
-    const int64_t chunks = ceil_div(a.n, kAdjChunk);
-    const int64_t per_sm = a.adj_ctas_per_sm > 0 ? a.adj_ctas_per_sm : 16;
-    int64_t nslab = ceil_div((int64_t)num_sms * per_sm, row_blocks);
-    if (nslab > chunks) nslab = chunks;
-    if (nslab > 65535) nslab = 65535;
-    if (part == nullptr || part_cap <= 0) nslab = 1;
-    while (nslab > 1 && nslab * a.d * rows > part_cap) --nslab;
-    if (nslab < 1) nslab = 1;
-    const int64_t slab = ceil_div(chunks, nslab) * kAdjChunk;
-    nslab = ceil_div(a.n, slab);
+    int64_t row_blocks, nslab, slab;
+    adjoint_split(a, part != nullptr ? part_cap : 0, &row_blocks, &nslab, &slab);
     T* pp = nslab > 1 ? part : nullptr;
     dim3 grid((unsigned)row_blocks, (unsigned)nslab);
 #define BGB_ADJ(DM)                                                                              \
@@ -1842,6 +2013,85 @@ int launch_adjoint(const QBatchArgs& a, const T* D, int64_t ldd, const T* XsT, T
 }
 
 #endif  // BGB_QB_ADJ_*
+
+#if defined(BGB_QB_ADJ_F32)
+// slabs: a.adj_ctas_per_sm CTAs per SM (default 16: about four waves of four
+// resident CTAs), slabs of whole chunks, partials within part_cap elements
+void adjoint_split(const QBatchArgs& a, int64_t part_cap, int64_t* row_blocks_out,
+                   int64_t* nslab_out, int64_t* slab_out) {
+    const int64_t rows = a.b * a.q;
+    const int64_t row_blocks = ceil_div(rows > 0 ? rows : 1, kAdjRows);
+    const int num_sms = sm_count();
+    const int64_t chunks = ceil_div(a.n, kAdjChunk);
+    const int64_t per_sm = a.adj_ctas_per_sm > 0 ? a.adj_ctas_per_sm : 16;
+    int64_t nslab = ceil_div((int64_t)num_sms * per_sm, row_blocks);
+    if (nslab > chunks) nslab = chunks;
+    if (nslab > 65535) nslab = 65535;
+    if (part_cap <= 0) nslab = 1;
+    while (nslab > 1 && nslab * a.d * rows > part_cap) --nslab;
+    if (nslab < 1) nslab = 1;
+    const int64_t slab = ceil_div(chunks, nslab) * kAdjChunk;
+    *row_blocks_out = row_blocks;
+    *nslab_out = ceil_div(a.n, slab);
+    *slab_out = slab;
+}
+
+int launch_adjoint_group(const GroupTab& t, int dmax, bool partials, int64_t total,
+                         cudaStream_t stream) {
+    if (total <= 0) return BGB_OK;
+    if (total > 0x7fffffff) return BGB_ERR_UNSUPPORTED;
+    const unsigned grid = (unsigned)total;
+#define BGB_ADJG(DM)                                                                             \
+    do {                                                                                        \
+        const size_t smem = adjoint_smem_bytes<float, DM>();                                    \
+        if (partials) {                                                                         \
+            if (smem > 48 * 1024)                                                               \
+                BGB_CUDA_TRY(cudaFuncSetAttribute(adjoint_group_kernel<float, DM, false>,       \
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                                  (int)smem));                                  \
+            adjoint_group_kernel<float, DM, false><<<grid, kAdjRows, smem, stream>>>(t);        \
+        } else {                                                                                \
+            if (smem > 48 * 1024)                                                               \
+                BGB_CUDA_TRY(cudaFuncSetAttribute(adjoint_group_kernel<float, DM, true>,        \
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                                  (int)smem));                                  \
+            adjoint_group_kernel<float, DM, true><<<grid, kAdjRows, smem, stream>>>(t);         \
+        }                                                                                       \
+    } while (0)
+    if (dmax <= 8) BGB_ADJG(8);
+    else if (dmax <= 12) BGB_ADJG(12);
+    else if (dmax <= 16) BGB_ADJG(16);
+    else if (dmax <= 20) BGB_ADJG(20);
+    else if (dmax <= 24) BGB_ADJG(24);
+    else if (dmax <= 32) BGB_ADJG(32);
+    else if (dmax <= 64) BGB_ADJG(64);
+    else return BGB_ERR_UNSUPPORTED;
+#undef BGB_ADJG
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+
+int launch_adjoint_finish_group(const GroupTab& t_sum, int64_t total_sum, const GroupTab& t_fin,
+                                int dmax, int64_t total_fin, cudaStream_t stream) {
+    if (total_sum > 0x7fffffff || total_fin > 0x7fffffff) return BGB_ERR_UNSUPPORTED;
+    if (total_sum > 0) {
+        adjoint_slab_sum_group_kernel<float><<<(unsigned)total_sum, 256, 0, stream>>>(t_sum);
+        BGB_CHECK_LAUNCH();
+    }
+    if (total_fin <= 0) return BGB_OK;
+    const unsigned grid = (unsigned)total_fin;
+    if (dmax <= 8) adjoint_finalize_group_kernel<float, 8><<<grid, 128, 0, stream>>>(t_fin);
+    else if (dmax <= 12) adjoint_finalize_group_kernel<float, 12><<<grid, 128, 0, stream>>>(t_fin);
+    else if (dmax <= 16) adjoint_finalize_group_kernel<float, 16><<<grid, 128, 0, stream>>>(t_fin);
+    else if (dmax <= 20) adjoint_finalize_group_kernel<float, 20><<<grid, 128, 0, stream>>>(t_fin);
+    else if (dmax <= 24) adjoint_finalize_group_kernel<float, 24><<<grid, 128, 0, stream>>>(t_fin);
+    else if (dmax <= 32) adjoint_finalize_group_kernel<float, 32><<<grid, 128, 0, stream>>>(t_fin);
+    else if (dmax <= 64) adjoint_finalize_group_kernel<float, 64><<<grid, 128, 0, stream>>>(t_fin);
+    else return BGB_ERR_UNSUPPORTED;
+    BGB_CHECK_LAUNCH();
+    return BGB_OK;
+}
+#endif  // BGB_QB_ADJ_F32
 
 #if defined(BGB_QB_STATS)
 int launch_posterior_out(const QBatchArgs& a, double* mean, double* covar, cudaStream_t stream) {

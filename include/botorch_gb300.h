@@ -372,6 +372,36 @@ int bgb_acq_forward_backward_timed(const bgb_acq_t* acq, const double* X, int64_
 int bgb_acq_forward_backward_noalloc(const bgb_acq_t* acq, const double* X, int64_t b,
                                      double* value, double* grad, int32_t* status, void* stream);
 
+/* ---- Grouped evaluation of many independent problems. The reference
+ * evaluates each model's acquisition function in its own optimize_acqf call
+ * (botorch/generation/gen.py:423-487 per model; MCAcquisitionFunction.forward,
+ * botorch/acquisition/logei.py:247-289); a group runs the value and gradient of
+ * `count` problems (one model each, uneven n and d) in about ten launches:
+ * each stage (kernel build, forward tensor-core GEMM, covariance reduction,
+ * batch step, row mix, adjoint GEMM, adjoint) is one launch over all problems,
+ * its CTAs mapped to (problem, block) through per-stage prefix tables, and the
+ * two GEMMs walk one tile list over all problems, dealt out largest first to
+ * the least-loaded two-SM cluster. The results equal `count` calls of
+ * bgb_acq_forward_backward on the same structs.
+ * Every member must be the mixed tensor-core form with a cached root (no
+ * BGB_FLAG_JOINT_SAMPLING), q <= 8, r <= 4; otherwise the size query returns 0
+ * and create returns BGB_ERR_UNSUPPORTED.
+ * The plan keeps the pointers it is given: X[i] (b[i] x q x d), value[i],
+ * grad[i], status[i] are read and written by every bgb_group_run, and the
+ * structs' operands must stay alive and unchanged. create synchronises
+ * `stream` and launches work on it; run only launches (capturable in a CUDA
+ * graph); the workspace belongs to the plan until destroy. */
+typedef struct bgb_group bgb_group_t;
+size_t bgb_group_workspace_bytes(const bgb_acq_t* acqs, const int64_t* b, int32_t count);
+int bgb_group_create(const bgb_acq_t* acqs, const int64_t* b, int32_t count,
+                     const double* const* X, double* const* value, double* const* grad,
+                     int32_t* const* status, void* workspace, size_t workspace_bytes, void* stream,
+                     bgb_group_t** out);
+int bgb_group_run(const bgb_group_t* group, void* stream);
+/* kernels one run launches (8, or 10 when an adjoint is split into slabs) */
+int32_t bgb_group_launches(const bgb_group_t* group);
+void bgb_group_destroy(bgb_group_t* group);
+
 /* ---- Fused log-areas of qLogEHVI / qLogNEHVI (the inner loop of
  * _compute_log_qehvi, botorch/acquisition/multi_objective/logei.py:272-392).
  * Replace the reference's CPU extension botorch/csrc/logei_fused.cpp:
