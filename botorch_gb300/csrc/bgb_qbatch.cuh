@@ -129,7 +129,7 @@ int launch_kernel_matrix_group(const GroupTab& t_scale, int64_t total_scale, con
                                int64_t total_km, cudaStream_t stream);
 
 // Sizes the standalone launchers use, shared with the grouped ones.
-int64_t mix_rows_groups(const QBatchArgs& a, int E);
+int64_t mix_rows_groups(const QBatchArgs& a, int E, int64_t total_b);
 size_t mix_rows_smem_bytes(const QBatchArgs& a);
 // adjoint split: row blocks, slabs and slab length for part_cap partial elements
 void adjoint_split(const QBatchArgs& a, int64_t part_cap, int64_t* row_blocks, int64_t* nslab,

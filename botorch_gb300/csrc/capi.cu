@@ -460,7 +460,7 @@ GroupSizes group_sizes(const bgb_acq_t* acqs, const int64_t* b, int count) {
                align_up(cnt * sizeof(QstatsG<float>)) + align_up(cnt * sizeof(BstepG)) +
                align_up(cnt * sizeof(MixG<float>)) + align_up(cnt * sizeof(AdjG<float>)) +
                GS_N * align_up((cnt + 1) * sizeof(int)) +
-               2 * kDBuckets * align_up((cnt + 1) * sizeof(int)) +
+               kDBuckets * align_up((cnt + 1) * sizeof(int)) +
                2 * (align_up(cnt * tc_group_entry_bytes()) + align_up(sizeof(int) * 256)) +
                align_up(sizeof(uint64_t) * (size_t)z.tiles_fwd) +
                align_up(sizeof(uint64_t) * (size_t)z.tiles_adj);
@@ -477,9 +477,9 @@ struct bgb_group {
     int* err = nullptr;
     GroupTab tab[GS_N];
     int64_t ctas[GS_N] = {};
-    // adjoint and its finish, per d bucket (models in bucket order in the AdjG table)
-    GroupTab adj_tab[kDBuckets], fin_tab[kDBuckets];
-    int64_t adj_ctas[kDBuckets] = {}, fin_ctas[kDBuckets] = {};
+    // the adjoint per d bucket (models in bucket order in the AdjG table)
+    GroupTab adj_tab[kDBuckets];
+    int64_t adj_ctas[kDBuckets] = {};
     int qmax = 0, rmax = 0, dmax = 0;
     size_t bs_smem = 0, mix_smem = 0;
     bool partials = false;
@@ -538,11 +538,12 @@ int group_create(const bgb_acq_t* acqs, const int64_t* b, int count, const doubl
         d_tc_off[k] = tar.take<int>(256);
     }
     uint64_t* d_tc_tiles[2] = {tar.take<uint64_t>(z.tiles_fwd), tar.take<uint64_t>(z.tiles_adj)};
-    int* d_boff[2][kDBuckets];
-    for (int j = 0; j < 2; ++j)
-        for (int k = 0; k < kDBuckets; ++k) d_boff[j][k] = tar.take<int>(count + 1);
-    if (d_boff[1][kDBuckets - 1] == nullptr) return BGB_ERR_WORKSPACE;
+    int* d_boff[kDBuckets];
+    for (int k = 0; k < kDBuckets; ++k) d_boff[k] = tar.take<int>(count + 1);
+    if (d_boff[kDBuckets - 1] == nullptr) return BGB_ERR_WORKSPACE;
     // per model: arena, arguments, CTA counts
+    int64_t total_b = 0;
+    for (int i = 0; i < count; ++i) total_b += b[i];
     size_t aoff = 0;
     int64_t c[GS_N] = {};
     for (int i = 0; i < count; ++i) {
@@ -581,7 +582,7 @@ int group_create(const bgb_acq_t* acqs, const int64_t* b, int count, const doubl
         hb.qs.push_back(QstatsG<float>{qa, static_cast<const float*>(C), a->ldb, a->beta32,
                                        a->Vb32, vec_ok});
         hb.bs.push_back(BstepG{qa, 1});
-        const int64_t mgx = mix_rows_groups(qa, 1);
+        const int64_t mgx = mix_rows_groups(qa, 1, total_b);
         hb.mix.push_back(MixG<float>{qa, static_cast<const float*>(C), a->ldb, a->Vb32, a->beta32,
                                      nullptr, Khi, Klo, a->ldl, mgx});
         hb.gemm[1].push_back(TcGroupGemm{rows, n, n, Khi, Klo, a->ldl,
@@ -622,24 +623,27 @@ int group_create(const bgb_acq_t* acqs, const int64_t* b, int count, const doubl
     });
     std::vector<AdjG<float>> adj_sorted;
     std::vector<int> sum_off(1, 0);
-    std::vector<int> boff[2][kDBuckets];
+    std::vector<int> boff[kDBuckets];
     int bstart[kDBuckets + 1] = {};
     for (int k = 0, pos = 0; k < kDBuckets; ++k) {
         bstart[k] = pos;
-        boff[0][k].assign(1, 0);
-        boff[1][k].assign(1, 0);
+        boff[k].assign(1, 0);
         for (; pos < count && d_bucket(acqs[order[pos]].gp.d) == k; ++pos) {
             const AdjG<float>& e = hb.adj[order[pos]];
             const int64_t rows = e.a.b * e.a.q;
             adj_sorted.push_back(e);
-            boff[0][k].push_back(boff[0][k].back() + (int)(e.gx * e.nslab));
-            boff[1][k].push_back(boff[1][k].back() + (int)ceil_div(rows, (int64_t)128));
+            boff[k].push_back(boff[k].back() + (int)(e.gx * e.nslab));
             sum_off.push_back(sum_off.back() + (int)ceil_div((int64_t)e.a.d * rows, (int64_t)256));
         }
         bstart[k + 1] = pos;
     }
     hb.adj.swap(adj_sorted);
     hb.off[GS_SUM] = sum_off;
+    // one finish launch over every model (latency-bound: per-bucket launches cost
+    // more than the larger register arrays), in the bucket order of the table
+    hb.off[GS_FIN].assign(1, 0);
+    for (const auto& e : hb.adj)
+        hb.off[GS_FIN].push_back(hb.off[GS_FIN].back() + (int)ceil_div(e.a.b * e.a.q, (int64_t)128));
     // tensor-core tile schedules
     std::vector<unsigned char> ent[2];
     std::vector<int> toff[2];
@@ -668,9 +672,8 @@ int group_create(const bgb_acq_t* acqs, const int64_t* b, int count, const doubl
         if (!rc) rc = up(d_tc_off[k], toff[k].data(), sizeof(int) * toff[k].size());
         if (!rc) rc = up(d_tc_tiles[k], tiles[k].data(), sizeof(uint64_t) * tiles[k].size());
     }
-    for (int j = 0; !rc && j < 2; ++j)
-        for (int k = 0; !rc && k < kDBuckets; ++k)
-            rc = up(d_boff[j][k], boff[j][k].data(), sizeof(int) * boff[j][k].size());
+    for (int k = 0; !rc && k < kDBuckets; ++k)
+        rc = up(d_boff[k], boff[k].data(), sizeof(int) * boff[k].size());
     if (rc) return rc;
     BGB_CUDA_TRY(cudaStreamSynchronize(st));
     const void* args[GS_N] = {d_km, d_km, d_qs, d_bs, d_mix, d_adj, d_adj, d_adj};
@@ -686,14 +689,13 @@ int group_create(const bgb_acq_t* acqs, const int64_t* b, int count, const doubl
     int nb = 0;
     for (int k = 0; k < kDBuckets; ++k) {
         const int nm = bstart[k + 1] - bstart[k];
-        g->adj_tab[k] = GroupTab{nm, d_boff[0][k], d_adj + bstart[k]};
-        g->fin_tab[k] = GroupTab{nm, d_boff[1][k], d_adj + bstart[k]};
-        g->adj_ctas[k] = nm > 0 ? boff[0][k].back() : 0;
-        g->fin_ctas[k] = nm > 0 && g->partials ? boff[1][k].back() : 0;
+        g->adj_tab[k] = GroupTab{nm, d_boff[k], d_adj + bstart[k]};
+        g->adj_ctas[k] = nm > 0 ? boff[k].back() : 0;
         nb += nm > 0 ? 1 : 0;
     }
     g->ctas[GS_SUM] = g->partials ? sum_off.back() : 0;
-    g->launches = 7 + nb + (g->partials ? 1 + nb : 0);
+    g->ctas[GS_FIN] = g->partials ? hb.off[GS_FIN].back() : 0;
+    g->launches = 7 + nb + (g->partials ? 2 : 0);
     *out = g.release();
     return BGB_OK;
 }
@@ -711,12 +713,9 @@ int group_run(const bgb_group* g, cudaStream_t st) {
                                   g->err, st);
     for (int k = 0; !rc && k < kDBuckets; ++k)
         rc = launch_adjoint_group(g->adj_tab[k], kDBound[k], g->partials, g->adj_ctas[k], st);
-    for (int k = 0, first = 1; !rc && g->partials && k < kDBuckets; ++k) {
-        if (g->fin_ctas[k] == 0) continue;
-        rc = launch_adjoint_finish_group(g->tab[GS_SUM], first ? g->ctas[GS_SUM] : 0, g->fin_tab[k],
-                                         kDBound[k], g->fin_ctas[k], st);
-        first = 0;
-    }
+    if (!rc && g->partials)
+        rc = launch_adjoint_finish_group(g->tab[GS_SUM], g->ctas[GS_SUM], g->tab[GS_FIN],
+                                         kDBound[d_bucket(g->dmax)], g->ctas[GS_FIN], st);
     return rc;
 }
 

@@ -1908,7 +1908,7 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
     const bool vec = (a.n % E == 0) && (ldv % E == 0) && (ld % E == 0) && al(V, 16) &&
                      al(beta, 16) && (a.r == 0 || al(Vb, 16)) &&
                      (H16 != nullptr ? (al(H16, 8) && al(H16_lo, 8)) : al(H, 16));
-    auto groups = [&](int64_t per) { return (unsigned)mix_rows_groups(a, (int)(per / 256)); };
+    auto groups = [&](int64_t per) { return (unsigned)mix_rows_groups(a, (int)(per / 256), 0); };
 #define BGB_MIX(QM)                                                                              \
     do {                                                                                        \
         if (vec) {                                                                              \
@@ -1931,9 +1931,11 @@ int launch_mix_rows(const QBatchArgs& a, const T* V, int64_t ldv, const T* Vb, c
 }
 // column groups per t-batch for vector width E: enough CTAs for ~6 per SM, each
 // CTA loads its t-batch's seeds once and strides over the rest
-int64_t mix_rows_groups(const QBatchArgs& a, int E) {
+// (total_b: the t-batches of every launch sharing the GPU, 0 for a.b alone)
+int64_t mix_rows_groups(const QBatchArgs& a, int E, int64_t total_b) {
     const int64_t all = ceil_div(a.n, (int64_t)256 * E);
-    const int64_t want = ceil_div((int64_t)sm_count() * 6, a.b > 0 ? a.b : 1);
+    const int64_t tb = total_b > 0 ? total_b : (a.b > 0 ? a.b : 1);
+    const int64_t want = ceil_div((int64_t)sm_count() * 6, tb);
     return want < 1 ? 1 : (want > all ? all : want);
 }
 
