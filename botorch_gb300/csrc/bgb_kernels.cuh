@@ -98,6 +98,8 @@ struct TcGroupGemm {
     const float* col_mul;
 };
 size_t tc_group_entry_bytes();
+// tiles of one GEMM (M x N) in a grouped launch
+int64_t tc_group_tiles(int64_t M, int64_t N);
 // Device tables of a grouped launch: `entries` (tc_group_entry_bytes() per GEMM,
 // to be copied to dev_entries, 64-byte aligned), per-cluster tile ranges `off`
 // (clusters + 1) and the tile list `tiles`.

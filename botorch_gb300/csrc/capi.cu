@@ -451,7 +451,7 @@ GroupSizes group_sizes(const bgb_acq_t* acqs, const int64_t* b, int count) {
     for (int i = 0; i < count; ++i) {
         z.arenas += align_up(acq_ws_layout(&acqs[i], b[i], nullptr, nullptr, nullptr, nullptr, nullptr));
         const int64_t rows = b[i] * acqs[i].q, n = acqs[i].gp.n;
-        const int64_t t = ceil_div(rows, (int64_t)256) * ceil_div(n, (int64_t)256);
+        const int64_t t = tc_group_tiles(rows, n);
         z.tiles_fwd += t;
         z.tiles_adj += t;
     }

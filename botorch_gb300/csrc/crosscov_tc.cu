@@ -965,6 +965,10 @@ int group_resident_clusters() {
 
 size_t tc_group_entry_bytes() { return sizeof(TcGroupEntry); }
 
+int64_t tc_group_tiles(int64_t M, int64_t N) {
+    return ceil_div(M, (int64_t)TC_BM * 2) * ceil_div(N, (int64_t)TC_BN);
+}
+
 // Device tables of a grouped launch (two-SM form) into host buffers: one entry
 // per GEMM (its maps and record; the record's maps pointer is the entry's
 // address in dev_entries), and every (GEMM, row block, column block) tile dealt
