@@ -155,6 +155,12 @@ int launch_adjoint_finish_group(const GroupTab& t_sum, int64_t total_sum, const 
 template <typename T>
 int launch_qstats(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb,
                   cudaStream_t stream);
+// the same outputs for q <= 32 from shared-memory tiles of V (BGB_ERR_UNSUPPORTED,
+// nothing launched, beyond its output count or shared memory); scratch holds the
+// float64 partial sums when few t-batches split their columns over CTAs
+template <typename T>
+int launch_qstats_tile(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb,
+                       void* scratch, size_t scratch_bytes, cudaStream_t stream);
 // mu (into a.mu) = m + V beta and P (b*q x r) = V Vb^T
 template <typename T>
 int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb, T* P,

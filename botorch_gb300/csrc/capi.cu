@@ -299,7 +299,11 @@ int run_front(const bgb_acq_t* a, const double* X, int64_t b, QBatchArgs* qa, T*
 after_gemm:
     if (ev) BGB_CUDA_TRY(cudaEventRecord(ev[2], st));
     rc = launch_qstats<T>(*qa, C, a->ldb, Ops<T>::beta(a), Ops<T>::Vb(a), st);
-    if (rc == BGB_ERR_UNSUPPORTED) {  // q > 8 or r > 4: separate row and pair passes
+    if (rc == BGB_ERR_UNSUPPORTED)  // q > 8 or r > 4: shared-memory tiles; the Kc region is
+        // free here (the forward GEMM has read it) and holds split partial sums
+        rc = launch_qstats_tile<T>(*qa, C, a->ldb, Ops<T>::beta(a), Ops<T>::Vb(a), Kc,
+                                   sizeof(T) * (size_t)kc_region_elems(a, b * a->q), st);
+    if (rc == BGB_ERR_UNSUPPORTED) {  // beyond those: separate row and pair passes
         rc = launch_row_dots<T>(*qa, C, a->ldb, Ops<T>::beta(a), Ops<T>::Vb(a), P, st);
         if (rc) return rc;
         rc = launch_sigma_reduce<T>(*qa, P, C, a->ldb, st);

@@ -444,6 +444,161 @@ __global__ void __launch_bounds__(kQstatsThreads) qstats_group_kernel(const Grou
     qstats_body<T, QMAX, RM>(g.a, g.V, g.ldv, g.beta, g.Vb, g.vec_ok, blockIdx.x - t.off[m]);
 }
 
+// ---------------------------------------------------------------- tiled statistics
+// mu, Sigma_qq and Sigma_qb for q up to 32 in one pass over V: one CTA per
+// t-batch stages 128-column tiles of its q rows of V, of beta and of the r rows
+// of Vb in shared memory; each thread owns up to kQtOut of the q(q+1)/2 + q + q r
+// dot products (pairs, mean, cross terms) and sums the tile's columns in four
+// chains, starting at a lane-dependent column so the warp reads 32 different
+// banks; tile partials add up in float64 (the mean's per tile compensated).
+constexpr int kQtThreads = 256, kQtCols = 128, kQtOut = 3;
+
+// With nsplit > 1 (few t-batches), CTA (t-batch, split) takes every nsplit-th
+// block of tiles and writes its partial sums to part[(t-batch, split, output)];
+// qstats_tile_finish_kernel adds the splits in order and writes the outputs.
+template <typename T>
+__device__ __forceinline__ void qstats_tile_outputs(const QBatchArgs& a, int q, int r,
+                                                    int64_t bidx, int kind, int i, int j,
+                                                    double tot);
+
+template <typename T>
+__global__ void __launch_bounds__(kQtThreads)
+    qstats_tile_kernel(const __grid_constant__ QBatchArgs a, const T* __restrict__ V, int64_t ldv,
+                       const T* __restrict__ beta, const T* __restrict__ Vb, int nsplit,
+                       double* __restrict__ part) {
+    extern __shared__ __align__(16) unsigned char qt_raw[];
+    T* S = reinterpret_cast<T*>(qt_raw);  // R x kQtCols, rows: V (q), beta, Vb (r)
+    const int q = a.q, r = a.r, R = q + 1 + r;
+    const int64_t n = a.n, bidx = blockIdx.x / nsplit, rbase = bidx * q;
+    const int split = blockIdx.x % nsplit;
+    const int np = q * (q + 1) / 2, nout = np + q + q * r;
+    const int tid = threadIdx.x, lane = tid % 32;
+    int ra[kQtOut], rb[kQtOut], kind[kQtOut];  // kind: 0 none, 1 pair, 2 mean, 3 cross
+    double tot[kQtOut];
+#pragma unroll
+    for (int k = 0; k < kQtOut; ++k) {
+        const int o = tid + k * kQtThreads;
+        tot[k] = 0.0;
+        ra[k] = rb[k] = 0;
+        kind[k] = 0;
+        if (o < np) {
+            int i = 0;
+            while ((i + 1) * (i + 2) / 2 <= o) ++i;
+            ra[k] = i;
+            rb[k] = o - i * (i + 1) / 2;
+            kind[k] = 1;
+        } else if (o < np + q) {
+            ra[k] = o - np;
+            rb[k] = q;
+            kind[k] = 2;
+        } else if (o < nout) {
+            const int p = o - np - q;
+            ra[k] = p / r;
+            rb[k] = q + 1 + p % r;
+            kind[k] = 3;
+        }
+    }
+    for (int64_t c0 = (int64_t)split * kQtCols; c0 < n; c0 += (int64_t)nsplit * kQtCols) {
+        const int64_t cw = (n - c0) < kQtCols ? (n - c0) : kQtCols;
+        for (int idx = tid; idx < R * kQtCols; idx += kQtThreads) {
+            const int row = idx / kQtCols, c = idx % kQtCols;
+            T v = T(0);
+            if (c < cw) {
+                if (row < q) v = V[(rbase + row) * ldv + c0 + c];
+                else if (row == q) v = beta[c0 + c];
+                else v = Vb[(int64_t)(row - q - 1) * n + c0 + c];
+            }
+            S[idx] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kQtOut; ++k) {
+            if (kind[k] == 0) continue;
+            const T* x = S + ra[k] * kQtCols;
+            const T* y = S + rb[k] * kQtCols;
+            if (kind[k] != 2) {
+                T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+#pragma unroll 4
+                for (int c = 0; c < kQtCols; c += 4) {
+                    const int c_a = (c + lane) % kQtCols, c_b = (c + 1 + lane) % kQtCols;
+                    const int c_c = (c + 2 + lane) % kQtCols, c_d = (c + 3 + lane) % kQtCols;
+                    s0 = fma(x[c_a], y[c_a], s0);
+                    s1 = fma(x[c_b], y[c_b], s1);
+                    s2 = fma(x[c_c], y[c_c], s2);
+                    s3 = fma(x[c_d], y[c_d], s3);
+                }
+                tot[k] += (double)((s0 + s1) + (s2 + s3));
+            } else {
+                T sh = T(0), sc = T(0);
+                for (int c = 0; c < kQtCols; ++c) {
+                    const int cc = (c + lane) % kQtCols;
+                    comp_add<T>(sh, sc, x[cc] * y[cc]);
+                }
+                tot[k] += (double)sh - (double)sc;
+            }
+        }
+        __syncthreads();
+    }
+    // the zero-padded columns of a partial last tile added nothing
+#pragma unroll
+    for (int k = 0; k < kQtOut; ++k) {
+        if (kind[k] == 0) continue;
+        if (nsplit > 1)
+            part[((int64_t)bidx * nsplit + split) * nout + tid + k * kQtThreads] = tot[k];
+        else
+            qstats_tile_outputs<T>(a, q, r, bidx, kind[k], ra[k], rb[k], tot[k]);
+    }
+}
+
+// sig / mu / sqb of output (kind, i, j) from its float64 sum
+template <typename T>
+__device__ __forceinline__ void qstats_tile_outputs(const QBatchArgs& a, int q, int r,
+                                                    int64_t bidx, int kind, int i, int j,
+                                                    double tot) {
+    const int64_t rbase = bidx * q;
+    if (kind == 1) {
+        const double v = kernel_pair<T>(a, rbase + i, rbase + j, 0) - tot;
+        a.sig[(bidx * q + i) * q + j] = v;
+        a.sig[(bidx * q + j) * q + i] = v;
+    } else if (kind == 2) {
+        a.mu[rbase + i] = a.mean_constant + tot;
+    } else if (kind == 3) {
+        const int kb = j - q - 1;
+        a.sqb[(bidx * q + i) * r + kb] = kernel_pair<T>(a, rbase + i, -1, kb) - tot;
+    }
+}
+
+// one CTA per t-batch: the splits' partial sums in split order, then the outputs
+template <typename T>
+__global__ void __launch_bounds__(kQtThreads)
+    qstats_tile_finish_kernel(const __grid_constant__ QBatchArgs a, int nsplit,
+                              const double* __restrict__ part) {
+    const int q = a.q, r = a.r;
+    const int np = q * (q + 1) / 2, nout = np + q + q * r;
+    const int64_t bidx = blockIdx.x;
+    for (int o = threadIdx.x; o < nout; o += kQtThreads) {
+        double tot = 0.0;
+        for (int sp = 0; sp < nsplit; ++sp) tot += part[((int64_t)bidx * nsplit + sp) * nout + o];
+        int kind, i, j;
+        if (o < np) {
+            i = 0;
+            while ((i + 1) * (i + 2) / 2 <= o) ++i;
+            j = o - i * (i + 1) / 2;
+            kind = 1;
+        } else if (o < np + q) {
+            i = o - np;
+            j = q;
+            kind = 2;
+        } else {
+            const int p = o - np - q;
+            i = p / r;
+            j = q + 1 + p % r;
+            kind = 3;
+        }
+        qstats_tile_outputs<T>(a, q, r, bidx, kind, i, j, tot);
+    }
+}
+
 // ---------------------------------------------------------------- smooth pieces
 // softplus with torch's threshold 20 (beta = 1)
 __device__ __forceinline__ double softplus_t(double x) { return x > 20.0 ? x : log1p(exp(x)); }
@@ -1882,6 +2037,36 @@ int launch_qstats_group(const GroupTab& t, int qmax, int rmax, int64_t total, cu
 }
 
 template <typename T>
+int launch_qstats_tile(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb,
+                       void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+    if (a.b <= 0) return BGB_OK;
+    const int q = a.q, r = a.r;
+    const int nout = q * (q + 1) / 2 + q + q * r;
+    const size_t smem = sizeof(T) * (size_t)(q + 1 + r) * kQtCols;
+    if (q > 32 || nout > kQtThreads * kQtOut || smem > 96 * 1024 || a.b > 0x7fffffff)
+        return BGB_ERR_UNSUPPORTED;
+    if (smem > 48 * 1024)
+        BGB_CUDA_TRY(cudaFuncSetAttribute(qstats_tile_kernel<T>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // few t-batches: split each one's tiles over CTAs (about two waves of CTAs),
+    // as far as the scratch holds the partial sums
+    const int64_t tiles = ceil_div(a.n, (int64_t)kQtCols);
+    int64_t nsplit = ceil_div((int64_t)sm_count() * 2, a.b);
+    if (nsplit > tiles) nsplit = tiles;
+    while (nsplit > 1 && (size_t)(a.b * nsplit * nout) * sizeof(double) > scratch_bytes) --nsplit;
+    if (nsplit < 1 || a.b * nsplit > 0x7fffffff) nsplit = 1;
+    double* part = nsplit > 1 ? static_cast<double*>(scratch) : nullptr;
+    qstats_tile_kernel<T><<<(unsigned)(a.b * nsplit), kQtThreads, smem, stream>>>(
+        a, V, ldv, beta, Vb, (int)nsplit, part);
+    BGB_CHECK_LAUNCH();
+    if (nsplit > 1) {
+        qstats_tile_finish_kernel<T><<<(unsigned)a.b, kQtThreads, 0, stream>>>(a, (int)nsplit, part);
+        BGB_CHECK_LAUNCH();
+    }
+    return BGB_OK;
+}
+
+template <typename T>
 int launch_row_dots(const QBatchArgs& a, const T* V, int64_t ldv, const T* beta, const T* Vb, T* P,
                     cudaStream_t stream) {
     const int64_t rows = a.b * a.q;
@@ -2112,6 +2297,10 @@ template int launch_qstats<double>(const QBatchArgs&, const double*, int64_t, co
                                    const double*, cudaStream_t);
 template int launch_qstats<float>(const QBatchArgs&, const float*, int64_t, const float*,
                                   const float*, cudaStream_t);
+template int launch_qstats_tile<double>(const QBatchArgs&, const double*, int64_t, const double*,
+                                        const double*, void*, size_t, cudaStream_t);
+template int launch_qstats_tile<float>(const QBatchArgs&, const float*, int64_t, const float*,
+                                       const float*, void*, size_t, cudaStream_t);
 template int launch_row_dots<double>(const QBatchArgs&, const double*, int64_t, const double*,
                                      const double*, double*, cudaStream_t);
 template int launch_row_dots<float>(const QBatchArgs&, const float*, int64_t, const float*,

@@ -224,6 +224,27 @@ def test_qlognei_ragged_q(cuda_lib, q):
     assert rel(v, ov) < 1e-9 and rel(X.grad, og) < 1e-8
 
 
+@pytest.mark.parametrize("q", [12, 16])
+def test_qlognei_mixed_large_q(cuda_lib, capsys, q):
+    """q > 8: the mixed path's covariance reduction from shared-memory tiles
+    (qstats_tile_kernel), held per t-batch against the float64 oracle with the
+    mean-shift sensitivities computed here (as the differentiation configuration,
+    whose workload generator this is, with its factor)."""
+    from oracle.sensitivity import mean_sensitivity
+
+    w = T.qlognei_diff(b=24, q=q, n=130)
+    gm = gpu_model(w)
+    ga, oa = _qlognei_pair(w, "mixed")
+    X = w.X.to(DEV).requires_grad_(True)
+    v = ga(X)
+    v.sum().backward()
+    ov, og = oa.value_and_grad(w.X)
+    sens_v, sens_g = mean_sensitivity(oa, w.X, ov, og)
+    check_mixed_per_batch(v.detach().cpu(), X.grad.cpu(), ov, og, sens_v, sens_g,
+                          mixed_mean_error(gm, w.X), f"mixed q={q}", capsys, normwise=False,
+                          factor=32.0)
+
+
 def test_qlognei_singular_q_batch_uses_jitter(cuda_lib):
     # two identical points in a q-batch make Sigma_qq singular: psd_safe_cholesky adds jitter
     w = T.qlognei_diff(b=8, q=3, n=100)

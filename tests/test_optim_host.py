@@ -1,5 +1,6 @@
 """Raw-sample initialisation host logic (no GPU)."""
 
+import platform
 import pytest
 import torch
 
@@ -155,7 +156,9 @@ def test_batched_lbfgsb_reproduces_the_reference_batched_driver():
     res = batched_lbfgsb(lambda X, rows: fg_batched(X, rows, c, w), x0, lo, hi, {"maxiter": 40})
     xs = np.stack([r["x"] for r in res])
     nit = np.array([r["nit"] for r in res])
-    if str(fx["scipy_version"]) == scipy.__version__:
+    # bit for bit where scipy's compiled routine is the fixture's (same version, x86-64);
+    # another build of it rounds differently
+    if str(fx["scipy_version"]) == scipy.__version__ and platform.machine() == "x86_64":
         assert np.array_equal(xs, fx["x"]) and np.array_equal(nit, fx["nit"])
     else:
         assert np.allclose(xs, fx["x"], rtol=0, atol=1e-10)
