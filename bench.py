@@ -56,6 +56,8 @@ def parse():
                    help="only warm up and run --steps mixed-precision steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     p.add_argument("--simt", action="store_true", help="FFMA GEMMs instead of tcgen05")
+    p.add_argument("--profile-precision", default="mixed", choices=["mixed", "fp64"],
+                   help="the path --profile runs (fp64: the plain float64 kernels)")
     p.add_argument("--config", default="headline",
                    choices=["headline", "many_gps", "optimize", "log_areas", "fit"],
                    help="many_gps: 64 GPs of uneven size in one tuned CUDA-graph launch; "
@@ -238,7 +240,7 @@ def run_ours(args) -> None:
         print(json.dumps({"profile_fit": True, "n": N_TRAIN, "jitter": m.train_jitter}))
         return
     model = make_model(device, w)
-    acqf = make_acqf(model, w, "mixed")
+    acqf = make_acqf(model, w, args.profile_precision if args.profile else "mixed")
     acqf.check_status = False
     acqf.use_tensor_cores = not args.simt
     Xd = w.X.to(device).contiguous()
