@@ -69,6 +69,22 @@ class BgbAcq(ctypes.Structure):
                 ("Lb_inv_lv", c_vp), ("best_f_lv", c_vp)]
 
 
+class BgbLbfgsbOpts(ctypes.Structure):
+    _fields_ = [("restarts", c_i64), ("n", c_i64), ("m", c_i32), ("maxls", c_i32),
+                ("maxiter", c_i64), ("maxfun", c_i64), ("factr", c_f64), ("pgtol", c_f64)]
+
+
+BGB_LBFGSB_MESSAGES = {
+    0: "RUNNING",
+    1: "CONVERGENCE: NORM OF PROJECTED GRADIENT <= PGTOL",
+    2: "CONVERGENCE: RELATIVE REDUCTION OF F <= FACTR*EPSMCH",
+    3: "ABNORMAL: ABNORMAL_TERMINATION_IN_LNSRCH",
+    4: "STOP: TOTAL NO. OF ITERATIONS REACHED LIMIT",
+    5: "STOP: TOTAL NO. OF F,G EVALUATIONS EXCEEDS LIMIT",
+    6: "ERROR: NON-FINITE VALUE OR GRADIENT",
+}
+
+
 _SIGNATURES = {
     "bgb_version": (c_i32, []),
     "bgb_kernel_matrix": (c_i32, [ctypes.POINTER(BgbGP), c_vp, c_i64, c_vp, c_i64, c_f64, c_vp,
@@ -128,6 +144,12 @@ _SIGNATURES = {
     "bgb_group_run": (c_i32, [c_vp, c_vp]),
     "bgb_group_launches": (c_i32, [c_vp]),
     "bgb_group_destroy": (None, [c_vp]),
+    "bgb_lbfgsb_workspace_bytes": (c_size, [ctypes.POINTER(BgbLbfgsbOpts)]),
+    "bgb_lbfgsb_init": (c_i32, [ctypes.POINTER(BgbLbfgsbOpts), c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
+    "bgb_lbfgsb_step": (c_i32, [ctypes.POINTER(BgbLbfgsbOpts), c_vp, c_vp, c_f64, c_vp, c_vp, c_i32,
+                                c_vp, c_size, c_vp, c_vp]),
+    "bgb_lbfgsb_results": (c_i32, [ctypes.POINTER(BgbLbfgsbOpts), c_vp, c_size, c_vp, c_vp, c_vp,
+                                   c_vp, c_vp]),
     "bgb_log_areas_forward": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64, c_i64,
                                       c_f64, c_f64, c_vp, c_vp]),
     "bgb_log_areas_forward_f32": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64,

@@ -10,25 +10,22 @@ argument meanings.
   samples, keeping the best raw sample (botorch/optim/initializers.py:959-1042,
   botorch/utils/sampling.py:1084-1115).
 * ``gen_candidates_scipy``: L-BFGS-B on the restarts, in either of the
-  reference's two modes. By default the restarts are aggregated into one
-  problem whose objective is minus the sum of the values (the reference's
-  aggregated mode, gen.py:249-395). With ``use_parallel_mode=True`` every
-  restart runs its own L-BFGS-B on minus its own value, with the objectives
-  of all restarts evaluated in one call per round (the reference's fast
-  path, botorch/generation/gen.py:226-247 with botorch/optim/batched_lbfgs_b.py,
-  which the reference takes by default). That mode steps scipy's
-  reverse-communication L-BFGS-B routine for every restart on the calling
-  thread, as the reference does, where the installed scipy has the interface
-  this driver follows (>= 1.15) and reproduces scipy's own ``minimize`` bit
-  for bit in a self-test; otherwise it runs one scipy optimiser per restart
-  in its own host thread, whose cost per round depends on the host's thread
-  wake-up latency (15 ms and 130 ms per round of 64 restarts on two GPU
-  hosts, same results). Either way its host cost is one L-BFGS-B step per
-  restart per round, so the aggregated mode stays the default. Each
-  evaluation copies the points to the device, evaluates value + gradient of
-  every restart in one call (a CUDA graph replay at fixed shape) and copies
-  both back through pinned host buffers (the f / grad wrapper of
-  gen.py:423-487).
+  reference's two modes. By default (``use_parallel_mode`` None or True, the
+  reference's fast path, botorch/generation/gen.py:226-247 with
+  botorch/optim/batched_lbfgs_b.py) every restart runs its own L-BFGS-B on
+  minus its own value, the objectives of all restarts evaluated in one call
+  per round. For an acquisition function on a CUDA device the restarts'
+  L-BFGS-B states live on the device (``botorch_gb300.lbfgsb``): a round is
+  the evaluation, one step launch and a four-integer summary read by the
+  host, captured in one CUDA graph. ``lbfgsb="scipy"`` instead steps scipy's
+  reverse-communication routine for every restart on the calling thread, as
+  the reference does (scipy >= 1.15, checked bit for bit against scipy's own
+  ``minimize`` in a self-test; else one scipy optimiser per restart in its own
+  host thread); each evaluation then copies the points to the device and the
+  values and gradients back through pinned buffers (the f / grad wrapper of
+  gen.py:423-487). With ``use_parallel_mode=False`` the restarts are
+  aggregated into one problem whose objective is minus the sum of the values
+  (the reference's aggregated mode, gen.py:249-395).
 * ``optimize_acqf``: raw samples -> restarts -> L-BFGS-B -> the best restart
   (botorch/optim/optimize.py:619, ``return_best_only=True``).
 """
@@ -39,6 +36,7 @@ import numpy as np
 import torch
 from torch import Tensor
 
+from botorch_gb300 import _native as nat
 from botorch_gb300._lbfgsb_rc import _RCRestart  # noqa: F401
 from botorch_gb300._lbfgsb_rc import lbfgsb_rc as _lbfgsb_rc
 
@@ -288,6 +286,72 @@ def _per_restart_rc(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape,
     return results, rounds.calls
 
 
+_DEVICE_LBFGSB_OPTIONS = ("maxcor", "ftol", "gtol", "maxls", "maxfun")
+
+
+def _per_restart_device(acqf, X0: Tensor, lo: np.ndarray, hi: np.ndarray, maxiter: int, options: dict,
+                        use_graph: bool):
+    """Each restart's own L-BFGS-B with its state on the device (``DeviceLbfgsb``):
+    a round is one batched evaluation of all restarts, one step launch and a
+    four-integer summary read by the host (the round captured in one CUDA graph).
+    A round whose evaluation reports a failed t-batch is evaluated again through
+    the acquisition function's checked call (its fallback route, or its error)
+    before the restarts consume it. Returns the points, the per-restart results
+    and the rounds."""
+    from botorch_gb300.lbfgsb import DeviceLbfgsb
+
+    b, q, d = X0.shape
+    dev = X0.device
+    X = X0.reshape(b, q * d).to(torch.float64).contiguous().clone()
+    Xv = X.view(b, q, d)
+    lb = DeviceLbfgsb(X, torch.from_numpy(np.tile(lo, q)), torch.from_numpy(np.tile(hi, q)), maxiter=maxiter,
+                      **{k: options[k] for k in _DEVICE_LBFGSB_OPTIONS if k in options})
+    value = torch.empty(b, dtype=torch.float64, device=dev)
+    grad = torch.empty(b, q, d, dtype=torch.float64, device=dev)
+    status = torch.zeros(b, dtype=torch.int32, device=dev)
+    acq_ws = nat.Workspace(dev)
+    host = torch.zeros(4, dtype=torch.int32).pin_memory()
+
+    def round_body():
+        acqf.value_and_grad_raw(Xv, True, check=False, out=(value, grad, status), ws=acq_ws)
+        lb.step(value, grad, sign=-1.0, status=status)
+        host.copy_(lb.summary, non_blocking=True)
+
+    graph = None
+    if use_graph:
+        # set up the acquisition's state for this shape, then capture one round
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            acqf.value_and_grad_raw(Xv, True, check=False, out=(value, grad, status), ws=acq_ws)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            round_body()
+    stream = torch.cuda.current_stream(dev)
+    rounds = 0
+    while True:
+        if graph is not None:
+            graph.replay()
+        else:
+            round_body()
+        stream.synchronize()
+        rounds += 1
+        act, held, nonfin = int(host[0]), int(host[1]), int(host[2])
+        if held:
+            v, g = acqf.value_and_grad_raw(Xv, True)
+            lb.step(v.contiguous(), g.contiguous(), sign=-1.0, ignore_status=True)
+            host.copy_(lb.summary, non_blocking=True)
+            stream.synchronize()
+            act, nonfin = int(host[0]), int(host[2])
+        if nonfin:
+            raise RuntimeError("the acquisition value or its gradient is not finite (NaN elements of the gradient)")
+        if act == 0:
+            break
+    return Xv, lb.results(), rounds
+
+
 def _per_restart_lbfgsb(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape, maxiter: int,
                         options: dict, use_graph: bool):
     """Each restart's own L-BFGS-B (scipy, one host thread each), objectives batched
@@ -324,15 +388,22 @@ def _per_restart_lbfgsb(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, sh
 def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower_bounds: float | Tensor,
                          upper_bounds: float | Tensor, options: dict | None = None,
                          use_graph: bool = True,
-                         use_parallel_mode: bool | None = None) -> tuple[Tensor, Tensor]:
+                         use_parallel_mode: bool | None = None,
+                         lbfgsb: str | None = None) -> tuple[Tensor, Tensor]:
     """L-BFGS-B from the ``b x q x d`` initial conditions on the box; returns the
     candidates and their acquisition values.
 
     ``use_parallel_mode`` None (the default) or True: the reference's fast path
     (botorch/generation/gen.py:226-247, taken unless use_parallel_mode is False):
     every restart runs its own L-BFGS-B on minus its own value, with one batched
-    evaluation per round (``batched_lbfgsb``). False: one L-BFGS-B on minus the
-    sum of all restarts' values (the reference's aggregated mode, gen.py:249-395)."""
+    evaluation per round. False: one L-BFGS-B on minus the sum of all restarts'
+    values (the reference's aggregated mode, gen.py:249-395).
+
+    ``lbfgsb`` (per-restart mode): "device" (the default for an acquisition
+    function on a CUDA device) keeps every restart's L-BFGS-B state on the
+    device (``botorch_gb300.lbfgsb``; the same algorithm as scipy's routine,
+    iterates equal to rounding); "scipy" steps scipy's own routine per restart
+    on the host (``batched_lbfgsb``; scipy's iterates bit for bit)."""
     from scipy.optimize import minimize
 
     options = dict(options or {})
@@ -346,6 +417,21 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
         v0, _ = acquisition_function.value_and_grad_raw(
             torch.from_numpy(x0.reshape(b, q, d)).to(acquisition_function.device), False)
         f0 = -float(v0.sum())
+        on_cuda = torch.device(acquisition_function.device).type == "cuda"
+        which = lbfgsb or ("device" if on_cuda else "scipy")
+        if which not in ("device", "scipy"):
+            raise ValueError(f"lbfgsb must be 'device' or 'scipy', got {lbfgsb!r}")
+        if which == "device":
+            X, res, calls = _per_restart_device(
+                acquisition_function, torch.from_numpy(x0.reshape(b, q, d)).to(acquisition_function.device),
+                lo, hi, maxiter, options, use_graph)
+            v, _ = acquisition_function.value_and_grad_raw(X.contiguous(), False)
+            nits = [int(t) for t in res["nit"]]
+            info = {"mode": "per-restart", "driver": "device", "nit": max(nits), "nfev": int(calls),
+                    "nit_per_restart": nits, "message": str(res["message"][0]),
+                    "messages": list(res["message"]), "f0": f0, "f": -float(v.sum())}
+            gen_candidates_scipy.last_info = info
+            return X, v.clone()
         rc = _lbfgsb_rc()
         if rc is not None:
             results, calls = _per_restart_rc(acquisition_function, x0.reshape(b, -1), lo, hi, (b, q, d),
@@ -377,7 +463,8 @@ def gen_candidates_scipy(initial_conditions: Tensor, acquisition_function, lower
 
 def optimize_acqf(acq_function, bounds: Tensor, q: int, num_restarts: int, raw_samples: int,
                   options: dict | None = None, seed: int | None = None,
-                  use_graph: bool = True, use_parallel_mode: bool | None = None) -> tuple[Tensor, Tensor]:
+                  use_graph: bool = True, use_parallel_mode: bool | None = None,
+                  lbfgsb: str | None = None) -> tuple[Tensor, Tensor]:
     """Raw samples -> Boltzmann-selected restarts -> L-BFGS-B -> the best restart.
 
     options: ``batch_limit`` (raw-sample evaluation chunk, 4096), ``eta`` (1.0),
@@ -391,6 +478,6 @@ def optimize_acqf(acq_function, bounds: Tensor, q: int, num_restarts: int, raw_s
     g = None if seed is None else torch.Generator(device=v_raw.device).manual_seed(seed)
     X0, _ = initialize_q_batch(X_raw.to(v_raw.device), v_raw, num_restarts, eta=eta, generator=g)
     X, v = gen_candidates_scipy(X0, acq_function, bounds[0], bounds[1], options, use_graph,
-                                use_parallel_mode)
+                                use_parallel_mode, lbfgsb)
     best = int(torch.argmax(v))
     return X[best], v[best]

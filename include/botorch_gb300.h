@@ -455,6 +455,55 @@ int bgb_log_areas_backward_jac_f32(const float* grad_out, const float* jac, int6
                                    int64_t n_sub, int64_t isz, int64_t m, int64_t nc,
                                    float* grad_obj, void* stream);
 
+/* ---- Batched L-BFGS-B on the device: the per-restart optimiser of the
+ * reference's fast path (botorch/generation/gen.py:226-247, which drives
+ * fmin_l_bfgs_b_batched, botorch/optim/batched_lbfgs_b.py:169-636, stepping
+ * scipy's L-BFGS-B routine once per restart and round). `restarts`
+ * independent problems of n variables share the bounds; each keeps its own
+ * L-BFGS-B 3.0 state (history m, line search of More and Thuente) in the
+ * workspace. Reverse communication, as scipy's routine: init projects every
+ * row of X (restarts x n) onto the box and leaves each restart waiting for f
+ * and g at its row; every step consumes the objective f = sign * value[r] and
+ * g = sign * grad[r] of the restarts that wait, advances each to the next
+ * point it needs (written into its row of X) or stops it, and (summary !=
+ * NULL) writes four int32 counts: restarts still waiting for f and g, restarts
+ * held back because some row's status was nonzero (ignore_status = 0; the
+ * caller evaluates X again another way and repeats the step with ignore_status
+ * = 1), restarts stopped on a non-finite value or gradient, restarts stopped.
+ * Stopped restarts keep their row of X. The stopping rules and options mean
+ * what they mean for scipy.optimize.minimize(method="L-BFGS-B"): factr =
+ * ftol / machine epsilon, pgtol = gtol, maxls, maxiter (iterations), maxfun
+ * (evaluations). 1 <= n <= 8192 and 1 <= m <= 20 (else BGB_ERR_UNSUPPORTED);
+ * lower / upper are device arrays of n bounds (+-inf: none). Every call only
+ * launches (capturable in a CUDA graph). */
+typedef struct bgb_lbfgsb_opts {
+    int64_t restarts;
+    int64_t n;
+    int32_t m;
+    int32_t maxls;
+    int64_t maxiter;
+    int64_t maxfun;
+    double factr;
+    double pgtol;
+} bgb_lbfgsb_opts;
+#define BGB_LBFGSB_RUNNING 0
+#define BGB_LBFGSB_CONV_PGTOL 1    /* projected gradient <= pgtol */
+#define BGB_LBFGSB_CONV_FTOL 2     /* relative reduction of f <= factr * eps */
+#define BGB_LBFGSB_ABNORMAL 3      /* line search failed with no history left */
+#define BGB_LBFGSB_MAXITER 4
+#define BGB_LBFGSB_MAXFUN 5
+#define BGB_LBFGSB_NONFINITE 6     /* f or g not finite at the restart's point */
+size_t bgb_lbfgsb_workspace_bytes(const bgb_lbfgsb_opts* opts);
+int bgb_lbfgsb_init(const bgb_lbfgsb_opts* opts, double* X, const double* lower, const double* upper,
+                    void* workspace, size_t workspace_bytes, void* stream);
+int bgb_lbfgsb_step(const bgb_lbfgsb_opts* opts, double* X, const double* value, double sign,
+                    const double* grad, const int32_t* status, int32_t ignore_status,
+                    void* workspace, size_t workspace_bytes, int32_t* summary, void* stream);
+/* Per restart: f at its row of X, iterations, evaluations, BGB_LBFGSB_* code
+ * (any pointer may be NULL). */
+int bgb_lbfgsb_results(const bgb_lbfgsb_opts* opts, const void* workspace, size_t workspace_bytes,
+                       double* f, int64_t* nit, int64_t* nfev, int32_t* code, void* stream);
+
 /* Number of kernel launches this library has issued in the process so far.
  * Measurement aid; no reference counterpart. */
 unsigned long long bgb_launch_count(void);

@@ -96,3 +96,45 @@ def test_header_constants_match_the_bindings():
                  "BGB_FLAG_JOINT_SAMPLING", "BGB_FLAG_UNCACHED_ROOT"):
         assert int(eval(defs[name])) == getattr(_native, name), name
     assert eval(defs["BGB_NOALLOC_SCRATCH_BYTES"].replace("(size_t)", "")) == _native.BGB_NOALLOC_SCRATCH_BYTES
+
+
+def test_lbfgsb_options_layout_and_queries(tmp_path):
+    """bgb_lbfgsb_opts has the C compiler's layout; the size query and the argument
+    checks need no GPU."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f for f, _ in _native.BgbLbfgsbOpts._fields_]
+    src = tmp_path / "lb.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "botorch_gb300.h"\n'
+        "int main(void) {\n"
+        '  printf("%zu\\n", sizeof(bgb_lbfgsb_opts));\n'
+        + "".join(f'  printf("%zu\\n", offsetof(bgb_lbfgsb_opts, {f}));\n' for f in fields)
+        + '  printf("%d %d %d\\n", BGB_LBFGSB_CONV_PGTOL, BGB_LBFGSB_ABNORMAL, BGB_LBFGSB_NONFINITE);\n'
+        + "  return 0;\n}\n")
+    exe = tmp_path / "lb"
+    subprocess.run([cc, "-I", str(HEADER.parent), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert int(out[0]) == ctypes.sizeof(_native.BgbLbfgsbOpts)
+    for f, off in zip(fields, out[1:1 + len(fields)]):
+        assert getattr(_native.BgbLbfgsbOpts, f).offset == int(off), f
+    codes = [int(v) for v in out[1 + len(fields):]]
+    assert [_native.BGB_LBFGSB_MESSAGES[c].split(":")[0] for c in codes] == ["CONVERGENCE", "ABNORMAL", "ERROR"]
+
+    lib = _native.lib()
+    opts = _native.BgbLbfgsbOpts(restarts=64, n=800, m=10, maxls=20, maxiter=100, maxfun=15000, factr=1e7,
+                                 pgtol=1e-5)
+    wsb = lib.bgb_lbfgsb_workspace_bytes(ctypes.byref(opts))
+    assert wsb >= 64 * (2 * 10 * 800 + 7 * 800) * 8
+    too_big = _native.BgbLbfgsbOpts(restarts=1, n=8193, m=10, maxls=20, maxiter=1, maxfun=1, factr=1e7, pgtol=0)
+    assert lib.bgb_lbfgsb_workspace_bytes(ctypes.byref(too_big)) == 0
+    assert lib.bgb_lbfgsb_init(ctypes.byref(too_big), 1, 1, 1, 1, 1 << 30, None) == _native.BGB_ERR_UNSUPPORTED
+    bad = _native.BgbLbfgsbOpts(restarts=1, n=4, m=0, maxls=20, maxiter=1, maxfun=1, factr=1e7, pgtol=0)
+    assert lib.bgb_lbfgsb_step(ctypes.byref(bad), 1, 1, 1.0, 1, None, 0, 1, 1 << 30, None, None) == \
+        _native.BGB_ERR_ARG
+    assert lib.bgb_lbfgsb_init(ctypes.byref(opts), None, 1, 1, 1, wsb, None) == _native.BGB_ERR_ARG
+    assert lib.bgb_lbfgsb_init(ctypes.byref(opts), 1, 1, 1, 1, wsb - 1, None) == _native.BGB_ERR_WORKSPACE
