@@ -8,6 +8,8 @@
 // four-integer summary.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "bgb_common.cuh"
 #include "lbfgsb_core.cuh"
 
@@ -24,9 +26,7 @@ __global__ void __launch_bounds__(LB_NT) lbfgsb_init_kernel(const __grid_constan
 __global__ void __launch_bounds__(LB_NT) lbfgsb_step_kernel(const __grid_constant__ bgb_lb::StepArgs a, int n2) {
     __shared__ bgb_lb::Shm sh;
     extern __shared__ __align__(16) unsigned char lb_dyn[];
-    double* key = reinterpret_cast<double*>(lb_dyn);
-    int* idx = reinterpret_cast<int*>(lb_dyn + sizeof(double) * n2);
-    bgb_lb::step_restart(a, blockIdx.x, sh, key, idx, n2);
+    bgb_lb::step_restart(a, blockIdx.x, sh, lb_dyn, n2);
 }
 
 __global__ void __launch_bounds__(LB_NT)
@@ -56,7 +56,23 @@ int check_opts(const bgb_lbfgsb_opts* o) {
 
 Layout layout_of(const bgb_lbfgsb_opts* o) { return bgb_lb::make_layout(o->restarts, o->n, o->m); }
 
-size_t step_smem_bytes(int n2) { return (size_t)n2 * (sizeof(double) + sizeof(int)); }
+size_t step_smem_bytes(int n2) { return (size_t)bgb_lb::step_dyn_bytes(n2); }
+
+// The step's static plus dynamic shared memory exceeds the default 48 KB: allow
+// the largest size (n = kMaxN) once per device, outside any stream work.
+bool allow_step_smem() {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    const unsigned long long bit = 1ULL << dev;
+    if (done.load() & bit) return true;
+    const int bytes = (int)step_smem_bytes(bgb_lb::sort_len(bgb_lb::kMaxN));
+    if (cudaFuncSetAttribute(lbfgsb_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) !=
+        cudaSuccess)
+        return false;
+    done.fetch_or(bit);
+    return true;
+}
 
 }  // namespace
 }  // namespace bgb
@@ -84,6 +100,7 @@ int bgb_lbfgsb_init(const bgb_lbfgsb_opts* o, double* X, const double* lower, co
     a.X = X;
     a.lo = lower;
     a.hi = upper;
+    if (!bgb::allow_step_smem()) return BGB_ERR_CUDA;
     bgb::lbfgsb_init_kernel<<<(unsigned)o->restarts, LB_NT, 0, static_cast<cudaStream_t>(stream)>>>(a);
     BGB_CHECK_LAUNCH();
     return BGB_OK;
@@ -116,12 +133,7 @@ int bgb_lbfgsb_step(const bgb_lbfgsb_opts* o, double* X, const double* value, do
     a.ignore_status = ignore_status;
     const int n2 = bgb_lb::sort_len(a.n);
     const size_t smem = bgb::step_smem_bytes(n2);
-    if (smem > 48 * 1024) {
-        const size_t limit = smem;
-        if (cudaFuncSetAttribute(bgb::lbfgsb_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)limit) != cudaSuccess)
-            return BGB_ERR_CUDA;
-    }
+    if (!bgb::allow_step_smem()) return BGB_ERR_CUDA;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     bgb::lbfgsb_step_kernel<<<(unsigned)o->restarts, LB_NT, smem, s>>>(a, n2);
     BGB_CHECK_LAUNCH();

@@ -39,13 +39,19 @@
 #if defined(LB_HOST_EMU)
 #define LB_FN static inline
 #define LB_SYNC() ((void)0)
+#define LB_SYNCWARP() ((void)0)
 #define LB_NT 1
 #define LB_NW 1
+#define LB_WARP 1
+#define LB_HD inline
 #else
 #define LB_FN __device__ __forceinline__
 #define LB_SYNC() __syncthreads()
+#define LB_SYNCWARP() __syncwarp()
 #define LB_NT 256
 #define LB_NW 8
+#define LB_WARP 32
+#define LB_HD __host__ __device__ inline
 #endif
 
 namespace bgb_lb {
@@ -122,6 +128,7 @@ struct Shm {
     double wn[4 * kMaxM * kMaxM];
     double p[2 * kMaxM], c[2 * kMaxM], v[2 * kMaxM], wbp[2 * kMaxM], wv[2 * kMaxM];
     double dots[kMaxM * (2 * kMaxM + 1)];
+    double rd[2 * kMaxM], dinv[kMaxM], rsq[kMaxM], rwt[kMaxM];
     double red_d[LB_NW];
     int red_i[LB_NW];
     double f1, f2, f2_org, dtm, tsum, bkmin, alpha, rr, dr;
@@ -135,7 +142,14 @@ struct Ctx {
     double* key;  // breakpoint sort scratch (n2 entries)
     int* idx;
     int n2;
+    double* tile;   // row tiles of S and Y for the Gram sums (kTileRows + 1) x kTileCols
+    int8_t* tmask;  // free flags of the tile's rows
 };
+
+constexpr int kTileRows = 64;
+constexpr int kTileCols = 2 * kMaxM;
+// Dynamic shared memory of the step launch: breakpoint sort scratch, then the tile.
+
 
 // ---------------------------------------------------------------------------
 // Thread-level helpers.
@@ -259,91 +273,166 @@ LB_FN void warp_dots(int J, int n, const int8_t* iwhere, Setup setup, double* ou
     LB_SYNC();
 }
 
+// out[o] = sum_k a_o[k] b_o[k] over the free (mode 1) or active (mode 2) k, for
+// o < J, where a_o and b_o are among ncols <= kTileCols columns (column c at
+// col(c)) staged tile by tile in shared memory, so that each column is read
+// from memory once per 4 * LB_NT outputs: pair(o, ia, ib, mode) names them.
+template <class Col, class Pair>
+LB_FN void tiled_gram(int J, int n, int ncols, Col col, const int8_t* iwhere, Pair pair, double* tile,
+                      int8_t* tmask, double* out) {
+    const int t = lb_tid();
+    constexpr int ld = kTileRows + 1;  // (odd stride: the columns start in different banks)
+    for (int o0 = 0; o0 < J; o0 += 4 * LB_NT) {
+        int ia[4], ib[4], md[4];
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int q = 0; q < 4; ++q) {
+            const int o = o0 + t + q * LB_NT;
+            ia[q] = ib[q] = md[q] = -1;
+            if (o < J) pair(o, ia[q], ib[q], md[q]);
+        }
+        for (int k0 = 0; k0 < n; k0 += kTileRows) {
+            const int rows = n - k0 < kTileRows ? n - k0 : kTileRows;
+            for (int e = t; e < ncols * kTileRows; e += LB_NT) {
+                const int c = e / kTileRows, r = e - c * kTileRows;
+                tile[c * ld + r] = r < rows ? col(c)[k0 + r] : 0.0;
+            }
+            for (int r = t; r < kTileRows; r += LB_NT) tmask[r] = (r < rows && iwhere[k0 + r] <= 0) ? 1 : 0;
+            LB_SYNC();
+            for (int q = 0; q < 4; ++q) {
+                if (ia[q] < 0) continue;
+                const double* a = tile + ia[q] * ld;
+                const double* b = tile + ib[q] * ld;
+                const int8_t want = md[q] == 1 ? 1 : 0;
+                double sum = 0.0;
+                for (int r = 0; r < rows; ++r)
+                    if (tmask[r] == want) sum += a[r] * b[r];
+                acc[q] += sum;
+            }
+            LB_SYNC();
+        }
+        for (int q = 0; q < 4; ++q)
+            if (ia[q] >= 0) out[o0 + t + q * LB_NT] = acc[q];
+    }
+    LB_SYNC();
+}
+
 // Column of S or Y holding logical pair j (0 = oldest).
 LB_FN int colptr(const State& s, int m, int j) { return (s.head + j) % m; }
 
 // ---------------------------------------------------------------------------
-// Small dense kernels (one thread). Column-major, leading dimension ld.
+// Small dense kernels, run by the first warp of the CTA (all its lanes call
+// them; results are in shared memory after the call). Column-major, leading
+// dimension ld; n <= 2 * kMaxM.
 
-// Upper Cholesky factor R (A = R^T R) in place; 0 or the 1-based failing column.
-LB_FN int chol_upper(double* a, int ld, int n) {
-    for (int j = 0; j < n; ++j) {
-        double s = 0.0;
-        for (int k = 0; k < j; ++k) {
-            double t = a[k + j * ld];
-            for (int i = 0; i < k; ++i) t -= a[i + k * ld] * a[i + j * ld];
-            t /= a[k + k * ld];
-            a[k + j * ld] = t;
-            s += t * t;
+LB_FN int lane_id() { return lb_tid() & (LB_WARP - 1); }
+
+// sum_i a[i] b[i] over i < n, every lane gets it.
+LB_FN double warp_dot(const double* a, const double* b, int n) {
+    double acc = 0.0;
+    for (int i = lane_id(); i < n; i += LB_WARP) acc += a[i] * b[i];
+    return warp_sum(acc);
+}
+
+// Upper Cholesky factor R (A = R^T R) in place, right-looking; rdiag = 1 / diag(R).
+// Returns 0 or the 1-based column whose pivot is not positive.
+LB_FN int warp_chol_upper(double* a, int ld, int n, double* rdiag) {
+    const int l = lane_id();
+    for (int k = 0; k < n; ++k) {
+        const double akk = a[k + k * ld];
+        if (!(akk > 0.0)) return k + 1;
+        const double rkk = sqrt(akk);
+        const double inv = 1.0 / rkk;
+        for (int j = k + 1 + l; j < n; j += LB_WARP) a[k + j * ld] *= inv;
+        LB_SYNCWARP();
+        if (l == 0) {
+            a[k + k * ld] = rkk;
+            rdiag[k] = inv;
         }
-        s = a[j + j * ld] - s;
-        if (s <= 0.0) return j + 1;
-        a[j + j * ld] = sqrt(s);
+        for (int j = k + 1 + l; j < n; j += LB_WARP) {
+            const double rkj = a[k + j * ld];
+            for (int i = k + 1; i <= j; ++i) a[i + j * ld] -= a[k + i * ld] * rkj;
+        }
+        LB_SYNCWARP();
     }
     return 0;
 }
 
-LB_FN int zero_diag(const double* t, int ld, int n) {
+// rdiag = 1 / diag(T); 0, or the 1-based index of a zero diagonal entry.
+LB_FN int warp_rdiag(const double* t, int ld, int n, double* rdiag) {
+    for (int i = lane_id(); i < n; i += LB_WARP) rdiag[i] = 1.0 / t[i + i * ld];
+    LB_SYNCWARP();
     for (int i = 0; i < n; ++i)
         if (t[i + i * ld] == 0.0) return i + 1;
     return 0;
 }
 
-// Solve T x = b, T upper triangular (b overwritten).
-LB_FN int solve_upper(const double* t, int ld, int n, double* b) {
-    int info = zero_diag(t, ld, n);
-    if (info) return info;
-    b[n - 1] /= t[(n - 1) + (n - 1) * ld];
-    for (int j = n - 2; j >= 0; --j) {
-        const double tmp = -b[j + 1];
-        for (int i = 0; i <= j; ++i) b[i] += tmp * t[i + (j + 1) * ld];
-        b[j] /= t[j + j * ld];
+// Solve T^T x = b in place, T upper triangular.
+LB_FN void warp_solve_upper_t(const double* t, int ld, int n, const double* rdiag, double* b) {
+    const int l = lane_id();
+    for (int j = 0; j < n; ++j) {
+        const double xj = b[j] * rdiag[j];
+        LB_SYNCWARP();
+        if (l == 0) b[j] = xj;
+        for (int i = j + 1 + l; i < n; i += LB_WARP) b[i] -= t[j + i * ld] * xj;
+        LB_SYNCWARP();
     }
-    return 0;
 }
 
-// Solve T^T x = b, T upper triangular.
-LB_FN int solve_upper_t(const double* t, int ld, int n, double* b) {
-    int info = zero_diag(t, ld, n);
-    if (info) return info;
-    b[0] /= t[0];
-    for (int j = 1; j < n; ++j) {
-        double acc = 0.0;
-        for (int i = 0; i < j; ++i) acc += t[i + j * ld] * b[i];
-        b[j] = (b[j] - acc) / t[j + j * ld];
+// Solve T x = b in place, T upper triangular.
+LB_FN void warp_solve_upper(const double* t, int ld, int n, const double* rdiag, double* b) {
+    const int l = lane_id();
+    for (int j = n - 1; j >= 0; --j) {
+        const double xj = b[j] * rdiag[j];
+        LB_SYNCWARP();
+        if (l == 0) b[j] = xj;
+        for (int i = l; i < j; i += LB_WARP) b[i] -= t[i + j * ld] * xj;
+        LB_SYNCWARP();
     }
-    return 0;
+}
+
+// Solve T^T X = B for nrhs columns (column c at B + c * ldb), one lane per column.
+LB_FN void warp_solve_upper_t_multi(const double* t, int ld, int n, const double* rdiag, double* B, int ldb,
+                                    int nrhs) {
+    for (int c = lane_id(); c < nrhs; c += LB_WARP) {
+        double* b = B + c * ldb;
+        for (int j = 0; j < n; ++j) {
+            double acc = 0.0;
+            for (int i = 0; i < j; ++i) acc += t[i + j * ld] * b[i];
+            b[j] = (b[j] - acc) * rdiag[j];
+        }
+    }
+    LB_SYNCWARP();
 }
 
 // p = M v for the 2col x 2col middle matrix M of the compact form, through the
-// factor of T = theta S^T S + L D^-1 L^T (Byrd et al. 1995, section 3).
-LB_FN int middle_times(const Shm& sh, int m, int col, const double* v, double* p) {
+// factor of T = theta S^T S + L D^-1 L^T (Byrd et al. 1995, section 3); p and v distinct.
+LB_FN int middle_times(Shm& sh, int m, int col, const double* v, double* p) {
     if (col == 0) return 0;
+    const int l = lane_id();
     const double* sy = sh.sy;
-    p[col] = v[col];
-    for (int i = 1; i < col; ++i) {
+    for (int i = l; i < col; i += LB_WARP) {
+        const double di = sy[i + i * m];
+        sh.dinv[i] = 1.0 / di;
+        sh.rsq[i] = 1.0 / sqrt(di);
+    }
+    const int info = warp_rdiag(sh.wt, m, col, sh.rwt);
+    if (info) return info;
+    for (int i = l; i < col; i += LB_WARP) {
         double acc = 0.0;
-        for (int k = 0; k < i; ++k) acc += sy[i + k * m] * v[k] / sy[k + k * m];
+        for (int k = 0; k < i; ++k) acc += sy[i + k * m] * v[k] * sh.dinv[k];
         p[col + i] = v[col + i] + acc;
+        p[i] = v[i] * sh.rsq[i];
     }
-    int info = solve_upper_t(sh.wt, m, col, p + col);
-    if (info) return info;
-    for (int i = 0; i < col; ++i) p[i] = v[i] / sqrt(sy[i + i * m]);
-    info = solve_upper(sh.wt, m, col, p + col);
-    if (info) return info;
-    for (int i = 0; i < col; ++i) p[i] = -p[i] / sqrt(sy[i + i * m]);
-    for (int i = 0; i < col; ++i) {
+    LB_SYNCWARP();
+    warp_solve_upper_t(sh.wt, m, col, sh.rwt, p + col);
+    warp_solve_upper(sh.wt, m, col, sh.rwt, p + col);
+    for (int i = l; i < col; i += LB_WARP) {
         double acc = 0.0;
-        for (int k = i + 1; k < col; ++k) acc += sy[k + i * m] * p[col + k] / sy[i + i * m];
-        p[i] += acc;
+        for (int k = i + 1; k < col; ++k) acc += sy[k + i * m] * p[col + k];
+        p[i] = -p[i] * sh.rsq[i] + acc * sh.dinv[i];
     }
+    LB_SYNCWARP();
     return 0;
-}
-
-LB_FN double dot_small(const double* a, const double* b, int n) {
-    double s = 0.0;
-    for (int i = 0; i < n; ++i) s += a[i] * b[i];
-    return s;
 }
 
 // ---------------------------------------------------------------------------
@@ -495,34 +584,40 @@ LB_FN int cauchy(Ctx& c) {
                   mode = 0;
               },
               sh.p);
-    if (t == 0) {
-        for (int j = 0; j < col; ++j) sh.p[col + j] *= theta;
-        for (int j = 0; j < col2; ++j) sh.c[j] = 0.0;
+    if (t < LB_WARP) {
+        for (int j = lane_id(); j < col; j += LB_WARP) sh.p[col + j] *= theta;
+        for (int j = lane_id(); j < col2; j += LB_WARP) sh.c[j] = 0.0;
+        LB_SYNCWARP();
         double f2 = -theta * f1;
-        sh.f2_org = f2;
+        const double f2_org = f2;
         int info = 0;
         if (col > 0) {
             info = middle_times(sh, m, col, sh.p, sh.v);
-            if (!info) f2 -= dot_small(sh.v, sh.p, col2);
+            if (!info) f2 -= warp_dot(sh.v, sh.p, col2);
         }
-        sh.info = info;
-        sh.f1 = f1;
-        sh.f2 = f2;
-        sh.dtm = -f1 / f2;
-        sh.tsum = 0.0;
-        sh.nbreak = nbreak;
-        sh.bkmin = bk;
-        sh.need_walk = (nbreak > 0 && !(sh.dtm < bk)) ? 1 : 0;
-        sh.to999 = 0;
+        if (t == 0) {
+            sh.f2_org = f2_org;
+            sh.info = info;
+            sh.f1 = f1;
+            sh.f2 = f2;
+            sh.dtm = -f1 / f2;
+            sh.tsum = 0.0;
+            sh.nbreak = nbreak;
+            sh.bkmin = bk;
+            sh.need_walk = (nbreak > 0 && !(-f1 / f2 < bk)) ? 1 : 0;
+            sh.to999 = 0;
+        }
     }
     LB_SYNC();
     if (sh.info) return sh.info;
     if (sh.need_walk) {
         sort_breakpoints(c);
-        if (t == 0) {
+        if (t < LB_WARP) {
+            const int l = lane_id();
             const bool bnded = unbnded == 0;
-            int nleft = nbreak, it = 0, info = 0;
+            int nleft = nbreak, it = 0, info = 0, to999 = 0;
             double tj = 0.0, f1w = sh.f1, f2w = sh.f2, dtm = sh.dtm, tsum = 0.0;
+            const double f2_org = sh.f2_org;
             while (true) {
                 const double tj0 = tj;
                 tj = c.key[it];
@@ -533,42 +628,39 @@ LB_FN int cauchy(Ctx& c) {
                 --nleft;
                 ++it;
                 const double dibp = A.d[ibp];
-                A.d[ibp] = 0.0;
-                double zibp;
-                if (dibp > 0.0) {
-                    zibp = P.hi[ibp] - A.x[ibp];
-                    A.z[ibp] = P.hi[ibp];
-                    A.iwhere[ibp] = 2;
-                } else {
-                    zibp = P.lo[ibp] - A.x[ibp];
-                    A.z[ibp] = P.lo[ibp];
-                    A.iwhere[ibp] = 1;
+                const double zibp = (dibp > 0.0 ? P.hi[ibp] : P.lo[ibp]) - A.x[ibp];
+                LB_SYNCWARP();
+                if (l == 0) {
+                    A.d[ibp] = 0.0;
+                    A.z[ibp] = dibp > 0.0 ? P.hi[ibp] : P.lo[ibp];
+                    A.iwhere[ibp] = dibp > 0.0 ? 2 : 1;
                 }
                 if (nleft == 0 && nbreak == n) {
                     dtm = dt;
-                    sh.to999 = 1;
+                    to999 = 1;
                     break;
                 }
                 const double dibp2 = dibp * dibp;
                 f1w = f1w + dt * f2w + dibp2 - theta * dibp * zibp;
                 f2w = f2w - theta * dibp2;
                 if (col > 0) {
-                    for (int j = 0; j < col2; ++j) sh.c[j] += dt * sh.p[j];
-                    for (int j = 0; j < col; ++j) {
-                        const size_t pj = (size_t)colptr(s, m, j) * n;
-                        sh.wbp[j] = A.wy[pj + ibp];
-                        sh.wbp[col + j] = theta * A.ws[pj + ibp];
+                    for (int j = l; j < col2; j += LB_WARP) {
+                        sh.c[j] += dt * sh.p[j];
+                        const size_t pj = (size_t)colptr(s, m, j < col ? j : j - col) * n;
+                        sh.wbp[j] = j < col ? A.wy[pj + ibp] : theta * A.ws[pj + ibp];
                     }
+                    LB_SYNCWARP();
                     info = middle_times(sh, m, col, sh.wbp, sh.v);
                     if (info) break;
-                    const double wmc = dot_small(sh.c, sh.v, col2);
-                    const double wmp = dot_small(sh.p, sh.v, col2);
-                    const double wmw = dot_small(sh.wbp, sh.v, col2);
-                    for (int j = 0; j < col2; ++j) sh.p[j] -= dibp * sh.wbp[j];
+                    const double wmc = warp_dot(sh.c, sh.v, col2);
+                    const double wmp = warp_dot(sh.p, sh.v, col2);
+                    const double wmw = warp_dot(sh.wbp, sh.v, col2);
+                    for (int j = l; j < col2; j += LB_WARP) sh.p[j] -= dibp * sh.wbp[j];
+                    LB_SYNCWARP();
                     f1w += dibp * wmc;
                     f2w += 2.0 * dibp * wmp - dibp2 * wmw;
                 }
-                f2w = fmax(kEpsMch * sh.f2_org, f2w);
+                f2w = fmax(kEpsMch * f2_org, f2w);
                 if (nleft > 0) {
                     dtm = -f1w / f2w;
                     continue;
@@ -581,9 +673,12 @@ LB_FN int cauchy(Ctx& c) {
                 }
                 break;
             }
-            sh.info = info;
-            sh.dtm = dtm;
-            sh.tsum = tsum;
+            if (l == 0) {
+                sh.info = info;
+                sh.dtm = dtm;
+                sh.tsum = tsum;
+                sh.to999 = to999;
+            }
         }
         LB_SYNC();
         if (sh.info) return sh.info;
@@ -640,35 +735,39 @@ LB_FN int form_k(Ctx& c) {
     const int n = P.n, m = P.m, col = s.col, ld = 2 * P.m;
     const int J1 = col * (col + 1) / 2;
     const int J = 2 * J1 + col * col;
-    warp_dots(J, n, A.iwhere,
-              [&](int o, const double*& a, const double*& b, int& mode) {
-                  int i, j;
-                  if (o < 2 * J1) {  // lower triangles of Y^T Z Z^T Y, then S^T A A^T S
-                      const int oo = o < J1 ? o : o - J1;
-                      i = 0;
-                      while ((i + 1) * (i + 2) / 2 <= oo) ++i;
-                      j = oo - i * (i + 1) / 2;
-                      const double* w = o < J1 ? A.wy : A.ws;
-                      a = w + (size_t)colptr(s, m, i) * n;
-                      b = w + (size_t)colptr(s, m, j) * n;
-                      mode = o < J1 ? 1 : 2;
-                  } else {  // S^T Y split: active below the diagonal, free on and above
-                      const int oo = o - 2 * J1;
-                      i = oo / col;
-                      j = oo % col;
-                      a = A.ws + (size_t)colptr(s, m, i) * n;
-                      b = A.wy + (size_t)colptr(s, m, j) * n;
-                      mode = i > j ? 2 : 1;
-                  }
-              },
-              sh.dots);
-    if (lb_tid() == 0) {
+    // staged columns: Y (logical order) then S
+    tiled_gram(J, n, 2 * col,
+               [&](int q) {
+                   return (q < col ? A.wy : A.ws) + (size_t)colptr(s, m, q < col ? q : q - col) * n;
+               },
+               A.iwhere,
+               [&](int o, int& a, int& b, int& mode) {
+                   if (o < 2 * J1) {  // lower triangles of Y^T Z Z^T Y, then S^T A A^T S
+                       const int oo = o < J1 ? o : o - J1;
+                       int i = 0;
+                       while ((i + 1) * (i + 2) / 2 <= oo) ++i;
+                       const int j = oo - i * (i + 1) / 2;
+                       const int base = o < J1 ? 0 : col;
+                       a = base + i;
+                       b = base + j;
+                       mode = o < J1 ? 1 : 2;
+                   } else {  // S^T Y split: active below the diagonal, free on and above
+                       const int oo = o - 2 * J1;
+                       const int i = oo / col, j = oo % col;
+                       a = col + i;
+                       b = j;
+                       mode = i > j ? 2 : 1;
+                   }
+               },
+               c.tile, c.tmask, sh.dots);
+    if (lb_tid() < LB_WARP) {
+        const int l = lane_id();
         const double theta = s.theta;
         double* wn = sh.wn;
         const double* yzy = sh.dots;
         const double* sas = sh.dots + J1;
         const double* sym = sh.dots + 2 * J1;
-        for (int iy = 0; iy < col; ++iy) {
+        for (int iy = l; iy < col; iy += LB_WARP) {
             const int is = col + iy;
             for (int jy = 0; jy <= iy; ++jy) {
                 const int js = col + jy;
@@ -679,15 +778,24 @@ LB_FN int form_k(Ctx& c) {
             for (int jy = iy; jy < col; ++jy) wn[jy + is * ld] = sym[iy * col + jy];
             wn[iy + iy * ld] += sh.sy[iy + iy * m];
         }
-        int info = chol_upper(wn, ld, col) ? -1 : 0;
+        LB_SYNCWARP();
+        int info = warp_chol_upper(wn, ld, col, sh.rd) ? -1 : 0;
         if (!info) {
-            for (int js = col; js < 2 * col; ++js) solve_upper_t(wn, ld, col, wn + js * ld);
-            for (int is = col; is < 2 * col; ++is)
-                for (int js = is; js < 2 * col; ++js)
-                    wn[is + js * ld] += dot_small(wn + is * ld, wn + js * ld, col);
-            if (chol_upper(wn + col + col * ld, ld, col)) info = -2;
+            warp_solve_upper_t_multi(wn, ld, col, sh.rd, wn + col * ld, ld, col);
+            const int ne = col * (col + 1) / 2;
+            for (int e = l; e < ne; e += LB_WARP) {
+                int jj = 0;
+                while ((jj + 1) * (jj + 2) / 2 <= e) ++jj;
+                const int ii = e - jj * (jj + 1) / 2;
+                const int is = col + ii, js = col + jj;
+                double acc = 0.0;
+                for (int k = 0; k < col; ++k) acc += wn[k + is * ld] * wn[k + js * ld];
+                wn[is + js * ld] += acc;
+            }
+            LB_SYNCWARP();
+            if (warp_chol_upper(wn + col + col * ld, ld, col, sh.rd + col)) info = -2;
         }
-        sh.info = info;
+        if (l == 0) sh.info = info;
     }
     LB_SYNC();
     return sh.info;
@@ -705,7 +813,10 @@ LB_FN int reduced_gradient(Ctx& c) {
         LB_SYNC();
         return 0;
     }
-    if (lb_tid() == 0) sh.info = middle_times(sh, m, col, sh.c, sh.v) ? -8 : 0;
+    if (lb_tid() < LB_WARP) {
+        const int info = middle_times(sh, m, col, sh.c, sh.v) ? -8 : 0;
+        if (lb_tid() == 0) sh.info = info;
+    }
     LB_SYNC();
     if (sh.info) return sh.info;
     const double theta = s.theta;
@@ -744,14 +855,16 @@ LB_FN int subspace_min(Ctx& c) {
                   mode = 0;
               },
               sh.wv);
-    if (t == 0) {
-        for (int j = 0; j < col; ++j) sh.wv[col + j] *= theta;
-        int info = solve_upper_t(sh.wn, ld, col2, sh.wv);
+    if (t < LB_WARP) {
+        for (int j = lane_id(); j < col; j += LB_WARP) sh.wv[col + j] *= theta;
+        const int info = warp_rdiag(sh.wn, ld, col2, sh.rd);
         if (!info) {
-            for (int j = 0; j < col; ++j) sh.wv[j] = -sh.wv[j];
-            info = solve_upper(sh.wn, ld, col2, sh.wv);
+            warp_solve_upper_t(sh.wn, ld, col2, sh.rd, sh.wv);
+            for (int j = lane_id(); j < col; j += LB_WARP) sh.wv[j] = -sh.wv[j];
+            LB_SYNCWARP();
+            warp_solve_upper(sh.wn, ld, col2, sh.rd, sh.wv);
         }
-        sh.info = info;
+        if (t == 0) sh.info = info;
     }
     LB_SYNC();
     if (sh.info) return sh.info;
@@ -1255,25 +1368,33 @@ LB_FN int new_x(Ctx& c) {
                   mode = 0;
               },
               sh.dots);
-    if (t == 0) {
-        for (int j = 0; j < col - 1; ++j) {
+    if (t < LB_WARP) {
+        const int l = lane_id();
+        for (int j = l; j < col - 1; j += LB_WARP) {
             sh.sy[(col - 1) + j * m] = sh.dots[j];
             sh.ss[j + (col - 1) * m] = sh.dots[col - 1 + j];
         }
-        sh.ss[(col - 1) + (col - 1) * m] = stp == 1.0 ? s.dtd : stp * stp * s.dtd;
-        sh.sy[(col - 1) + (col - 1) * m] = sh.dr;
+        if (l == 0) {
+            sh.ss[(col - 1) + (col - 1) * m] = stp == 1.0 ? s.dtd : stp * stp * s.dtd;
+            sh.sy[(col - 1) + (col - 1) * m] = sh.dr;
+        }
+        LB_SYNCWARP();
+        for (int i = l; i < col; i += LB_WARP) sh.dinv[i] = 1.0 / sh.sy[i + i * m];
+        LB_SYNCWARP();
         // T = theta S^T S + L D^-1 L^T (upper), then its Cholesky factor
         const double theta = s.theta;
-        for (int j = 0; j < col; ++j) sh.wt[0 + j * m] = theta * sh.ss[0 + j * m];
-        for (int i = 1; i < col; ++i) {
-            for (int j = i; j < col; ++j) {
-                const int k1 = (i < j ? i : j);
-                double acc = 0.0;
-                for (int k = 0; k < k1; ++k) acc += sh.sy[i + k * m] * sh.sy[j + k * m] / sh.sy[k + k * m];
-                sh.wt[i + j * m] = acc + theta * sh.ss[i + j * m];
-            }
+        const int ne = col * (col + 1) / 2;
+        for (int e = l; e < ne; e += LB_WARP) {
+            int jj = 0;
+            while ((jj + 1) * (jj + 2) / 2 <= e) ++jj;
+            const int ii = e - jj * (jj + 1) / 2;
+            double acc = 0.0;
+            for (int k = 0; k < ii; ++k) acc += sh.sy[ii + k * m] * sh.sy[jj + k * m] * sh.dinv[k];
+            sh.wt[ii + jj * m] = acc + theta * sh.ss[ii + jj * m];
         }
-        if (chol_upper(sh.wt, m, col)) reset_memory(s);
+        LB_SYNCWARP();
+        const int info = warp_chol_upper(sh.wt, m, col, sh.rd);
+        if (l == 0 && info) reset_memory(s);
     }
     LB_SYNC();
     return kLIter;
@@ -1347,6 +1468,13 @@ inline int sort_len(int n) {
     int n2 = 1;
     while (n2 < n) n2 <<= 1;
     return n2;
+}
+
+// Dynamic shared memory of a step: sort keys (n2 doubles) and indices (n2 ints),
+// then the Gram tile and its row flags.
+LB_HD long long tile_offset(int n2) { return (12LL * n2 + 15) / 16 * 16; }
+inline long long step_dyn_bytes(int n2) {
+    return tile_offset(n2) + 8LL * (kTileRows + 1) * kTileCols + kTileRows;
 }
 
 struct InitArgs {
@@ -1445,7 +1573,11 @@ LB_FN void init_restart(const InitArgs& a, int r, Shm& sh) {
 }
 
 // Restart r: consume f and g, advance to the next request or stop.
-LB_FN void step_restart(const StepArgs& a, int r, Shm& sh, double* key, int* idx, int n2) {
+LB_FN void step_restart(const StepArgs& a, int r, Shm& sh, unsigned char* dyn, int n2) {
+    double* key = reinterpret_cast<double*>(dyn);
+    int* idx = reinterpret_cast<int*>(dyn + 8LL * n2);
+    double* tile = reinterpret_cast<double*>(dyn + tile_offset(n2));
+    int8_t* tmask = reinterpret_cast<int8_t*>(tile + (kTileRows + 1) * kTileCols);
     const int n = a.n, m = a.m, t = lb_tid();
     State* st = reinterpret_cast<State*>(a.ws + a.L.states) + r;
     if (t == 0) sh.s = *st;
@@ -1478,6 +1610,8 @@ LB_FN void step_restart(const StepArgs& a, int r, Shm& sh, double* key, int* idx
     c.key = key;
     c.idx = idx;
     c.n2 = n2;
+    c.tile = tile;
+    c.tmask = tmask;
     for (int i = t; i < m * m; i += LB_NT) {
         sh.sy[i] = c.A.sy[i];
         sh.ss[i] = c.A.ss[i];

@@ -50,10 +50,10 @@ void emu_step(long long R, int n, int m, int maxls, long long maxiter, long long
     a.status = status;
     a.ignore_status = ignore_status;
     const int n2 = sort_len(n);
-    std::vector<double> key(n2);
-    std::vector<int> idx(n2);
+    std::vector<double> dyn((step_dyn_bytes(n2) + 7) / 8);
     std::vector<Shm> sh(1);
-    for (long long r = 0; r < R; ++r) step_restart(a, (int)r, sh[0], key.data(), idx.data(), n2);
+    for (long long r = 0; r < R; ++r)
+        step_restart(a, (int)r, sh[0], reinterpret_cast<unsigned char*>(dyn.data()), n2);
     if (summary) summarize(a.L, ws, R, sh[0], summary);
 }
 
