@@ -542,8 +542,12 @@ def run_optimize(args) -> None:
     torch.cuda.synchronize(device)
     init_s = time.perf_counter() - t0
     bounds = torch.stack([torch.zeros(d), torch.ones(d)]).double()
-    # warm-up of the shapes used below (library set-up, graph capture)
-    evaluate_raw(acqf, draw_sobol_samples(bounds, 4096, q, seed=1), 4096)
+    # warm-up of the shapes and torch kernels used below (library set-up, graph
+    # capture, the first use of torch's sampling kernels)
+    Xr_w = draw_sobol_samples(bounds, 4096, q, seed=1)
+    vr_w = evaluate_raw(acqf, Xr_w, 4096)
+    initialize_q_batch(Xr_w.to(device), vr_w, restarts, eta=1.0,
+                       generator=torch.Generator(device=device).manual_seed(1))
     Xw = torch.rand(restarts, q, d, dtype=torch.float64, device=device)
     acqf.graphed_value_and_grad(Xw, True)
     gen_candidates_scipy(Xw, acqf, 0.0, 1.0, {"maxiter": 2})
