@@ -199,6 +199,41 @@ def lib():
     return handle
 
 
+_ops = None
+
+
+def ext_path() -> Path:
+    return _LIB_PATH.parent / "libbotorch_gb300_torch.so"
+
+
+def ops():
+    """Load (once) the thin torch extension over the library and return its
+    operators, ``torch.ops.botorch_gb300``: the acquisition's value (+ adjoint)
+    call and the fused log-areas contract run through the dispatcher; raise if
+    the extension is unavailable."""
+    global _ops
+    if _ops is not None:
+        return _ops
+    lib()  # the extension links against the library
+    path = ext_path()
+    if not path.exists():
+        raise NativeLibraryError(
+            f"{path} is missing: build it with `python -m botorch_gb300.build` "
+            "(botorch_gb300 has no CPU fallback).")
+    try:
+        torch.ops.load_library(str(path))
+    except OSError as e:  # pragma: no cover - depends on the machine
+        raise NativeLibraryError(f"cannot load {path}: {e}") from e
+    _ops = torch.ops.botorch_gb300
+    return _ops
+
+
+def struct_bytes(s: ctypes.Structure) -> torch.Tensor:
+    """The bytes of a ctypes struct as a CPU uint8 tensor sharing its memory (the
+    form in which the torch operators take a bgb_acq_t)."""
+    return torch.frombuffer(s, dtype=torch.uint8)
+
+
 def ptr(t: torch.Tensor | None) -> int | None:
     if t is None:
         return None
@@ -231,7 +266,11 @@ class Workspace:
         self.buf: torch.Tensor | None = None
 
     def get(self, nbytes: int) -> tuple[int, int]:
+        t = self.tensor(nbytes)
+        return t.data_ptr(), t.numel()
+
+    def tensor(self, nbytes: int) -> torch.Tensor:
         nbytes = max(int(nbytes), 256)
         if self.buf is None or self.buf.numel() < nbytes:
             self.buf = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
-        return self.buf.data_ptr(), self.buf.numel()
+        return self.buf

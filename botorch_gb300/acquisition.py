@@ -163,14 +163,12 @@ class _MCAcquisition:
             value, grad, status = out
         if b not in ws_bytes:
             ws_bytes[b] = lib.bgb_acq_workspace_bytes(ctypes.byref(acq), b)
-        wp, wb = (ws or self._ws).get(ws_bytes[b])
-        stream = nat.stream_handle(self.device)
+        wt = (ws or self._ws).tensor(ws_bytes[b])
+        packed = nat.struct_bytes(acq)
         if need_grad:
-            rc = lib.bgb_acq_forward_backward(ctypes.byref(acq), nat.ptr(Xd), b, nat.ptr(value),
-                                              nat.ptr(grad), nat.ptr(status), wp, wb, stream)
+            rc = nat.ops().acq_forward_backward(packed, Xd, value, grad, status, wt)
         else:
-            rc = lib.bgb_acq_forward(ctypes.byref(acq), nat.ptr(Xd), b, nat.ptr(value),
-                                     nat.ptr(status), wp, wb, stream)
+            rc = nat.ops().acq_forward(packed, Xd, value, status, wt)
         nat.check(rc, type(self).__name__)
         return value, grad, status
 

@@ -13,7 +13,10 @@ autograd function (logei.py:107-165).
         -> gradient w.r.t. obj_subsets, (B, n_sub, i, m)
 
 float64 and float32 inputs compute in their own type, as the reference's
-AT_DISPATCH_FLOATING_TYPES. There is no CPU path: CPU tensors raise.
+AT_DISPATCH_FLOATING_TYPES. ``forward`` and ``backward`` run through the
+library's torch operators (``torch.ops.botorch_gb300.log_areas_forward`` /
+``log_areas_backward``, registered for CUDA only). There is no CPU path: CPU
+tensors raise.
 
 ``FusedLogAreas`` differs from the reference in one respect: when the input
 needs a gradient and the Jacobian fits ``JACOBIAN_BUDGET_BYTES``, its forward
@@ -64,14 +67,8 @@ def _prepare(obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor):
 def forward(obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor, tau_relu: float,
             tau_max: float) -> Tensor:
     """Log areas (B, nc, n_sub) of every cell and q-subset (logei_fused.cpp:184-264)."""
-    obj, cl, cu, (B, n_sub, isz, m, B_cells, nc) = _prepare(obj_subsets, cell_lower, cell_upper)
-    out = torch.empty(B, nc, n_sub, dtype=obj.dtype, device=obj.device)
-    fn = nat.lib().bgb_log_areas_forward if obj.dtype == torch.float64 else nat.lib().bgb_log_areas_forward_f32
-    with torch.cuda.device(obj.device):
-        rc = fn(obj.data_ptr(), B, n_sub, isz, m, cl.data_ptr(), cu.data_ptr(), B_cells, nc,
-                float(tau_relu), float(tau_max), out.data_ptr(), nat.stream_handle(obj.device))
-    nat.check(rc, "bgb_log_areas_forward")
-    return out
+    obj, cl, cu, _ = _prepare(obj_subsets, cell_lower, cell_upper)
+    return nat.ops().log_areas_forward(obj, cl, cu, float(tau_relu), float(tau_max))
 
 
 def backward(grad_output: Tensor, obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor,
@@ -81,15 +78,7 @@ def backward(grad_output: Tensor, obj_subsets: Tensor, cell_lower: Tensor, cell_
     go = grad_output.contiguous()
     if tuple(go.shape) != (B, nc, n_sub) or go.dtype != obj.dtype or go.device != obj.device:
         raise RuntimeError("fused log-areas: grad_output must be (B, num_cells, n_sub) like the forward output")
-    g_obj = torch.empty_like(obj)
-    fn = (nat.lib().bgb_log_areas_backward if obj.dtype == torch.float64
-          else nat.lib().bgb_log_areas_backward_f32)
-    with torch.cuda.device(obj.device):
-        rc = fn(go.data_ptr(), obj.data_ptr(), B, n_sub, isz, m, cl.data_ptr(), cu.data_ptr(),
-                B_cells, nc, float(tau_relu), float(tau_max), g_obj.data_ptr(),
-                nat.stream_handle(obj.device))
-    nat.check(rc, "bgb_log_areas_backward")
-    return g_obj
+    return nat.ops().log_areas_backward(go, obj, cl, cu, float(tau_relu), float(tau_max))
 
 
 def forward_with_jacobian(obj_subsets: Tensor, cell_lower: Tensor, cell_upper: Tensor, tau_relu: float,

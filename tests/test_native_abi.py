@@ -138,3 +138,26 @@ def test_lbfgsb_options_layout_and_queries(tmp_path):
         _native.BGB_ERR_ARG
     assert lib.bgb_lbfgsb_init(ctypes.byref(opts), None, 1, 1, 1, wsb, None) == _native.BGB_ERR_ARG
     assert lib.bgb_lbfgsb_init(ctypes.byref(opts), 1, 1, 1, 1, wsb - 1, None) == _native.BGB_ERR_WORKSPACE
+
+
+def test_torch_extension_registers_the_operators():
+    """The thin torch extension loads and registers the hot path's operators with
+    their schemas; with no CPU kernel registered, CPU tensors raise in the dispatcher."""
+    import torch
+
+    if not _native.ext_path().exists():
+        from botorch_gb300.build import build
+        build()
+    ops = _native.ops()
+    schemas = {n: str(getattr(ops, n).default._schema) for n in
+               ("acq_forward_backward", "acq_forward", "log_areas_forward", "log_areas_backward")}
+    assert schemas["acq_forward_backward"].startswith("botorch_gb300::acq_forward_backward(Tensor acq, Tensor X, "
+                                                      "Tensor(a!) value, Tensor(b!) grad, Tensor(c!) status")
+    assert schemas["log_areas_forward"] == ("botorch_gb300::log_areas_forward(Tensor obj_subsets, Tensor cell_lower, "
+                                            "Tensor cell_upper, float tau_relu, float tau_max) -> Tensor")
+    assert "-> Tensor" in schemas["log_areas_backward"] and "-> int" in schemas["acq_forward"]
+    with pytest.raises(NotImplementedError):
+        ops.log_areas_forward(torch.zeros(1, 1, 1, 1), torch.zeros(1, 1), torch.ones(1, 1), 1e-6, 1e-2)
+    acq = _native.BgbAcq(q=2)
+    packed = _native.struct_bytes(acq)
+    assert packed.numel() == ctypes.sizeof(_native.BgbAcq) and int(packed[ctypes.sizeof(_native.BgbGP) + 8]) == 2
