@@ -112,7 +112,15 @@ Cells prepare(const at::Tensor& obj_subsets, const at::Tensor& cell_lower, const
     return c;
 }
 
-void check_rc(int rc, const char* what) { TORCH_CHECK(rc == BGB_OK, what, " failed with code ", rc); }
+// The C ABI's argument and launch errors, named as the Python layer names them.
+void check_rc(int rc, const char* what) {
+    const char* name = rc == BGB_ERR_ARG           ? "invalid argument"
+                       : rc == BGB_ERR_WORKSPACE   ? "workspace too small"
+                       : rc == BGB_ERR_CUDA        ? "CUDA error"
+                       : rc == BGB_ERR_UNSUPPORTED ? "unsupported size"
+                                                   : "error";
+    TORCH_CHECK(rc == BGB_OK, what, ": ", name, " (code ", rc, ")");
+}
 
 at::Tensor log_areas_forward(const at::Tensor& obj_subsets, const at::Tensor& cell_lower,
                              const at::Tensor& cell_upper, double tau_relu, double tau_max) {
