@@ -559,6 +559,21 @@ def run_optimize(args) -> None:
     t2 = time.perf_counter()
     X0, _ = initialize_q_batch(X_raw.to(device), v_raw, restarts, eta=1.0,
                                generator=torch.Generator(device=device).manual_seed(0))
+    if args.profile:  # one round (evaluation + device L-BFGS-B step) inside the profiler range
+        from botorch_gb300.lbfgsb import DeviceLbfgsb
+
+        Xr = X0.reshape(restarts, q * d).contiguous().clone()
+        lb = DeviceLbfgsb(Xr, torch.zeros(q * d), torch.ones(q * d), maxiter=args.maxiter)
+        for r in range(args.warmup + 1):
+            if r == args.warmup:
+                torch.cuda.synchronize(device)
+                torch.cuda.profiler.start()
+            v, g = acqf.value_and_grad_raw(Xr.view(restarts, q, d), True, check=False)
+            lb.step(v, g, sign=-1.0)
+        torch.cuda.synchronize(device)
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_rounds": 1, "after_rounds": args.warmup, "summary": lb.summary.tolist()}))
+        return
     # the default (the reference's): each restart its own L-BFGS-B, one batched
     # evaluation per round
     X, v = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": args.maxiter})

@@ -1009,6 +1009,7 @@ __global__ void __launch_bounds__(128) batch_step_kernel(QBatchArgs a, int backw
 // storing it, and accumulates d[bl, br] = sum_s dY_s z_s^T per chunk of samples
 // (float32 within a chunk, float64 across chunks).
 constexpr int kBsThreads = 64;
+constexpr int kBsThreadsFew = 256;
 constexpr int kDyLd = kSampleChunk + 1;  // row stride of the reverse-pass dY tile
 
 __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
@@ -1085,11 +1086,11 @@ __device__ int psd_chol_warp(double* M, double* scr, int q, int max_tries, doubl
     return BGB_NOT_PSD;
 }
 
-template <int QMAX>
+template <int QMAX, int NT>
 __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int backward,
                                                     int64_t bidx_) {
     extern __shared__ double smd[];
-    constexpr int NW = kBsThreads / 32;
+    constexpr int NW = NT / 32;
     const int q = a.q, r = a.r, S = a.S, D = r + q;
     const int64_t bidx = bidx_;
     const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
@@ -1114,9 +1115,9 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
             a.value[bidx] = NAN;
         }
         if (backward && status != BGB_DEVICE_TIMEOUT) {
-            for (int p = tid; p < q * q; p += kBsThreads) a.gqq[bidx * q * q + p] = 0.0;
-            for (int p = tid; p < q * r; p += kBsThreads) a.gqb[bidx * q * r + p] = 0.0;
-            for (int p = tid; p < q; p += kBsThreads) a.gmu[bidx * q + p] = 0.0;
+            for (int p = tid; p < q * q; p += NT) a.gqq[bidx * q * q + p] = 0.0;
+            for (int p = tid; p < q * r; p += NT) a.gqb[bidx * q * r + p] = 0.0;
+            for (int p = tid; p < q; p += NT) a.gmu[bidx * q + p] = 0.0;
         }
     };
     if (tid == 0) s_status = (a.dev_err != nullptr && *a.dev_err != 0) ? BGB_DEVICE_TIMEOUT : 0;
@@ -1126,13 +1127,13 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
         return;
     }
     // (1) untransformed mean as a float pair, covariance blocks
-    for (int i = tid; i < QMAX; i += kBsThreads) {
+    for (int i = tid; i < QMAX; i += NT) {
         const double mu = (i < q) ? a.y_mean + sy * a.mu[bidx * q + i] : 0.0;
         const float h = (float)mu;
         s_muh[i] = h;
         s_mul[i] = (float)(mu - (double)h);
     }
-    for (int p = tid; p < q * q; p += kBsThreads) M[p] = sy2 * a.sig[bidx * q * q + p];
+    for (int p = tid; p < q * q; p += NT) M[p] = sy2 * a.sig[bidx * q * q + p];
     __syncthreads();
     // (2)-(4) the q new rows [bl, br] of the Cholesky factor of the joint covariance:
     // cached root (joint == 0) or joint sampling level by level, as in the float64 step
@@ -1146,13 +1147,13 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
             Lbi = a.Lb_inv_lv + (int64_t)lv * r * r;
             if (r > 0 && isnan(Lbi[0])) continue;  // chol(Sigma_bb + j_t I) failed at this level
             if (lv > 0) {  // M holds the previous level's attempt
-                for (int p = tid; p < q * q; p += kBsThreads) M[p] = sy2 * a.sig[bidx * q * q + p];
+                for (int p = tid; p < q * q; p += NT) M[p] = sy2 * a.sig[bidx * q * q + p];
                 __syncthreads();
             }
         }
         const double jit = (a.joint && lv > 0) ? a.jitter * pow(10.0, (double)(lv - 1)) : 0.0;
         // (2) bl = Sigma_qb Lb^-T (Lb^-1 lower triangular)
-        for (int p = tid; p < q * r; p += kBsThreads) {
+        for (int p = tid; p < q * r; p += NT) {
             const int i = p / r, k = p % r;
             double acc = 0.0;
             for (int kk = 0; kk <= k; ++kk) acc += sy2 * a.sqb[(bidx * q + i) * r + kk] * Lbi[k * r + kk];
@@ -1160,7 +1161,7 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
         }
         __syncthreads();
         // (3) M = Sigma_qq (+ j_t I) - bl bl^T
-        for (int p = tid; p < q * q; p += kBsThreads) {
+        for (int p = tid; p < q * q; p += NT) {
             const int i = p / q, j = p % q;
             double acc = 0.0;
             for (int k = 0; k < r; ++k) acc += Lq[i * D + k] * Lq[j * D + k];
@@ -1192,7 +1193,7 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
         return;
     }
     if (a.joint) Lbi = a.Lb_inv_lv + (int64_t)s_lv * r * r;
-    for (int p = tid; p < D * QMAX; p += kBsThreads) {
+    for (int p = tid; p < D * QMAX; p += NT) {
         const int k = p / QMAX, i = p % QMAX;
         Lf[p] = (i < q) ? (float)Lq[i * D + k] : 0.f;
     }
@@ -1206,7 +1207,7 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
     const float* __restrict__ bf32 = a.joint == 2 ? a.bf32 + 2 * (int64_t)s_lv * S : a.bf32;
     // (5) forward: t_s per sample
     int local_bad = 0;
-    for (int s = tid; s < S; s += kBsThreads) {
+    for (int s = tid; s < S; s += NT) {
         float u[QMAX];
         sample_u<QMAX>(Lf, z32 + (int64_t)s * D, q, D, s_muh, s_mul, bf32[2 * s], bf32[2 * s + 1], u);
         float Mx = -INFINITY, li[QMAX];
@@ -1238,7 +1239,7 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
     }
     // (6) reduction over samples: qEI mean, qLogNEI log-mean-exp (inf handling as the reference)
     float mx = -INFINITY;
-    for (int s = tid; s < S; s += kBsThreads) mx = fmaxf(mx, tS[s]);
+    for (int s = tid; s < S; s += NT) mx = fmaxf(mx, tS[s]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) s_redf[warp] = mx;
@@ -1246,12 +1247,13 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
     mx = s_redf[0];
 #pragma unroll
     for (int w = 1; w < NW; ++w) mx = fmaxf(mx, s_redf[w]);
-    float part = 0.f;
-    for (int s = tid; s < S; s += kBsThreads) {
-        if (qei) part += tS[s];
-        else if (!isinf(mx)) part += __expf(tS[s] - mx);
+    // per-thread partial sums in float64, so that the value does not depend on
+    // how the samples are dealt to the threads beyond float64 rounding
+    double acc = 0.0;
+    for (int s = tid; s < S; s += NT) {
+        if (qei) acc += (double)tS[s];
+        else if (!isinf(mx)) acc += (double)__expf(tS[s] - mx);
     }
-    double acc = (double)part;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) s_red[warp] = acc;
@@ -1275,15 +1277,15 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
         s_lse = lse;
     }
     if (!backward) return;
-    for (int p = tid; p < q * D; p += kBsThreads) dLq[p] = 0.0;
-    for (int i = tid; i < QMAX; i += kBsThreads) s_dmu[i] = 0.0;
+    for (int p = tid; p < q * D; p += NT) dLq[p] = 0.0;
+    for (int i = tid; i < QMAX; i += NT) s_dmu[i] = 0.0;
     __syncthreads();
     const float lse_f = (float)s_lse;
     const bool inf_mx = isinf(mx);
     // (7) reverse through the sample reduction and the sample step, a chunk of samples at a time
     for (int s0 = 0; s0 < S; s0 += kSampleChunk) {
         const int sc = min(kSampleChunk, S - s0);
-        for (int ls = tid; ls < sc; ls += kBsThreads) {
+        for (int ls = tid; ls < sc; ls += NT) {
             const int s = s0 + ls;
             float u[QMAX], li[QMAX], dli[QMAX], g[QMAX];
             sample_u<QMAX>(Lf, z32 + (int64_t)s * D, q, D, s_muh, s_mul, bf32[2 * s], bf32[2 * s + 1], u);
@@ -1334,7 +1336,7 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
                 if (i < q) dY[i * kDyLd + ls] = g[i];  // point-major, padded: no bank conflicts
         }
         __syncthreads();
-        for (int p = tid; p < q * D; p += kBsThreads) {
+        for (int p = tid; p < q * D; p += NT) {
             const int i = p / D, k = p % D;
             if (k >= r + i + 1) continue;  // the upper part of br stays zero
             float cs = 0.f;
@@ -1342,7 +1344,7 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
             for (int ls = 0; ls < sc; ++ls) cs = fmaf(dyi[ls], z32[(int64_t)(s0 + ls) * D + k], cs);
             dLq[p] += (double)cs;
         }
-        for (int i = tid; i < q; i += kBsThreads) {
+        for (int i = tid; i < q; i += NT) {
             float cs = 0.f;
             const float* dyi = dY + i * kDyLd;
             for (int ls = 0; ls < sc; ++ls) cs += dyi[ls];
@@ -1388,29 +1390,29 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
     }
     __syncthreads();
     // (9) d bl += -2 gA bl;  dSigma_qb = d bl Lb^-1;  seeds in standardised units
-    for (int p = tid; p < q * r; p += kBsThreads) {
+    for (int p = tid; p < q * r; p += NT) {
         const int i = p / r, k = p % r;
         double acc2 = dLq[i * D + k];
         for (int j = 0; j < q; ++j) acc2 -= 2.0 * gA[i * q + j] * Lq[j * D + k];
         scr[p] = acc2;
     }
     __syncthreads();
-    for (int p = tid; p < q * r; p += kBsThreads) dLq[(p / r) * D + (p % r)] = scr[p];
+    for (int p = tid; p < q * r; p += NT) dLq[(p / r) * D + (p % r)] = scr[p];
     __syncthreads();
-    for (int p = tid; p < q * r; p += kBsThreads) {
+    for (int p = tid; p < q * r; p += NT) {
         const int i = p / r, kp = p % r;
         double acc2 = 0.0;
         for (int k = kp; k < r; ++k) acc2 += dLq[i * D + k] * Lbi[k * r + kp];
         a.gqb[(bidx * q + i) * r + kp] = sy2 * acc2;
     }
-    for (int p = tid; p < q * q; p += kBsThreads) a.gqq[bidx * q * q + p] = sy2 * gA[p];
-    for (int i = tid; i < q; i += kBsThreads) a.gmu[bidx * q + i] = sy * s_dmu[i];
+    for (int p = tid; p < q * q; p += NT) a.gqq[bidx * q * q + p] = sy2 * gA[p];
+    for (int i = tid; i < q; i += NT) a.gmu[bidx * q + i] = sy * s_dmu[i];
     if (a.hmul == nullptr) return;
     // power-of-two row scales of H = gmu beta^T - 2 Gqq V - Gqb Vb for its float16
     // split, from |H[i,c]| <= |gmu_i| max|beta| + sqrt(outputscale) (sum_j 2|Gqq_ij| +
     // sum_k |Gqb_ik|) (rows of V and Vb have 2-norm <= sqrt(outputscale))
     __syncthreads();
-    for (int i = tid; i < q; i += kBsThreads) {
+    for (int i = tid; i < q; i += NT) {
         double sv = 0.0;
         for (int j = 0; j < q; ++j) sv += 2.0 * fabs(a.gqq[(bidx * q + i) * q + j]);
         for (int k = 0; k < r; ++k) sv += fabs(a.gqb[(bidx * q + i) * r + k]);
@@ -1425,17 +1427,20 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
     }
 }
 
-template <int QMAX>
-__global__ void __launch_bounds__(kBsThreads)
+// NT threads per t-batch: kBsThreads when the t-batches fill the GPU, kBsThreadsFew
+// when they are few (the sample loops and the per-sample reverse sums then
+// spread over more threads; the q x q phases stay on one warp).
+template <int QMAX, int NT>
+__global__ void __launch_bounds__(NT)
     batch_step_f32_kernel(const __grid_constant__ QBatchArgs a, int backward) {
-    batch_step_f32_body<QMAX>(a, backward, blockIdx.x);
+    batch_step_f32_body<QMAX, NT>(a, backward, blockIdx.x);
 }
 
 template <int QMAX>
 __global__ void __launch_bounds__(kBsThreads) batch_step_f32_group_kernel(const GroupTab t) {
     const int m = group_model(t);
     const BstepG& g = static_cast<const BstepG*>(t.args)[m];
-    batch_step_f32_body<QMAX>(g.a, g.backward, blockIdx.x - t.off[m]);
+    batch_step_f32_body<QMAX, kBsThreads>(g.a, g.backward, blockIdx.x - t.off[m]);
 }
 
 #if defined(BGB_QB_STEP)
@@ -1944,19 +1949,28 @@ int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bo
     if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
     int rc = launch_prep_samples(a, stream);
     if (rc) return rc;
-#define BGB_BS(QM)                                                                               \
+    const bool few = a.b < 2 * kNumSMs;
+#define BGB_BS1(QM, NTH)                                                                         \
     do {                                                                                        \
         if (smem > 48 * 1024)                                                                   \
-            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_f32_kernel<QM>,                        \
+            BGB_CUDA_TRY(cudaFuncSetAttribute(batch_step_f32_kernel<QM, NTH>,                   \
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                               (int)smem));                                      \
-        batch_step_f32_kernel<QM><<<(unsigned)a.b, kBsThreads, smem, stream>>>(a, backward);    \
+        batch_step_f32_kernel<QM, NTH><<<(unsigned)a.b, NTH, smem, stream>>>(a, backward);      \
+    } while (0)
+#define BGB_BS(QM)                          \
+    do {                                   \
+        if (few)                           \
+            BGB_BS1(QM, kBsThreadsFew);    \
+        else                               \
+            BGB_BS1(QM, kBsThreads);       \
     } while (0)
     if (a.q <= 4) BGB_BS(4);
     else if (a.q <= 8) BGB_BS(8);
     else if (a.q <= 16) BGB_BS(16);
     else BGB_BS(32);
 #undef BGB_BS
+#undef BGB_BS1
     BGB_CHECK_LAUNCH();
     return BGB_OK;
 }
