@@ -22,11 +22,13 @@
 // algorithms with guaranteed sufficient decrease" (ACM TOMS 20, 1994), with
 // ftol = 1e-3, gtol = 0.9, xtol = 0.1 and the step bounded by the box.
 //
-// Arithmetic differs from scipy's compiled routine only in summation order:
-// the O(m n) dot products are CTA reductions, and the middle matrix of the
-// subspace step is formed from its definition every time the free set changes
-// instead of being updated by the entering and leaving variables. Ties between
-// equal breakpoints are taken in index order.
+// Arithmetic differs from scipy's compiled routine only in summation order and
+// rounding: the O(m n) dot products are CTA reductions, the small factors are
+// applied with reciprocal pivots, and the Gram blocks of the subspace matrix
+// are formed from their definition (rather than updated by the variables that
+// changed sides) after a memory refresh or when more than an eighth of the
+// variables changed sides. Ties between equal breakpoints are taken in index
+// order.
 //
 // The same source compiles for the host with LB_HOST_EMU (one thread, all
 // barriers no-ops): the host build exists only so that tests can step it in
@@ -87,7 +89,7 @@ struct State {
     double ls_stx, ls_sty, ls_stmin, ls_stmax, ls_width, ls_width1;
     int ls_brackt, ls_stage, ls_task;
     int col, head, itail, iupdat, updatd, iter, ifun, iback, nfgv, nfree, nskip, info, wrk;
-    int wait, code, held, pad;
+    int wait, code, held, wn1_valid;  // wn1_valid: the Gram blocks of the subspace matrix are current
     long long nit, nfev;
 };
 
@@ -117,6 +119,7 @@ struct Arrays {
     double* ss;    // S^T S
     double* wt;    // Cholesky factor of theta S^T S + L D^-1 L^T (upper)
     double* wn;    // factor of the subspace middle matrix (2m x 2m, upper)
+    double* wn1;   // its Gram blocks (2m x 2m, lower): Y^T Z Z^T Y, S^T A A^T S, S^T Y split
     int8_t* iwhere;
     int8_t* wasfree;
 };
@@ -126,9 +129,12 @@ struct Shm {
     State s;
     double sy[kMaxM * kMaxM], ss[kMaxM * kMaxM], wt[kMaxM * kMaxM];
     double wn[4 * kMaxM * kMaxM];
+    double wn1[4 * kMaxM * kMaxM];
     double p[2 * kMaxM], c[2 * kMaxM], v[2 * kMaxM], wbp[2 * kMaxM], wv[2 * kMaxM];
     double dots[kMaxM * (2 * kMaxM + 1)];
     double rd[2 * kMaxM], dinv[kMaxM], rsq[kMaxM], rwt[kMaxM];
+    int red_i2[LB_NW];
+    int nenter, nleave;
     double red_d[LB_NW];
     int red_i[LB_NW];
     double f1, f2, f2_org, dtm, tsum, bkmin, alpha, rr, dr;
@@ -144,6 +150,8 @@ struct Ctx {
     int n2;
     double* tile;   // row tiles of S and Y for the Gram sums (kTileRows + 1) x kTileCols
     int8_t* tmask;  // free flags of the tile's rows
+    int* elist;     // variables that entered / left the free set (free_set -> form_k)
+    int* llist;
 };
 
 constexpr int kTileRows = 64;
@@ -460,6 +468,7 @@ LB_FN double proj_grad_norm(Ctx& c) {
 }
 
 LB_FN void reset_memory(State& s) {
+    s.wn1_valid = 0;
     s.info = 0;
     s.col = 0;
     s.head = 0;
@@ -698,26 +707,72 @@ LB_FN int cauchy(Ctx& c) {
     return 0;
 }
 
+// Appends, in increasing k, the k < n with fe(k) to le and those with fl(k)
+// to ll (tile by tile over the CTA, warp ballots for the offsets).
+template <class FE, class FL>
+LB_FN void block_append2(Shm& sh, int n, FE fe, FL fl, int* le, int* ll, int& ne, int& nl) {
+    const int t = lb_tid();
+    int be = 0, bl = 0;
+    for (int k0 = 0; k0 < n; k0 += LB_NT) {
+        const int k = k0 + t;
+        const bool e = k < n && fe(k), l = k < n && fl(k);
+#if defined(LB_HOST_EMU)
+        if (e) le[be] = k;
+        if (l) ll[bl] = k;
+        be += e ? 1 : 0;
+        bl += l ? 1 : 0;
+#else
+        const unsigned me = __ballot_sync(0xffffffffu, e), ml = __ballot_sync(0xffffffffu, l);
+        const unsigned below = (1u << lane_of(t)) - 1u;
+        if (lane_of(t) == 0) {
+            sh.red_i[warp_of(t)] = __popc(me);
+            sh.red_i2[warp_of(t)] = __popc(ml);
+        }
+        LB_SYNC();
+        int oe = be, ol = bl, te = 0, tl = 0;
+        for (int w = 0; w < LB_NW; ++w) {
+            if (w < warp_of(t)) {
+                oe += sh.red_i[w];
+                ol += sh.red_i2[w];
+            }
+            te += sh.red_i[w];
+            tl += sh.red_i2[w];
+        }
+        if (e) le[oe + __popc(me & below)] = k;
+        if (l) ll[ol + __popc(ml & below)] = k;
+        be += te;
+        bl += tl;
+        LB_SYNC();
+#endif
+    }
+    ne = be;
+    nl = bl;
+}
+
 // Free set at the Cauchy point; sets s.nfree and s.wrk (the set changed or
-// the memory was updated).
+// the memory was updated), and the lists of the variables that entered and
+// left it (used to update the subspace matrix's Gram blocks).
 LB_FN void free_set(Ctx& c) {
     const Problem& P = c.P;
     const Arrays& A = c.A;
     Shm& sh = *c.sh;
     const bool count = sh.s.iter > 0 && P.cnstnd;
-    int ne = 0, nf = 0;
+    int ne = 0, nl = 0, nf = 0;
+    if (count)
+        block_append2(
+            sh, P.n, [&](int k) { return A.iwhere[k] <= 0 && A.wasfree[k] == 0; },
+            [&](int k) { return A.iwhere[k] > 0 && A.wasfree[k] != 0; }, c.elist, c.llist, ne, nl);
     for (int k = lb_tid(); k < P.n; k += LB_NT) {
         const bool fr = A.iwhere[k] <= 0;
-        const bool was = A.wasfree[k] != 0;
-        if (count && fr != was) ++ne;
         A.wasfree[k] = fr ? 1 : 0;
         nf += fr ? 1 : 0;
     }
-    ne = block_sum_i(sh, ne);
     nf = block_sum_i(sh, nf);
     if (lb_tid() == 0) {
-        sh.s.wrk = (ne > 0 || sh.s.updatd) ? 1 : 0;
+        sh.s.wrk = (ne + nl > 0 || sh.s.updatd) ? 1 : 0;
         sh.s.nfree = nf;
+        sh.nenter = ne;
+        sh.nleave = nl;
     }
     LB_SYNC();
 }
@@ -727,63 +782,160 @@ LB_FN void free_set(Ctx& c) {
 //       [ -L_a + R_z            theta S^T A A^T S     ]
 // (Z the free, A the active variables; L_a the strictly lower part of S^T A A^T Y,
 // R_z the upper part of S^T Z Z^T Y), as [[R11, R12], [0, R22]] upper in sh.wn.
+// The Gram blocks are kept in wn1 (2m x 2m, column-major, lower):
+//   wn1(i, j)         = y_i^T Z Z^T y_j         (j <= i)
+//   wn1(m + i, m + j) = s_i^T A A^T s_j         (j <= i)
+//   wn1(m + i, j)     = s_i^T A A^T y_j (i > j), s_i^T Z Z^T y_j (i <= j)
+// and, as in the published algorithm, updated from the previous iteration's
+// blocks: the newest pair's row and column over all variables, and the old
+// entries by the variables that entered or left the free set. They are formed
+// from their definition after a memory refresh, when the previous blocks are
+// stale, or when more than an eighth of the variables changed sides.
 LB_FN int form_k(Ctx& c) {
     const Problem& P = c.P;
     const Arrays& A = c.A;
     Shm& sh = *c.sh;
-    const State& s = sh.s;
+    State& s = sh.s;
     const int n = P.n, m = P.m, col = s.col, ld = 2 * P.m;
-    const int J1 = col * (col + 1) / 2;
-    const int J = 2 * J1 + col * col;
-    // staged columns: Y (logical order) then S
-    tiled_gram(J, n, 2 * col,
-               [&](int q) {
-                   return (q < col ? A.wy : A.ws) + (size_t)colptr(s, m, q < col ? q : q - col) * n;
-               },
-               A.iwhere,
-               [&](int o, int& a, int& b, int& mode) {
-                   if (o < 2 * J1) {  // lower triangles of Y^T Z Z^T Y, then S^T A A^T S
-                       const int oo = o < J1 ? o : o - J1;
-                       int i = 0;
-                       while ((i + 1) * (i + 2) / 2 <= oo) ++i;
-                       const int j = oo - i * (i + 1) / 2;
-                       const int base = o < J1 ? 0 : col;
-                       a = base + i;
-                       b = base + j;
-                       mode = o < J1 ? 1 : 2;
-                   } else {  // S^T Y split: active below the diagonal, free on and above
-                       const int oo = o - 2 * J1;
-                       const int i = oo / col, j = oo % col;
-                       a = col + i;
-                       b = j;
-                       mode = i > j ? 2 : 1;
-                   }
-               },
-               c.tile, c.tmask, sh.dots);
+    double* wn1 = sh.wn1;
+    auto wcol = [&](int q) {  // staged columns: Y (logical order) then S
+        return (q < col ? A.wy : A.ws) + (size_t)colptr(s, m, q < col ? q : q - col) * n;
+    };
+    const bool incremental = s.wn1_valid && 8 * (sh.nenter + sh.nleave) <= n;
+    if (!incremental) {
+        const int J1 = col * (col + 1) / 2;
+        const int J = 2 * J1 + col * col;
+        tiled_gram(J, n, 2 * col, wcol, A.iwhere,
+                   [&](int o, int& a, int& b, int& mode) {
+                       if (o < 2 * J1) {  // lower triangles of Y^T Z Z^T Y, then S^T A A^T S
+                           const int oo = o < J1 ? o : o - J1;
+                           int i = 0;
+                           while ((i + 1) * (i + 2) / 2 <= oo) ++i;
+                           const int j = oo - i * (i + 1) / 2;
+                           const int base = o < J1 ? 0 : col;
+                           a = base + i;
+                           b = base + j;
+                           mode = o < J1 ? 1 : 2;
+                       } else {  // S^T Y split: active below the diagonal, free on and above
+                           const int oo = o - 2 * J1;
+                           const int i = oo / col, j = oo % col;
+                           a = col + i;
+                           b = j;
+                           mode = i > j ? 2 : 1;
+                       }
+                   },
+                   c.tile, c.tmask, sh.dots);
+        for (int o = lb_tid(); o < J; o += LB_NT) {
+            if (o < 2 * J1) {
+                const int oo = o < J1 ? o : o - J1;
+                int i = 0;
+                while ((i + 1) * (i + 2) / 2 <= oo) ++i;
+                const int j = oo - i * (i + 1) / 2;
+                const int off = o < J1 ? 0 : m;
+                wn1[(off + i) + (off + j) * ld] = sh.dots[o];
+            } else {
+                const int oo = o - 2 * J1;
+                wn1[(m + oo / col) + (oo % col) * ld] = sh.dots[o];
+            }
+        }
+        LB_SYNC();
+    } else {
+        int upcl = col;
+        if (s.updatd) {
+            if (s.iupdat > m && lb_tid() < LB_WARP) {  // drop the oldest pair's rows and columns
+                for (int jy = 0; jy < m - 1; ++jy) {
+                    for (int i = lane_id(); i < m - 1; i += LB_WARP) {
+                        if (i < m - 1 - jy) {
+                            wn1[(jy + i) + jy * ld] = wn1[(jy + 1 + i) + (jy + 1) * ld];
+                            wn1[(m + jy + i) + (m + jy) * ld] = wn1[(m + jy + 1 + i) + (m + jy + 1) * ld];
+                        }
+                        wn1[(m + i) + jy * ld] = wn1[(m + 1 + i) + (jy + 1) * ld];
+                    }
+                    LB_SYNCWARP();
+                }
+            }
+            LB_SYNC();
+            // the newest pair (logical col - 1) against every pair, over all variables
+            const int nw = col - 1;
+            tiled_gram(4 * col, n, 2 * col, wcol, A.iwhere,
+                       [&](int o, int& a, int& b, int& mode) {
+                           const int j = o % col;
+                           switch (o / col) {
+                               case 0: a = nw; b = j; mode = 1; break;               // y_new^T Z Z^T y_j
+                               case 1: a = col + nw; b = col + j; mode = 2; break;   // s_new^T A A^T s_j
+                               case 2: a = col + nw; b = j; mode = 2; break;         // s_new^T A A^T y_j
+                               default: a = col + j; b = nw; mode = 1; break;        // s_j^T Z Z^T y_new
+                           }
+                       },
+                       c.tile, c.tmask, sh.dots);
+            if (lb_tid() < LB_WARP) {
+                for (int j = lane_id(); j < col; j += LB_WARP) {
+                    wn1[nw + j * ld] = sh.dots[j];
+                    wn1[(m + nw) + (m + j) * ld] = sh.dots[col + j];
+                    if (j < nw) wn1[(m + nw) + j * ld] = sh.dots[2 * col + j];
+                    wn1[(m + j) + nw * ld] = sh.dots[3 * col + j];
+                }
+            }
+            LB_SYNC();
+            upcl = col - 1;
+        }
+        // the old entries: add the entering variables' products, remove the leaving ones'
+        const int np = upcl * (upcl + 1) / 2;
+        const int ne = sh.nenter, nl = sh.nleave;
+        for (int o = lb_tid(); o < 2 * np + upcl * upcl; o += LB_NT) {
+            int i, j;
+            const double *u, *w;
+            double sgn = 1.0;
+            int row, cl;
+            if (o < 2 * np) {
+                const int oo = o < np ? o : o - np;
+                i = 0;
+                while ((i + 1) * (i + 2) / 2 <= oo) ++i;
+                j = oo - i * (i + 1) / 2;
+                const bool ys = o < np;
+                u = (ys ? A.wy : A.ws) + (size_t)colptr(s, m, i) * n;
+                w = (ys ? A.wy : A.ws) + (size_t)colptr(s, m, j) * n;
+                sgn = ys ? 1.0 : -1.0;  // free-set Gram of Y grows with the entering set, S^T A A^T S shrinks
+                row = ys ? i : m + i;
+                cl = ys ? j : m + j;
+            } else {
+                const int oo = o - 2 * np;
+                i = oo / upcl;
+                j = oo % upcl;
+                u = A.ws + (size_t)colptr(s, m, i) * n;
+                w = A.wy + (size_t)colptr(s, m, j) * n;
+                sgn = i <= j ? 1.0 : -1.0;  // R_z: free set; L_a: active set
+                row = m + i;
+                cl = j;
+            }
+            double te = 0.0, tl = 0.0;
+            for (int e = 0; e < ne; ++e) te += u[c.elist[e]] * w[c.elist[e]];
+            for (int e = 0; e < nl; ++e) tl += u[c.llist[e]] * w[c.llist[e]];
+            wn1[row + cl * ld] += sgn * (te - tl);
+        }
+        LB_SYNC();
+    }
     if (lb_tid() < LB_WARP) {
         const int l = lane_id();
         const double theta = s.theta;
         double* wn = sh.wn;
-        const double* yzy = sh.dots;
-        const double* sas = sh.dots + J1;
-        const double* sym = sh.dots + 2 * J1;
         for (int iy = l; iy < col; iy += LB_WARP) {
             const int is = col + iy;
             for (int jy = 0; jy <= iy; ++jy) {
                 const int js = col + jy;
-                wn[jy + iy * ld] = yzy[iy * (iy + 1) / 2 + jy] / theta;
-                wn[js + is * ld] = sas[iy * (iy + 1) / 2 + jy] * theta;
+                wn[jy + iy * ld] = wn1[iy + jy * ld] / theta;
+                wn[js + is * ld] = wn1[(m + iy) + (m + jy) * ld] * theta;
             }
-            for (int jy = 0; jy < iy; ++jy) wn[jy + is * ld] = -sym[iy * col + jy];
-            for (int jy = iy; jy < col; ++jy) wn[jy + is * ld] = sym[iy * col + jy];
+            for (int jy = 0; jy < iy; ++jy) wn[jy + is * ld] = -wn1[(m + iy) + jy * ld];
+            for (int jy = iy; jy < col; ++jy) wn[jy + is * ld] = wn1[(m + iy) + jy * ld];
             wn[iy + iy * ld] += sh.sy[iy + iy * m];
         }
         LB_SYNCWARP();
         int info = warp_chol_upper(wn, ld, col, sh.rd) ? -1 : 0;
         if (!info) {
             warp_solve_upper_t_multi(wn, ld, col, sh.rd, wn + col * ld, ld, col);
-            const int ne = col * (col + 1) / 2;
-            for (int e = l; e < ne; e += LB_WARP) {
+            const int ne2 = col * (col + 1) / 2;
+            for (int e = l; e < ne2; e += LB_WARP) {
                 int jj = 0;
                 while ((jj + 1) * (jj + 2) / 2 <= e) ++jj;
                 const int ii = e - jj * (jj + 1) / 2;
@@ -795,7 +947,10 @@ LB_FN int form_k(Ctx& c) {
             LB_SYNCWARP();
             if (warp_chol_upper(wn + col + col * ld, ld, col, sh.rd + col)) info = -2;
         }
-        if (l == 0) sh.info = info;
+        if (l == 0) {
+            sh.info = info;
+            s.wn1_valid = info == 0 ? 1 : 0;
+        }
     }
     LB_SYNC();
     return sh.info;
@@ -1228,7 +1383,11 @@ LB_FN int iteration(Ctx& c) {
     const int n = P.n, t = lb_tid();
     if (!P.cnstnd && s.col > 0) {
         for (int k = t; k < n; k += LB_NT) A.z[k] = A.x[k];
-        if (t == 0) s.wrk = s.updatd;
+        if (t == 0) {
+            s.wrk = s.updatd;
+            sh.nenter = 0;
+            sh.nleave = 0;
+        }
         LB_SYNC();
     } else {
         if (cauchy(c)) {
@@ -1248,6 +1407,9 @@ LB_FN int iteration(Ctx& c) {
             LB_SYNC();
             return kLIter;
         }
+    } else if (s.wrk) {  // the free set or the pairs changed without the Gram blocks following
+        if (t == 0) s.wn1_valid = 0;
+        LB_SYNC();
     }
     // line search start (lnsrlb before label 556)
     double dtd = 0.0, stpmx = kBig;
@@ -1455,7 +1617,7 @@ inline Layout make_layout(long long R, long long n, int m) {
     L.hi = take(8 * n);
     L.nbd = take(n);
     L.states = take(R * (long long)sizeof(State));
-    const long long doubles = 7 * n + 2 * (long long)m * n + 7 * (long long)m * m;
+    const long long doubles = 7 * n + 2 * (long long)m * n + 11 * (long long)m * m;
     L.per_bytes = lb_align(8 * doubles + 2 * n);
     L.per = off;
     off += R * L.per_bytes;
@@ -1519,7 +1681,8 @@ LB_FN Arrays restart_arrays(const Layout& L, char* ws, double* X, int r, int n, 
     A.ss = A.sy + m * m;
     A.wt = A.ss + m * m;
     A.wn = A.wt + m * m;
-    int8_t* q = reinterpret_cast<int8_t*>(A.wn + 4 * m * m);
+    A.wn1 = A.wn + 4 * m * m;
+    int8_t* q = reinterpret_cast<int8_t*>(A.wn1 + 4 * m * m);
     A.iwhere = q;
     A.wasfree = q + n;
     return A;
@@ -1612,12 +1775,17 @@ LB_FN void step_restart(const StepArgs& a, int r, Shm& sh, unsigned char* dyn, i
     c.n2 = n2;
     c.tile = tile;
     c.tmask = tmask;
+    c.elist = idx;
+    c.llist = reinterpret_cast<int*>(key);
     for (int i = t; i < m * m; i += LB_NT) {
         sh.sy[i] = c.A.sy[i];
         sh.ss[i] = c.A.ss[i];
         sh.wt[i] = c.A.wt[i];
     }
-    for (int i = t; i < 4 * m * m; i += LB_NT) sh.wn[i] = c.A.wn[i];
+    for (int i = t; i < 4 * m * m; i += LB_NT) {
+        sh.wn[i] = c.A.wn[i];
+        sh.wn1[i] = c.A.wn1[i];
+    }
     const double fv = a.sign * a.value[r];
     int bad = isfinite(fv) ? 0 : 1;
     for (int k = t; k < n; k += LB_NT) {
@@ -1642,7 +1810,10 @@ LB_FN void step_restart(const StepArgs& a, int r, Shm& sh, unsigned char* dyn, i
         c.A.ss[i] = sh.ss[i];
         c.A.wt[i] = sh.wt[i];
     }
-    for (int i = t; i < 4 * m * m; i += LB_NT) c.A.wn[i] = sh.wn[i];
+    for (int i = t; i < 4 * m * m; i += LB_NT) {
+        c.A.wn[i] = sh.wn[i];
+        c.A.wn1[i] = sh.wn1[i];
+    }
     if (t == 0) *st = sh.s;
 }
 
