@@ -59,9 +59,10 @@ class DeviceLbfgsb:
         self.lower = torch.as_tensor(lower, dtype=torch.float64, device=self.device).expand(n).contiguous()
         self.upper = torch.as_tensor(upper, dtype=torch.float64, device=self.device).expand(n).contiguous()
         self.summary = torch.zeros(4, dtype=torch.int32, device=self.device)
-        nat.check(lib.bgb_lbfgsb_init(ctypes.byref(self.opts), nat.ptr(X), nat.ptr(self.lower),
-                                      nat.ptr(self.upper), nat.ptr(self.ws), self.ws_bytes,
-                                      nat.stream_handle(self.device)), "bgb_lbfgsb_init")
+        with torch.cuda.device(self.device):
+            nat.check(lib.bgb_lbfgsb_init(ctypes.byref(self.opts), nat.ptr(X), nat.ptr(self.lower),
+                                          nat.ptr(self.upper), nat.ptr(self.ws), self.ws_bytes,
+                                          nat.stream_handle(self.device)), "bgb_lbfgsb_init")
 
     def step(self, value: Tensor, grad: Tensor, sign: float = 1.0, status: Tensor | None = None,
              ignore_status: bool = False) -> None:
@@ -69,10 +70,15 @@ class DeviceLbfgsb:
         capturable in a CUDA graph. ``status`` (int32 per row, 0 = good): unless
         ``ignore_status``, a nonzero entry anywhere holds every restart back (the
         summary's second count) so the caller can re-evaluate first."""
-        nat.check(nat.lib().bgb_lbfgsb_step(ctypes.byref(self.opts), nat.ptr(self.X), nat.ptr(value), float(sign),
-                                            nat.ptr(grad), nat.ptr(status), int(bool(ignore_status)),
-                                            nat.ptr(self.ws), self.ws_bytes, nat.ptr(self.summary),
-                                            nat.stream_handle(self.device)), "bgb_lbfgsb_step")
+        if value.device != self.device or grad.device != self.device or (
+                status is not None and status.device != self.device):
+            raise ValueError("value, grad and status must be on the optimiser's device")
+        with torch.cuda.device(self.device):
+            nat.check(nat.lib().bgb_lbfgsb_step(ctypes.byref(self.opts), nat.ptr(self.X), nat.ptr(value),
+                                                float(sign), nat.ptr(grad), nat.ptr(status),
+                                                int(bool(ignore_status)), nat.ptr(self.ws), self.ws_bytes,
+                                                nat.ptr(self.summary), nat.stream_handle(self.device)),
+                      "bgb_lbfgsb_step")
 
     def results(self) -> dict:
         """Per restart: f at its row of X, iterations, evaluations, stop code and message."""
@@ -81,9 +87,10 @@ class DeviceLbfgsb:
         nit = torch.empty(R, dtype=torch.int64, device=self.device)
         nfev = torch.empty(R, dtype=torch.int64, device=self.device)
         code = torch.empty(R, dtype=torch.int32, device=self.device)
-        nat.check(nat.lib().bgb_lbfgsb_results(ctypes.byref(self.opts), nat.ptr(self.ws), self.ws_bytes,
-                                               nat.ptr(f), nat.ptr(nit), nat.ptr(nfev), nat.ptr(code),
-                                               nat.stream_handle(self.device)), "bgb_lbfgsb_results")
+        with torch.cuda.device(self.device):
+            nat.check(nat.lib().bgb_lbfgsb_results(ctypes.byref(self.opts), nat.ptr(self.ws), self.ws_bytes,
+                                                   nat.ptr(f), nat.ptr(nit), nat.ptr(nfev), nat.ptr(code),
+                                                   nat.stream_handle(self.device)), "bgb_lbfgsb_results")
         codes = code.cpu().tolist()
         return {"fun": f.cpu(), "nit": nit.cpu(), "nfev": nfev.cpu(), "code": codes,
                 "message": [nat.BGB_LBFGSB_MESSAGES.get(c, str(c)) for c in codes]}
