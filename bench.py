@@ -56,6 +56,8 @@ def parse():
                    help="only warm up and run --steps mixed-precision steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     p.add_argument("--simt", action="store_true", help="FFMA GEMMs instead of tcgen05")
+    p.add_argument("--profile-raw", action="store_true",
+                   help="with --config optimize --profile: one raw-sample chunk instead of one round")
     p.add_argument("--profile-precision", default="mixed", choices=["mixed", "fp64"],
                    help="the path --profile runs (fp64: the plain float64 kernels)")
     p.add_argument("--config", default="headline",
@@ -559,6 +561,16 @@ def run_optimize(args) -> None:
     t2 = time.perf_counter()
     X0, _ = initialize_q_batch(X_raw.to(device), v_raw, restarts, eta=1.0,
                                generator=torch.Generator(device=device).manual_seed(0))
+    if args.profile and args.profile_raw:  # one forward-only chunk of the raw-sample evaluation
+        Xc = X_raw[:4096].to(device, torch.float64).contiguous()
+        acqf.value_and_grad_raw(Xc, False, check=False)
+        torch.cuda.synchronize(device)
+        torch.cuda.profiler.start()
+        acqf.value_and_grad_raw(Xc, False, check=False)
+        torch.cuda.synchronize(device)
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_raw_chunk": 4096}))
+        return
     if args.profile:  # one round (evaluation + device L-BFGS-B step) inside the profiler range
         from botorch_gb300.lbfgsb import DeviceLbfgsb
 
