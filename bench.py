@@ -546,6 +546,7 @@ def run_optimize(args) -> None:
     bounds = torch.stack([torch.zeros(d), torch.ones(d)]).double()
     # warm-up of the shapes and torch kernels used below (library set-up, graph
     # capture, the first use of torch's sampling kernels)
+    bounds = bounds.to(device)  # raw samples drawn on the device
     Xr_w = draw_sobol_samples(bounds, 4096, q, seed=1)
     vr_w = evaluate_raw(acqf, Xr_w, 4096)
     initialize_q_batch(Xr_w.to(device), vr_w, restarts, eta=1.0,

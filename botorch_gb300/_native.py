@@ -166,6 +166,7 @@ _SIGNATURES = {
                                            c_vp]),
     "bgb_log_areas_backward_jac_f32": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp,
                                                c_vp]),
+    "bgb_sobol_box": (c_i32, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i64, c_i64, c_vp, c_vp, c_i32, c_vp, c_vp]),
     "bgb_launch_count": (ctypes.c_ulonglong, []),
 }
 

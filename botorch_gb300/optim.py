@@ -42,11 +42,29 @@ from botorch_gb300._lbfgsb_rc import lbfgsb_rc as _lbfgsb_rc
 
 
 def draw_sobol_samples(bounds: Tensor, n: int, q: int, seed: int | None = None) -> Tensor:
-    """``n x q x d`` scrambled-Sobol points in the box ``bounds`` (2 x d)."""
+    """``n x q x d`` scrambled-Sobol points in the box ``bounds`` (2 x d), on
+    ``bounds``' device (botorch/utils/sampling.py:74-111).
+
+    The engine is torch's ``SobolEngine(q * d, scramble=True, seed)``. For
+    float64 bounds on a CUDA device its state is built on the host and the
+    points are generated and mapped to the box on the device (``bgb_sobol_box``),
+    bit for bit what the engine's draw and the elementwise map give on the host."""
     d = bounds.shape[-1]
     engine = torch.quasirandom.SobolEngine(q * d, scramble=True, seed=seed)
-    raw = engine.draw(n, dtype=bounds.dtype).view(n, q, d).to(bounds.device)
     lo, hi = bounds[0], bounds[1]
+    if bounds.device.type == "cuda" and bounds.dtype == torch.float64 and n > 0:
+        dev = bounds.device
+        state = engine.sobolstate.to(dev).contiguous()
+        shift = engine.shift.to(dev).contiguous()
+        first_point = engine._first_point.to(torch.float64).reshape(-1).to(dev).contiguous()
+        lo_d, hi_d = lo.contiguous(), hi.contiguous()
+        out = torch.empty(n, q, d, dtype=torch.float64, device=dev)
+        with torch.cuda.device(dev):
+            nat.check(nat.lib().bgb_sobol_box(nat.ptr(state), nat.ptr(shift), nat.ptr(first_point), q * d,
+                                              engine.MAXBIT, 0, n, nat.ptr(lo_d), nat.ptr(hi_d), d, nat.ptr(out),
+                                              nat.stream_handle(dev)), "bgb_sobol_box")
+        return out
+    raw = engine.draw(n, dtype=bounds.dtype).view(n, q, d).to(bounds.device)
     return lo + (hi - lo) * raw
 
 
@@ -473,7 +491,7 @@ def optimize_acqf(acq_function, bounds: Tensor, q: int, num_restarts: int, raw_s
     batch_limit = int(options.pop("batch_limit", 4096))
     eta = float(options.pop("eta", 1.0))
     bounds = bounds.to(torch.float64)
-    X_raw = draw_sobol_samples(bounds.cpu(), raw_samples, q, seed=seed)
+    X_raw = draw_sobol_samples(bounds.to(acq_function.device), raw_samples, q, seed=seed)
     v_raw = evaluate_raw(acq_function, X_raw, batch_limit)
     g = None if seed is None else torch.Generator(device=v_raw.device).manual_seed(seed)
     X0, _ = initialize_q_batch(X_raw.to(v_raw.device), v_raw, num_restarts, eta=eta, generator=g)

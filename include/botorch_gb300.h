@@ -504,6 +504,20 @@ int bgb_lbfgsb_step(const bgb_lbfgsb_opts* opts, double* X, const double* value,
 int bgb_lbfgsb_results(const bgb_lbfgsb_opts* opts, const void* workspace, size_t workspace_bytes,
                        double* f, int64_t* nit, int64_t* nfev, int32_t* code, void* stream);
 
+/* ---- Scrambled Sobol points mapped to a box (the raw samples of the
+ * acquisition optimisation: botorch/utils/sampling.py:74-111, draw_sobol_samples,
+ * which draws torch.quasirandom.SobolEngine(q * d, scramble=True, seed) on the
+ * host). The engine's state comes from the host: `state` (dim x maxbit int64,
+ * its scrambled direction numbers), `shift` (dim int64, its digital shift) and
+ * `first_point` (dim doubles: point 0 as the engine returns it). Writes points
+ * first .. first + n - 1 of the sequence, mapped to lower + (upper - lower) * u
+ * with the bounds repeating every `period` dimensions (dim % period == 0), as
+ * out (n x dim, row-major), bit for bit what the engine's draw followed by the
+ * elementwise map gives in float64. first + n <= 2^maxbit. */
+int bgb_sobol_box(const int64_t* state, const int64_t* shift, const double* first_point, int32_t dim,
+                  int32_t maxbit, int64_t first, int64_t n, const double* lower, const double* upper,
+                  int32_t period, double* out, void* stream);
+
 /* Number of kernel launches this library has issued in the process so far.
  * Measurement aid; no reference counterpart. */
 unsigned long long bgb_launch_count(void);

@@ -59,3 +59,17 @@ def test_per_restart_and_aggregated_modes(cuda_lib):
     Xa, va = gen_candidates_scipy(X0, acqf, 0.0, 1.0, {"maxiter": 20}, use_parallel_mode=False)
     assert gen_candidates_scipy.last_info["mode"] == "aggregated"
     assert float(va.sum()) >= float(v0.sum()) - 1e-9
+
+
+@pytest.mark.parametrize("n,q,d,seed", [(1, 2, 3, 0), (257, 16, 50, 0), (1000, 3, 7, 11)])
+def test_device_sobol_samples_equal_the_host_engine(cuda_lib, n, q, d, seed):
+    """The raw samples drawn on the device are, bit for bit, torch's SobolEngine
+    draw mapped to the box on the host (the reference's draw_sobol_samples)."""
+    g = torch.Generator().manual_seed(seed + 1)
+    lo = -torch.rand(d, generator=g, dtype=torch.float64)
+    hi = lo + 0.5 + torch.rand(d, generator=g, dtype=torch.float64)
+    bounds = torch.stack([lo, hi])
+    host = draw_sobol_samples(bounds, n, q, seed=seed)
+    dev = draw_sobol_samples(bounds.to(DEV), n, q, seed=seed)
+    assert dev.device.type == "cuda" and dev.shape == (n, q, d)
+    assert torch.equal(dev.cpu(), host)
