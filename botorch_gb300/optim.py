@@ -308,66 +308,97 @@ _DEVICE_LBFGSB_OPTIONS = ("maxcor", "ftol", "gtol", "maxls", "maxfun")
 
 
 def _per_restart_device(acqf, X0: Tensor, lo: np.ndarray, hi: np.ndarray, maxiter: int, options: dict,
-                        use_graph: bool):
+                        use_graph: bool, groups: int | None = None):
     """Each restart's own L-BFGS-B with its state on the device (``DeviceLbfgsb``):
-    a round is one batched evaluation of all restarts, one step launch and a
+    a round is one batched evaluation of the restarts, one step launch and a
     four-integer summary read by the host (the round captured in one CUDA graph).
-    A round whose evaluation reports a failed t-batch is evaluated again through
-    the acquisition function's checked call (its fallback route, or its error)
-    before the restarts consume it. Returns the points, the per-restart results
-    and the rounds."""
+    ``groups`` > 1 cuts the restarts into groups whose rounds run on their own
+    streams, so that one group's L-BFGS-B step (one CTA per restart) can overlap
+    another's evaluation; restarts are independent, so each one's path does not
+    depend on the grouping beyond rounding. (At 64 restarts of q = 16 two
+    groups gave 0.887 ms per round against 0.873 ms for one: the default is
+    one.) A group whose evaluation reports a failed t-batch is evaluated again
+    through the acquisition function's checked call (its fallback route, or its
+    error) before its restarts consume it. Returns the points, the per-restart
+    results and the rounds."""
     from botorch_gb300.lbfgsb import DeviceLbfgsb
 
     b, q, d = X0.shape
     dev = X0.device
     X = X0.reshape(b, q * d).to(torch.float64).contiguous().clone()
-    Xv = X.view(b, q, d)
-    lb = DeviceLbfgsb(X, torch.from_numpy(np.tile(lo, q)), torch.from_numpy(np.tile(hi, q)), maxiter=maxiter,
-                      **{k: options[k] for k in _DEVICE_LBFGSB_OPTIONS if k in options})
-    value = torch.empty(b, dtype=torch.float64, device=dev)
-    grad = torch.empty(b, q, d, dtype=torch.float64, device=dev)
-    status = torch.zeros(b, dtype=torch.int32, device=dev)
-    acq_ws = nat.Workspace(dev)
-    host = torch.zeros(4, dtype=torch.int32).pin_memory()
+    ng = groups if groups is not None else 1
+    ng = max(1, min(ng, b))
+    bounds_lo, bounds_hi = torch.from_numpy(np.tile(lo, q)), torch.from_numpy(np.tile(hi, q))
+    lb_opts = {k: options[k] for k in _DEVICE_LBFGSB_OPTIONS if k in options}
+    cut = [b * g // ng for g in range(ng + 1)]
+    G = []
+    for g in range(ng):
+        Xg = X[cut[g]:cut[g + 1]]
+        bg = cut[g + 1] - cut[g]
+        G.append(dict(Xv=Xg.view(bg, q, d), lb=DeviceLbfgsb(Xg, bounds_lo, bounds_hi, maxiter=maxiter, **lb_opts),
+                      value=torch.empty(bg, dtype=torch.float64, device=dev),
+                      grad=torch.empty(bg, q, d, dtype=torch.float64, device=dev),
+                      status=torch.zeros(bg, dtype=torch.int32, device=dev), ws=nat.Workspace(dev),
+                      host=torch.zeros(4, dtype=torch.int32).pin_memory(),
+                      stream=torch.cuda.Stream(dev) if ng > 1 else torch.cuda.current_stream(dev),
+                      graph=None, active=True))
 
-    def round_body():
-        acqf.value_and_grad_raw(Xv, True, check=False, out=(value, grad, status), ws=acq_ws)
-        lb.step(value, grad, sign=-1.0, status=status)
-        host.copy_(lb.summary, non_blocking=True)
+    def round_body(gr):
+        acqf.value_and_grad_raw(gr["Xv"], True, check=False, out=(gr["value"], gr["grad"], gr["status"]),
+                                ws=gr["ws"])
+        gr["lb"].step(gr["value"], gr["grad"], sign=-1.0, status=gr["status"])
+        gr["host"].copy_(gr["lb"].summary, non_blocking=True)
 
-    graph = None
+    main = torch.cuda.current_stream(dev)
+    for gr in G:
+        gr["stream"].wait_stream(main)
     if use_graph:
-        # set up the acquisition's state for this shape, then capture one round
-        side = torch.cuda.Stream(dev)
-        side.wait_stream(torch.cuda.current_stream(dev))
-        with torch.cuda.stream(side):
-            acqf.value_and_grad_raw(Xv, True, check=False, out=(value, grad, status), ws=acq_ws)
-        torch.cuda.current_stream(dev).wait_stream(side)
-        torch.cuda.synchronize(dev)
-        graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph):
-            round_body()
-    stream = torch.cuda.current_stream(dev)
+        for gr in G:
+            # set up the acquisition's state for this shape, then capture one round
+            side = torch.cuda.Stream(dev)
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                acqf.value_and_grad_raw(gr["Xv"], True, check=False, out=(gr["value"], gr["grad"], gr["status"]),
+                                        ws=gr["ws"])
+            main.wait_stream(side)
+            torch.cuda.synchronize(dev)
+            gr["graph"] = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gr["graph"]):
+                round_body(gr)
     rounds = 0
-    while True:
-        if graph is not None:
-            graph.replay()
-        else:
-            round_body()
-        stream.synchronize()
+    while any(gr["active"] for gr in G):
+        live = [gr for gr in G if gr["active"]]
+        for gr in live:
+            with torch.cuda.stream(gr["stream"]):
+                if gr["graph"] is not None:
+                    gr["graph"].replay()
+                else:
+                    round_body(gr)
+        for gr in live:
+            gr["stream"].synchronize()
         rounds += 1
-        act, held, nonfin = int(host[0]), int(host[1]), int(host[2])
-        if held:
-            v, g = acqf.value_and_grad_raw(Xv, True)
-            lb.step(v.contiguous(), g.contiguous(), sign=-1.0, ignore_status=True)
-            host.copy_(lb.summary, non_blocking=True)
-            stream.synchronize()
-            act, nonfin = int(host[0]), int(host[2])
-        if nonfin:
-            raise RuntimeError("the acquisition value or its gradient is not finite (NaN elements of the gradient)")
-        if act == 0:
-            break
-    return Xv, lb.results(), rounds
+        for gr in live:
+            host = gr["host"]
+            act, held, nonfin = int(host[0]), int(host[1]), int(host[2])
+            if held:
+                with torch.cuda.stream(gr["stream"]):
+                    v, g = acqf.value_and_grad_raw(gr["Xv"], True)
+                    gr["lb"].step(v.contiguous(), g.contiguous(), sign=-1.0, ignore_status=True)
+                    host.copy_(gr["lb"].summary, non_blocking=True)
+                gr["stream"].synchronize()
+                act, nonfin = int(host[0]), int(host[2])
+            if nonfin:
+                raise RuntimeError("the acquisition value or its gradient is not finite "
+                                   "(NaN elements of the gradient)")
+            gr["active"] = act > 0
+    main.wait_stream(G[-1]["stream"])
+    for gr in G:
+        main.wait_stream(gr["stream"])
+    res = [gr["lb"].results() for gr in G]
+    merged = {"fun": torch.cat([r["fun"] for r in res]), "nit": torch.cat([r["nit"] for r in res]),
+              "nfev": torch.cat([r["nfev"] for r in res]), "code": sum((r["code"] for r in res), []),
+              "message": sum((r["message"] for r in res), [])}
+    return X.view(b, q, d), merged, rounds
 
 
 def _per_restart_lbfgsb(acqf, x0: np.ndarray, lo: np.ndarray, hi: np.ndarray, shape, maxiter: int,
