@@ -69,7 +69,7 @@ enum : int { kStopped = 0, kWaitFgStart = 1, kWaitFgLn = 2 };
 // Line-search task.
 enum : int { kLsStart = 0, kLsFg = 1, kLsConv = 2, kLsWarn = 3, kLsError = 4 };
 // Control labels of the state machine.
-enum : int { kLIter = 0, kLFgStart = 1, kLLsCont = 2, kLNewX = 3, kLExit = 4 };
+enum : int { kLIter = 0, kLNewX = 1, kLExit = 2 };
 
 // Stop codes (mirror the include file's BGB_LBFGSB_*).
 enum : int {
@@ -137,8 +137,8 @@ struct Shm {
     int nenter, nleave;
     double red_d[LB_NW];
     int red_i[LB_NW];
-    double f1, f2, f2_org, dtm, tsum, bkmin, alpha, rr, dr;
-    int nbreak, nfree_dec, unbnded, ibkmin, need_walk, to999, iword, ibd, info, label, trial;
+    double f1, f2, f2_org, dtm, tsum, dr;
+    int need_walk, to999, info, label, trial;
 };
 
 struct Ctx {
@@ -611,8 +611,6 @@ LB_FN int cauchy(Ctx& c) {
             sh.f2 = f2;
             sh.dtm = -f1 / f2;
             sh.tsum = 0.0;
-            sh.nbreak = nbreak;
-            sh.bkmin = bk;
             sh.need_walk = (nbreak > 0 && !(-f1 / f2 < bk)) ? 1 : 0;
             sh.to999 = 0;
         }
@@ -1488,7 +1486,6 @@ LB_FN int new_x(Ctx& c) {
             ddum = -s.gdold * stp;
         }
         sh.dr = dr;
-        sh.rr = rr;
         if (dr <= kEpsMch * ddum) {
             ++s.nskip;
             s.updatd = 0;

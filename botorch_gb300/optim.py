@@ -391,7 +391,6 @@ def _per_restart_device(acqf, X0: Tensor, lo: np.ndarray, hi: np.ndarray, maxite
                 raise RuntimeError("the acquisition value or its gradient is not finite "
                                    "(NaN elements of the gradient)")
             gr["active"] = act > 0
-    main.wait_stream(G[-1]["stream"])
     for gr in G:
         main.wait_stream(gr["stream"])
     res = [gr["lb"].results() for gr in G]
