@@ -562,15 +562,16 @@ def run_optimize(args) -> None:
     t2 = time.perf_counter()
     X0, _ = initialize_q_batch(X_raw.to(device), v_raw, restarts, eta=1.0,
                                generator=torch.Generator(device=device).manual_seed(0))
-    if args.profile and args.profile_raw:  # one forward-only chunk of the raw-sample evaluation
+    if args.profile and args.profile_raw:  # the raw samples' draw and one forward-only chunk
         Xc = X_raw[:4096].to(device, torch.float64).contiguous()
         acqf.value_and_grad_raw(Xc, False, check=False)
         torch.cuda.synchronize(device)
         torch.cuda.profiler.start()
+        draw_sobol_samples(bounds, raw, q, seed=0)
         acqf.value_and_grad_raw(Xc, False, check=False)
         torch.cuda.synchronize(device)
         torch.cuda.profiler.stop()
-        print(json.dumps({"profile_raw_chunk": 4096}))
+        print(json.dumps({"profile_raw_draw": raw, "profile_raw_chunk": 4096}))
         return
     if args.profile:  # one round (evaluation + device L-BFGS-B step) inside the profiler range
         from botorch_gb300.lbfgsb import DeviceLbfgsb
