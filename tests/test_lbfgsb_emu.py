@@ -101,7 +101,10 @@ def assert_same_run(out, x_tol=1e-12):
     for i in range(R):
         ref = out["ref"][i]
         assert out["nit"][i] == ref["nit"] and out["nfev"][i] == ref["nfev"], (i, out["nit"][i], ref)
-        assert abs(out["f"][i] - ref["fun"]) <= 1e-13 * max(1.0, abs(ref["fun"]))
+        if ref_code(ref["message"]) != 3:
+            # (after a failed line search scipy's driver reports the last trial's f
+            # beside the restored x; the device keeps f at x)
+            assert abs(out["f"][i] - ref["fun"]) <= 1e-13 * max(1.0, abs(ref["fun"]))
         assert out["code"][i] == ref_code(ref["message"]), (out["code"][i], ref["message"])
 
 
@@ -232,3 +235,44 @@ def test_non_finite_values_stop_the_restart_and_status_holds_the_round(emu):
     code = np.zeros(R, np.int32)
     emu.emu_results(R, n, m, P(ws), P(np.zeros(R)), P(np.zeros(R, np.int64)), P(np.zeros(R, np.int64)), P(code))
     assert code.tolist() == [0, 6, 0]
+
+
+@pytest.mark.parametrize("case", ["scalar", "history_one", "history_twenty", "one_trial", "all_fixed",
+                                  "start_on_bounds", "zero_gradient"])
+def test_edge_cases_match_scipy(emu, case):
+    """Edge cases of the sizes, the options and the starting points."""
+    rng = np.random.default_rng(7)
+    opts = {}
+    if case == "scalar":
+        n = 1
+        lo, hi = np.array([-2.0]), np.array([3.0])
+
+        def fg(x):
+            return float((x[0] - 1.3) ** 4 + np.cos(3 * x[0])), np.array([4 * (x[0] - 1.3) ** 3 - 3 * np.sin(3 * x[0])])
+
+        x0 = rng.uniform(-2, 3, (4, n))
+    else:
+        n = 24
+        lo, hi = np.zeros(n), np.ones(n)
+        A, c = rng.uniform(0.5, 4, n), rng.uniform(-0.5, 1.5, n)
+
+        def fg(x):
+            return (float(np.sum(A * (x - c) ** 2) + 0.2 * np.sum(np.sin(5 * x))),
+                    2 * A * (x - c) + np.cos(5 * x))
+
+        x0 = rng.uniform(0, 1, (4, n))
+        if case == "history_one":
+            opts["m"] = 1
+        elif case == "history_twenty":
+            opts["m"] = 20
+        elif case == "one_trial":
+            opts["maxls"] = 1
+        elif case == "all_fixed":
+            hi = lo.copy()
+        elif case == "start_on_bounds":
+            x0 = np.where(rng.uniform(size=x0.shape) < 0.5, 0.0, 1.0)
+        elif case == "zero_gradient":
+            def fg(x):  # noqa: F811 - flat objective
+                return 1.5, np.zeros_like(x)
+    out = lockstep(emu, fg, x0, lo, hi, **opts)
+    assert_same_run(out, x_tol=1e-10)
