@@ -1428,8 +1428,9 @@ __device__ __forceinline__ void batch_step_f32_body(const QBatchArgs& a, int bac
 }
 
 // NT threads per t-batch: kBsThreads when the t-batches fill the GPU, kBsThreadsFew
-// when they are few (the sample loops and the per-sample reverse sums then
-// spread over more threads; the q x q phases stay on one warp).
+// when they are few and each has many samples (the sample loops and the
+// per-sample reverse sums then spread over more threads; the q x q phases stay
+// on one warp).
 template <int QMAX, int NT>
 __global__ void __launch_bounds__(NT)
     batch_step_f32_kernel(const __grid_constant__ QBatchArgs a, int backward) {
@@ -1949,7 +1950,9 @@ int launch_batch_step(const QBatchArgs& a, int backward, cudaStream_t stream, bo
     if (smem > 200 * 1024) return BGB_ERR_UNSUPPORTED;
     int rc = launch_prep_samples(a, stream);
     if (rc) return rc;
-    const bool few = a.b < 2 * kNumSMs;
+    // few t-batches with many samples each: 256 threads per t-batch (small q x S
+    // problems keep 64: their fixed per-CTA costs grow with the CTA)
+    const bool few = a.b < 2 * kNumSMs && (int64_t)a.S * a.q >= 4096;
 #define BGB_BS1(QM, NTH)                                                                         \
     do {                                                                                        \
         if (smem > 48 * 1024)                                                                   \
