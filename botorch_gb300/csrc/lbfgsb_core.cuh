@@ -1746,7 +1746,7 @@ LB_FN void step_restart(const StepArgs& a, int r, Shm& sh, unsigned char* dyn, i
     if (!a.ignore_status && a.status != nullptr) {
         int bad = 0;
         for (long long i = t; i < a.R; i += LB_NT) bad += a.status[i] != 0;
-        if (block_sum_i(sh, bad) > 0) {  // the caller re-evaluates this round first
+        if (block_sum_i(sh, bad) > 0) {  // the caller evaluates these points again first
             if (t == 0) st->held = 1;
             return;
         }
