@@ -222,3 +222,52 @@ def test_device_driver_groups_agree(cuda_lib):
     assert [int(v) for v in r1["nit"]] == [int(v) for v in r2["nit"]]
     assert float((X1 - X2).abs().max()) <= 1e-8
     assert float((r1["fun"] - r2["fun"]).abs().max()) <= 1e-10
+
+
+class _FlakyObjective:
+    """A stand-in acquisition function (a smooth bowl) whose batched call
+    reports a failed t-batch in chosen rounds; its checked call (the fallback
+    route) returns the same, correct values."""
+
+    def __init__(self, bad_calls):
+        self.device = DEV
+        self.bad_calls = set(bad_calls)
+        self.calls = 0
+        self.checked = 0
+
+    def value_and_grad_raw(self, Xd, need_grad, check=None, out=None, ws=None):
+        w = torch.arange(1, Xd.shape[-1] + 1, dtype=torch.float64, device=Xd.device) ** 2
+        v = -(w * (Xd - 0.3) ** 2 + 0.05 * torch.sin(7 * Xd)).sum((-1, -2))
+        g = -(2.0 * w * (Xd - 0.3) + 0.35 * torch.cos(7 * Xd))
+        if out is None:
+            if need_grad:
+                self.checked += 1
+            return v, (g if need_grad else None)
+        value, grad, status = out
+        value.copy_(v)
+        grad.copy_(g)
+        status.zero_()
+        if self.calls in self.bad_calls:
+            status[0] = 1  # the batched call failed for one t-batch
+            value[0] = float("nan")
+        self.calls += 1
+        return value, grad
+
+
+def test_device_driver_reevaluates_held_rounds(cuda_lib):
+    """A round whose batched evaluation reports a failed t-batch is held back,
+    evaluated again through the checked call, and then consumed: the optimisation
+    ends where the one without failures ends."""
+    from botorch_gb300.optim import _per_restart_device
+
+    g = torch.Generator().manual_seed(2)
+    X0 = torch.rand(5, 2, 3, generator=g, dtype=torch.float64).to(DEV)
+    lo, hi = np.zeros(3), np.ones(3)
+    clean = _FlakyObjective([])
+    Xc, rc, nc = _per_restart_device(clean, X0, lo, hi, 50, {}, False)
+    assert nc >= 4
+    flaky = _FlakyObjective([0, 1, 3])
+    Xf, rf, nf = _per_restart_device(flaky, X0, lo, hi, 50, {}, False)
+    assert flaky.checked == 3  # each held round evaluated once more through the checked call
+    assert nf == nc and torch.equal(Xf, Xc)
+    assert [int(v) for v in rf["nit"]] == [int(v) for v in rc["nit"]]
