@@ -168,6 +168,7 @@ LB_FN double warp_sum(double v) { return v; }
 LB_FN int warp_sum_i(int v) { return v; }
 LB_FN double warp_max(double v) { return v; }
 LB_FN void warp_argmin(double&, int&) {}
+LB_FN double group_sum(double v, int) { return v; }
 #else
 LB_FN int lb_tid() { return threadIdx.x; }
 LB_FN double warp_sum(double v) {
@@ -183,6 +184,12 @@ LB_FN double warp_max(double v) {
         double w = __shfl_xor_sync(0xffffffffu, v, o);
         v = w > v ? w : v;
     }
+    return v;
+}
+// Sum over aligned groups of g lanes (g a power of two <= 32); every lane of the
+// warp calls it.
+LB_FN double group_sum(double v, int g) {
+    for (int o = g / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 LB_FN void warp_argmin(double& v, int& i) {
@@ -285,16 +292,22 @@ LB_FN void warp_dots(int J, int n, const int8_t* iwhere, Setup setup, double* ou
 // o < J, where a_o and b_o are among ncols <= kTileCols columns (column c at
 // col(c)) staged tile by tile in shared memory, so that each column is read
 // from memory once per 4 * LB_NT outputs: pair(o, ia, ib, mode) names them.
+// With few outputs (the newest pair's products) g consecutive lanes share one,
+// each summing every g-th row of a tile, and their sums are added at the end:
+// the chain of dependent float64 adds per thread is n / g long instead of n.
 template <class Col, class Pair>
 LB_FN void tiled_gram(int J, int n, int ncols, Col col, const int8_t* iwhere, Pair pair, double* tile,
                       int8_t* tmask, double* out) {
     const int t = lb_tid();
     constexpr int ld = kTileRows + 1;  // (odd stride: the columns start in different banks)
-    for (int o0 = 0; o0 < J; o0 += 4 * LB_NT) {
+    int g = 1;
+    while (g < LB_WARP && 2 * J * g <= LB_NT) g *= 2;
+    const int sub = t % g, tg = t / g, ng = LB_NT / g;
+    for (int o0 = 0; o0 < J; o0 += 4 * ng) {
         int ia[4], ib[4], md[4];
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
         for (int q = 0; q < 4; ++q) {
-            const int o = o0 + t + q * LB_NT;
+            const int o = o0 + tg + q * ng;
             ia[q] = ib[q] = md[q] = -1;
             if (o < J) pair(o, ia[q], ib[q], md[q]);
         }
@@ -312,14 +325,16 @@ LB_FN void tiled_gram(int J, int n, int ncols, Col col, const int8_t* iwhere, Pa
                 const double* b = tile + ib[q] * ld;
                 const int8_t want = md[q] == 1 ? 1 : 0;
                 double sum = 0.0;
-                for (int r = 0; r < rows; ++r)
+                for (int r = sub; r < rows; r += g)
                     if (tmask[r] == want) sum += a[r] * b[r];
                 acc[q] += sum;
             }
             LB_SYNC();
         }
-        for (int q = 0; q < 4; ++q)
-            if (ia[q] >= 0) out[o0 + t + q * LB_NT] = acc[q];
+        for (int q = 0; q < 4; ++q) {
+            acc[q] = group_sum(acc[q], g);  // (every lane: g divides the warp)
+            if (sub == 0 && ia[q] >= 0) out[o0 + tg + q * ng] = acc[q];
+        }
     }
     LB_SYNC();
 }
